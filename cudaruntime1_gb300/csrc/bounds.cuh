@@ -1,0 +1,60 @@
+// bounds.cuh -- lower bounds (upper bounds for LCSS) used to prune pairs
+// before the exact computation.  Every bound is computed with directed
+// rounding toward the safe side, so in FP32 it never exceeds the exact
+// (real-number) value of the measure and a true neighbour is never pruned.
+#pragma once
+#include "tsim_internal.cuh"
+
+namespace tsim {
+
+// |a - b| rounded down
+__device__ __forceinline__ float absdiff_rd(float a, float b) {
+  return a >= b ? __fsub_rd(a, b) : __fsub_rd(b, a);
+}
+
+// squared point distance, rounded down
+__device__ __forceinline__ float pd2_rd(float ax, float ay, float bx, float by) {
+  float dx = absdiff_rd(ax, bx), dy = absdiff_rd(ay, by);
+  return __fadd_rd(__fmul_rd(dx, dx), __fmul_rd(dy, dy));
+}
+
+// squared distance from point (x, y) to box (x0, y0, x1, y1), rounded down
+__device__ __forceinline__ float box_pt_d2_rd(float x0, float y0, float x1, float y1, float x,
+                                              float y) {
+  float dx = x < x0 ? __fsub_rd(x0, x) : (x > x1 ? __fsub_rd(x, x1) : 0.0f);
+  float dy = y < y0 ? __fsub_rd(y0, y) : (y > y1 ? __fsub_rd(y, y1) : 0.0f);
+  return __fadd_rd(__fmul_rd(dx, dx), __fmul_rd(dy, dy));
+}
+
+// squared distance between two boxes (x0, y0, x1, y1), rounded down
+__device__ __forceinline__ float box_box_d2_rd(float4 a, float4 b) {
+  float dx = a.x > b.z ? __fsub_rd(a.x, b.z) : (b.x > a.z ? __fsub_rd(b.x, a.z) : 0.0f);
+  float dy = a.y > b.w ? __fsub_rd(a.y, b.w) : (b.y > a.w ? __fsub_rd(b.y, a.w) : 0.0f);
+  return __fadd_rd(__fmul_rd(dx, dx), __fmul_rd(dy, dy));
+}
+
+// Floor division with a non-negative remainder, for incremental stepping.
+struct FloorDiv {
+  int q, r, d;
+  __device__ __forceinline__ void init(long long num, int den) {
+    d = den;
+    long long qq = num / den, rr = num % den;
+    if (rr < 0) {
+      rr += den;
+      qq -= 1;
+    }
+    q = (int)qq;
+    r = (int)rr;
+  }
+  // num += dq * d + dr with 0 <= dr < d
+  __device__ __forceinline__ void step(int dq, int dr) {
+    q += dq;
+    r += dr;
+    if (r >= d) {
+      r -= d;
+      q += 1;
+    }
+  }
+};
+
+}  // namespace tsim

@@ -1,0 +1,326 @@
+// capi.cu -- context, scratch arena, device-resident database and status
+// reporting of the C ABI (include/tsim.h).
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "tsim_internal.cuh"
+
+namespace tsim {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int status, const std::string& msg) {
+  g_last_error = msg;
+  return status;
+}
+
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+  char b[512];
+  snprintf(b, sizeof b, "%s failed at %s:%d: %s (%s)", what, file, line, cudaGetErrorName(e),
+           cudaGetErrorString(e));
+  g_last_error = b;
+  return e == cudaErrorMemoryAllocation ? TSIM_ERR_OUT_OF_MEMORY : TSIM_ERR_CUDA;
+}
+
+int arena_reserve(tsim_ctx* ctx, size_t bytes) {
+  ctx->arena_used = 0;
+  if (bytes <= ctx->arena_cap) return TSIM_OK;
+  size_t cap = std::max(bytes + bytes / 4, size_t(1) << 20);
+  if (ctx->arena) {
+    TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+    TSIM_CUDA(cudaFree(ctx->arena));
+    ctx->arena = nullptr;
+    ctx->arena_cap = 0;
+  }
+  TSIM_CUDA(cudaMalloc(&ctx->arena, cap));
+  ctx->arena_cap = cap;
+  return TSIM_OK;
+}
+
+int pinned_reserve(tsim_ctx* ctx, size_t bytes) {
+  if (bytes <= ctx->pinned_cap) return TSIM_OK;
+  size_t cap = std::max(bytes + bytes / 4, size_t(1) << 20);
+  if (ctx->pinned) {
+    TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+    TSIM_CUDA(cudaFreeHost(ctx->pinned));
+    ctx->pinned = nullptr;
+    ctx->pinned_cap = 0;
+  }
+  TSIM_CUDA(cudaMallocHost(&ctx->pinned, cap));
+  ctx->pinned_cap = cap;
+  return TSIM_OK;
+}
+
+namespace {
+
+// Per-trajectory summaries: bounding box and first/last point.
+__global__ void summarize_kernel(const float2* __restrict__ pts, const int64_t* __restrict__ off,
+                                 int count, float4* __restrict__ box, float4* __restrict__ ends,
+                                 int* __restrict__ len) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int t = warp; t < count; t += nwarps) {
+    const int64_t b = off[t], e = off[t + 1];
+    float x0 = TSIM_INF, y0 = TSIM_INF, x1 = -TSIM_INF, y1 = -TSIM_INF;
+    for (int64_t i = b + lane; i < e; i += 32) {
+      float2 p = pts[i];
+      x0 = fminf(x0, p.x);
+      x1 = fmaxf(x1, p.x);
+      y0 = fminf(y0, p.y);
+      y1 = fmaxf(y1, p.y);
+    }
+    for (int o = 16; o; o >>= 1) {
+      x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+      y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+      x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+      y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+    if (lane == 0) {
+      box[t] = make_float4(x0, y0, x1, y1);
+      if (e > b) {
+        float2 f = pts[b], l = pts[e - 1];
+        ends[t] = make_float4(f.x, f.y, l.x, l.y);
+      } else {
+        ends[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      len[t] = (int)(e - b);
+    }
+  }
+}
+
+}  // namespace
+
+int summarize(tsim_ctx* ctx, const float2* pts, const int64_t* off, int count, float4* box,
+              float4* ends, int* len) {
+  if (count == 0) return TSIM_OK;
+  int blocks = std::min((count + 7) / 8, ctx->num_sms * 16);
+  summarize_kernel<<<blocks, 256, 0, ctx->stream>>>(pts, off, count, box, ends, len);
+  TSIM_CUDA(cudaGetLastError());
+  return TSIM_OK;
+}
+
+int db_summarize(tsim_db* db) {
+  if (db->count == 0) return TSIM_OK;
+  int blocks = std::min((db->count + 7) / 8, db->ctx->num_sms * 16);
+  summarize_kernel<<<blocks, 256, 0, db->ctx->stream>>>(db->pts, db->off, db->count, db->box,
+                                                         db->ends, db->len);
+  TSIM_CUDA(cudaGetLastError());
+  return TSIM_OK;
+}
+
+}  // namespace tsim
+
+using namespace tsim;
+
+extern "C" {
+
+const char* tsim_status_string(int s) {
+  switch (s) {
+    case TSIM_OK: return "ok";
+    case TSIM_ERR_INVALID_ARG: return "invalid argument";
+    case TSIM_ERR_CUDA: return "CUDA error";
+    case TSIM_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case TSIM_ERR_TIMEOUT: return "bounded wait timed out";
+    case TSIM_ERR_UNSUPPORTED: return "unsupported";
+    case TSIM_ERR_BUDGET: return "over admission budget";
+  }
+  return "unknown status";
+}
+
+const char* tsim_last_error(void) { return g_last_error.c_str(); }
+
+int tsim_version(void) { return 10000; }
+
+int tsim_ctx_create(int device, void* stream, tsim_ctx** out) {
+  TSIM_CHECK_ARG(out != nullptr, "out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  TSIM_CUDA(cudaGetDeviceCount(&ndev));
+  TSIM_CHECK_ARG(device >= 0 && device < ndev, "no such CUDA device");
+  TSIM_CUDA(cudaSetDevice(device));
+  tsim_ctx* c = new tsim_ctx;
+  c->device = device;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "cudaGetDeviceProperties", __FILE__, __LINE__);
+  }
+  c->num_sms = prop.multiProcessorCount;
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+  } else {
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete c;
+      return cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__);
+    }
+    c->owns_stream = true;
+  }
+  cudaEventCreate(&c->ev0);
+  cudaEventCreate(&c->ev1);
+  *out = c;
+  return TSIM_OK;
+}
+
+int tsim_ctx_destroy(tsim_ctx* c) {
+  if (!c) return TSIM_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  if (c->arena) cudaFree(c->arena);
+  if (c->pinned) cudaFreeHost(c->pinned);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->owns_stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return TSIM_OK;
+}
+
+int tsim_ctx_set_stream(tsim_ctx* c, void* stream) {
+  TSIM_CHECK_ARG(c != nullptr, "ctx is NULL");
+  TSIM_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->owns_stream) cudaStreamDestroy(c->stream);
+  c->owns_stream = false;
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+  } else {
+    TSIM_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->owns_stream = true;
+  }
+  return TSIM_OK;
+}
+
+int tsim_ctx_synchronize(tsim_ctx* c) {
+  TSIM_CHECK_ARG(c != nullptr, "ctx is NULL");
+  TSIM_CUDA(cudaStreamSynchronize(c->stream));
+  return TSIM_OK;
+}
+
+int64_t tsim_ctx_scratch_bytes(const tsim_ctx* c) { return c ? (int64_t)c->arena_cap : 0; }
+
+static int db_alloc(tsim_db* db) {
+  TSIM_CUDA(cudaMalloc(&db->box, sizeof(float4) * std::max(db->count, 1)));
+  TSIM_CUDA(cudaMalloc(&db->ends, sizeof(float4) * std::max(db->count, 1)));
+  TSIM_CUDA(cudaMalloc(&db->len, sizeof(int) * std::max(db->count, 1)));
+  return TSIM_OK;
+}
+
+static void db_free(tsim_db* db) {
+  if (db->owns) {
+    cudaFree(db->pts);
+    cudaFree(db->off);
+  }
+  cudaFree(db->box);
+  cudaFree(db->ends);
+  cudaFree(db->len);
+}
+
+int tsim_db_create(tsim_ctx* ctx, const tsim_point* h_pts, const int64_t* h_off, int count,
+                   tsim_db** out) {
+  TSIM_CHECK_ARG(ctx && out && h_off && count >= 0, "bad arguments");
+  *out = nullptr;
+  TSIM_CHECK_ARG(h_off[0] == 0, "offsets must start at 0");
+  int max_len = 0;
+  for (int t = 0; t < count; ++t) {
+    TSIM_CHECK_ARG(h_off[t + 1] > h_off[t], "trajectories must be non-empty (offsets increasing)");
+    max_len = std::max<int64_t>(max_len, h_off[t + 1] - h_off[t]);
+  }
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  tsim_db* db = new tsim_db;
+  db->ctx = ctx;
+  db->count = count;
+  db->total = h_off[count];
+  db->max_len = max_len;
+  db->owns = true;
+  db->h_off.assign(h_off, h_off + count + 1);
+  int s = TSIM_OK;
+  cudaError_t e = cudaMalloc(&db->pts, sizeof(float2) * std::max<int64_t>(db->total, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&db->off, sizeof(int64_t) * (count + 1));
+  if (e == cudaSuccess && db->total > 0)
+    e = cudaMemcpyAsync(db->pts, h_pts, sizeof(float2) * db->total, cudaMemcpyHostToDevice,
+                        ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(db->off, h_off, sizeof(int64_t) * (count + 1), cudaMemcpyHostToDevice,
+                        ctx->stream);
+  if (e != cudaSuccess) s = cuda_fail(e, "tsim_db_create upload", __FILE__, __LINE__);
+  if (s == TSIM_OK) s = db_alloc(db);
+  if (s == TSIM_OK) s = db_summarize(db);
+  if (s == TSIM_OK) {
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) s = cuda_fail(e, "tsim_db_create sync", __FILE__, __LINE__);
+  }
+  if (s != TSIM_OK) {
+    db_free(db);
+    delete db;
+    return s;
+  }
+  *out = db;
+  return TSIM_OK;
+}
+
+int tsim_db_wrap_device(tsim_ctx* ctx, const tsim_point* d_pts, const int64_t* d_off, int count,
+                        int max_len, tsim_db** out) {
+  TSIM_CHECK_ARG(ctx && out && d_off && count >= 0, "bad arguments");
+  *out = nullptr;
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  tsim_db* db = new tsim_db;
+  db->ctx = ctx;
+  db->count = count;
+  db->owns = false;
+  db->pts = (float2*)d_pts;
+  db->off = (int64_t*)d_off;
+  db->h_off.resize(count + 1);
+  cudaError_t e = cudaMemcpyAsync(db->h_off.data(), d_off, sizeof(int64_t) * (count + 1),
+                                  cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    delete db;
+    return cuda_fail(e, "tsim_db_wrap_device offsets", __FILE__, __LINE__);
+  }
+  db->total = db->h_off[count];
+  int ml = 0;
+  for (int t = 0; t < count; ++t) {
+    if (db->h_off[t + 1] <= db->h_off[t] || db->h_off[0] != 0) {
+      delete db;
+      return fail(TSIM_ERR_INVALID_ARG, "tsim_db_wrap_device: offsets must start at 0 and increase");
+    }
+    ml = std::max<int64_t>(ml, db->h_off[t + 1] - db->h_off[t]);
+  }
+  db->max_len = max_len > 0 ? max_len : ml;
+  int s = db_alloc(db);
+  if (s == TSIM_OK) s = db_summarize(db);
+  if (s == TSIM_OK) {
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) s = cuda_fail(e, "tsim_db_wrap_device sync", __FILE__, __LINE__);
+  }
+  if (s != TSIM_OK) {
+    db_free(db);
+    delete db;
+    return s;
+  }
+  *out = db;
+  return TSIM_OK;
+}
+
+int tsim_db_destroy(tsim_db* db) {
+  if (!db) return TSIM_OK;
+  cudaSetDevice(db->ctx->device);
+  cudaStreamSynchronize(db->ctx->stream);
+  db_free(db);
+  delete db;
+  return TSIM_OK;
+}
+
+int tsim_db_count(const tsim_db* db) { return db ? db->count : 0; }
+
+int64_t tsim_db_device_bytes(const tsim_db* db) {
+  if (!db) return 0;
+  return (db->owns ? (int64_t)sizeof(float2) * db->total + 8 * (db->count + 1) : 0) +
+         (int64_t)db->count * (16 + 16 + 4);
+}
+
+}  // extern "C"

@@ -1,0 +1,825 @@
+// knn.cu -- exact k-nearest-neighbour search over a device-resident
+// trajectory database for DTW, LCSS and discrete Frechet.
+//
+// Stages (all on one stream, fixed launch shapes, data-dependent counts kept
+// on the device so the whole sequence can be captured in a CUDA graph):
+//   A  lb1_kernel      O(1) bound per (query, candidate) from 36-byte
+//                      summaries (box, first and last point, length); each
+//                      CTA also keeps its chunk's best few candidates;
+//   B  seeds           the S best chunk candidates per query are refined
+//                      exactly; the k-th best refined value, widened by the
+//                      FP32 error bound, is the query's pruning threshold;
+//   C  compact + lb2   pairs whose O(1) bound passes get the O(length)
+//                      bound (banded LB_Keogh from a sparse table of the
+//                      query in shared memory for DTW, box distances for
+//                      Frechet, the windowed eps-box count for LCSS);
+//   D  DP              the survivors run the wavefront DP with early
+//                      abandon against the threshold;
+//   E  final           the k-th best FP32 value fixes the re-score set (all
+//                      pairs within the error bound of it), which is
+//                      re-computed in FP64 with the oracle's arithmetic and
+//                      sorted by (distance, candidate index).
+// LCSS counts are exact integers in FP32, so LCSS skips the re-score.
+//
+// The reference's GPU path (CudaRuntime1/dtw.cu:99-234) instead ranks every
+// candidate by a heuristic bound, refines a fixed 10 and returns one value:
+// not an exact kNN.  This path returns the exact top-k ids and distances.
+#include "bounds.cuh"
+#include "topk.cuh"
+#include "tsim_internal.cuh"
+
+namespace tsim {
+
+int summarize(tsim_ctx* ctx, const float2* pts, const int64_t* off, int count, float4* box,
+              float4* ends, int* len);
+
+namespace {
+
+constexpr int kChunk = 256;     // candidates per stage-A CTA
+constexpr int kSelThreads = 256;
+constexpr int kLb2Warps = 8;
+constexpr int kMaxTable = 512;  // sparse-table columns (query rows, downsampled beyond)
+
+enum Meas { M_DTW = 0, M_LCSS = 1, M_FRECHET = 2 };
+
+struct KArgs {
+  // queries
+  const float2* qpts;
+  const int64_t* qoff;
+  const float4* qbox;
+  const float4* qends;
+  const int* qlen;
+  int nq;
+  // database
+  const float2* cpts;
+  const int64_t* coff;
+  const float4* cbox;
+  const float4* cends;
+  const int* clen;
+  int C;
+  int max_clen;
+  int max_qlen;  // shared-memory tables are sized for this query length
+  // parameters
+  int k, S, T, nch;
+  int cost;  // DTW: 0 squared, 1 Euclidean
+  int band_pct;
+  int delta;
+  float eps;
+  // scratch
+  float* lb1;               // [nq*C]
+  int* chunk_cand;          // [nq*nch*T]
+  int2* seeds;              // [nq*S]
+  unsigned* seedmap;        // [nq*Cw]
+  int Cw;
+  float* seed_vals;         // [nq*S]
+  float* thr;               // [nq]  pruning / abandon threshold
+  int* cnt1;                // [nq]
+  int* list1;               // [nq*C]
+  int* cnt2;                // [nq]
+  int* list2;               // [nq*C]
+  int* off2;                // [nq+1]
+  int* npairs;              // [1]
+  int2* flat;               // [nq*C]
+  float* flat_vals;         // [nq*C]
+  unsigned long long* fkeys;  // [nq*(S+C)]
+  int RC;
+  int2* rpairs;             // [nq*RC]
+  double* r64;              // [nq*RC]
+  int* rcnt;                // [nq]
+  // outputs
+  int* ids;
+  float* dists;
+  double* dists64;
+};
+
+__device__ __forceinline__ double gamma_dp(int meas, int n, int m) {
+  // relative error of an FP32 DP value against FP64 (both against exact):
+  // every cost carries <= 4 roundings, a path of <= n+m-1 cells adds one
+  // rounding per cell; Frechet values are single costs.
+  const double u = 1.0 / 16777216.0;
+  if (meas == M_FRECHET) return 8.0 * u;
+  return (double)(n + m + 8) * u * 1.01 + 1e-12;
+}
+
+// threshold widened by the error bound, rounded up to float
+__device__ __forceinline__ float widen(float t, double g) {
+  if (!(t < TSIM_INF)) return TSIM_INF;
+  return __double2float_ru((double)t * (1.0 + g) / (1.0 - g) * (1.0 + 1e-12));
+}
+
+// ---------------------------------------------------------------------------
+// stage A: O(1) bounds from summaries + chunk-local best candidates
+// ---------------------------------------------------------------------------
+template <int MEAS>
+__device__ __forceinline__ float bound1(const KArgs& a, float4 qb, float4 qe, int n, float4 cb,
+                                        float4 ce, int m) {
+  if (n <= 0 || m <= 0) return MEAS == M_LCSS ? 0.0f : TSIM_INF;  // empty: never a neighbour
+  if (MEAS == M_LCSS) {
+    // upper bound on the count: 0 when the eps-inflated boxes are disjoint
+    const float e2 = __fmul_ru(a.eps, 1.0f + 1.0f / 1048576.0f);
+    bool ov = cb.z >= __fsub_rd(qb.x, e2) && cb.x <= __fadd_ru(qb.z, e2) &&
+              cb.w >= __fsub_rd(qb.y, e2) && cb.y <= __fadd_ru(qb.w, e2);
+    return ov ? (float)min(n, m) : 0.0f;
+  }
+  const float first = pd2_rd(qe.x, qe.y, ce.x, ce.y);
+  const float last = pd2_rd(qe.z, qe.w, ce.z, ce.w);
+  const float bb = box_box_d2_rd(qb, cb);
+  if (MEAS == M_FRECHET) return fmaxf(fmaxf(first, last), bb);
+  // DTW: the path has >= max(n,m) cells; (0,0) and (n-1,m-1) are on it
+  const int L = max(n, m);
+  if (L < 2) return a.cost ? __fsqrt_rd(first) : first;
+  if (a.cost) {
+    float s = __fadd_rd(__fsqrt_rd(first), __fsqrt_rd(last));
+    return __fadd_rd(s, __fmul_rd((float)(L - 2), __fsqrt_rd(bb)));
+  }
+  return __fadd_rd(__fadd_rd(first, last), __fmul_rd((float)(L - 2), bb));
+}
+
+template <int MEAS>
+__global__ void __launch_bounds__(kChunk) lb1_kernel(KArgs a) {
+  __shared__ unsigned long long keys[kChunk];
+  __shared__ unsigned long long red[33];
+  __shared__ unsigned long long sel[64];
+  const int q = blockIdx.y, chunk = blockIdx.x;
+  const int c = chunk * kChunk + threadIdx.x;
+  const float4 qb = a.qbox[q], qe = a.qends[q];
+  const int n = a.qlen[q];
+  unsigned long long key = ~0ull;
+  if (c < a.C) {
+    float b = bound1<MEAS>(a, qb, qe, n, a.cbox[c], a.cends[c], a.clen[c]);
+    a.lb1[(size_t)q * a.C + c] = b;
+    key = pack_key(MEAS == M_LCSS ? -b : b, threadIdx.x);
+  }
+  keys[threadIdx.x] = key;
+  __syncthreads();
+  block_select_k(keys, kChunk, a.T, sel, red);
+  for (int i = threadIdx.x; i < a.T; i += kChunk) {
+    int li = key_index(sel[i]);
+    a.chunk_cand[((size_t)q * a.nch + chunk) * a.T + i] = li < 0 ? -1 : chunk * kChunk + li;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// stage B: seeds
+// ---------------------------------------------------------------------------
+template <int MEAS>
+__global__ void __launch_bounds__(kSelThreads) seed_kernel(KArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long red[33];
+  __shared__ unsigned long long sel[64];
+  const int q = blockIdx.x;
+  const int N = a.nch * a.T;
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem_raw);
+  const int* cc = a.chunk_cand + (size_t)q * N;
+  for (int i = threadIdx.x; i < N; i += kSelThreads) {
+    int c = cc[i];
+    unsigned long long key = ~0ull;
+    if (c >= 0) {
+      float b = a.lb1[(size_t)q * a.C + c];
+      key = pack_key(MEAS == M_LCSS ? -b : b, c);
+    }
+    keys[i] = key;
+  }
+  __syncthreads();
+  block_select_k(keys, N, a.S, sel, red);
+  for (int i = threadIdx.x; i < a.S; i += kSelThreads) {
+    int c = key_index(sel[i]);
+    a.seeds[(size_t)q * a.S + i] = make_int2(q, c);
+    if (c >= 0) atomicOr(a.seedmap + (size_t)q * a.Cw + (c >> 5), 1u << (c & 31));
+  }
+}
+
+// k-th best seed value -> threshold (DTW/Frechet: widened; LCSS: count)
+template <int MEAS>
+__global__ void thresh_kernel(KArgs a) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= a.nq) return;
+  float v[64];
+  int cnt = 0;
+  for (int i = 0; i < a.S; ++i) {
+    if (a.seeds[(size_t)q * a.S + i].y < 0) continue;
+    float x = a.seed_vals[(size_t)q * a.S + i];
+    if (MEAS == M_LCSS) x = -x;
+    int p = cnt++;
+    while (p > 0 && v[p - 1] > x) {
+      v[p] = v[p - 1];
+      --p;
+    }
+    v[p] = x;
+  }
+  float t;
+  if (cnt < a.k) {
+    t = MEAS == M_LCSS ? 0.0f : TSIM_INF;  // not enough seeds: keep everything
+  } else if (MEAS == M_LCSS) {
+    t = -v[a.k - 1];
+  } else {
+    t = widen(v[a.k - 1], gamma_dp(MEAS, a.qlen[q], a.max_clen));
+  }
+  a.thr[q] = t;
+  a.cnt1[q] = 0;
+  a.cnt2[q] = 0;
+  a.rcnt[q] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// stage C: compaction and O(length) bounds
+// ---------------------------------------------------------------------------
+template <int MEAS>
+__global__ void __launch_bounds__(kChunk) compact_kernel(KArgs a) {
+  const int q = blockIdx.y;
+  const int c = blockIdx.x * kChunk + threadIdx.x;
+  const float t = a.thr[q];
+  bool pass = false;
+  if (c < a.C) {
+    const bool seeded = (a.seedmap[(size_t)q * a.Cw + (c >> 5)] >> (c & 31)) & 1u;
+    const float b = a.lb1[(size_t)q * a.C + c];
+    pass = !seeded && (MEAS == M_LCSS ? (b >= t) : (b <= t));
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, pass);
+  if (ball) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ball) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(a.cnt1 + q, __popc(ball));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pass) a.list1[(size_t)q * a.C + base + __popc(ball & ((1u << lane) - 1))] = c;
+  }
+}
+
+// Sparse table of the query for O(1) range boxes: level l holds, for block b,
+// the box of blocks [b, b + 2^l).  Block = f consecutive rows (f = 1 for
+// queries up to kMaxTable rows, a power of two beyond, which widens boxes and
+// keeps the bound valid).
+struct QTable {
+  float4* t;  // [levels][nb] as (x0, y0, x1, y1)
+  int nb, f_log, levels;
+};
+
+__device__ __forceinline__ void qtable_build(QTable& T, const float2* A, int n, float4* smem) {
+  int f_log = 0;
+  while ((n + (1 << f_log) - 1) >> f_log > kMaxTable) ++f_log;
+  const int nb = (n + (1 << f_log) - 1) >> f_log;
+  int levels = 1;
+  while ((1 << levels) <= nb) ++levels;
+  T.t = smem;
+  T.nb = nb;
+  T.f_log = f_log;
+  T.levels = levels;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    float x0 = TSIM_INF, y0 = TSIM_INF, x1 = -TSIM_INF, y1 = -TSIM_INF;
+    const int r0 = b << f_log, r1 = min(n, (b + 1) << f_log);
+    for (int r = r0; r < r1; ++r) {
+      float2 p = A[r];
+      x0 = fminf(x0, p.x);
+      y0 = fminf(y0, p.y);
+      x1 = fmaxf(x1, p.x);
+      y1 = fmaxf(y1, p.y);
+    }
+    smem[b] = make_float4(x0, y0, x1, y1);
+  }
+  __syncthreads();
+  for (int l = 1; l < levels; ++l) {
+    const int h = 1 << (l - 1);
+    for (int b = threadIdx.x; b + (1 << l) <= nb; b += blockDim.x) {
+      float4 u = smem[(size_t)(l - 1) * nb + b], v = smem[(size_t)(l - 1) * nb + b + h];
+      smem[(size_t)l * nb + b] =
+          make_float4(fminf(u.x, v.x), fminf(u.y, v.y), fmaxf(u.z, v.z), fmaxf(u.w, v.w));
+    }
+    __syncthreads();
+  }
+}
+
+// box of query rows [lo, hi] (non-empty)
+__device__ __forceinline__ float4 qtable_box(const QTable& T, int lo, int hi) {
+  const int b0 = lo >> T.f_log, b1 = hi >> T.f_log;
+  const int l = 31 - __clz(b1 - b0 + 1);
+  const float4 u = T.t[(size_t)l * T.nb + b0], v = T.t[(size_t)l * T.nb + b1 - (1 << l) + 1];
+  return make_float4(fminf(u.x, v.x), fminf(u.y, v.y), fmaxf(u.z, v.z), fmaxf(u.w, v.w));
+}
+
+size_t qtable_bytes(int max_n) {
+  int f_log = 0;
+  while ((max_n + (1 << f_log) - 1) >> f_log > kMaxTable) ++f_log;
+  int nb = (max_n + (1 << f_log) - 1) >> f_log;
+  int levels = 1;
+  while ((1 << levels) <= nb) ++levels;
+  return (size_t)levels * nb * sizeof(float4);
+}
+
+template <int MEAS>
+__global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int q = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int cnt = a.cnt1[q];
+  if (cnt == 0) return;  // uniform across the CTA
+  const float2* A = a.qpts + a.qoff[q];
+  const int n = a.qlen[q];
+  const float4 qb = a.qbox[q];
+  const float t = a.thr[q];
+  // a query longer than the table was sized for passes every pair (the
+  // bound is skipped, never guessed)
+  const bool use_table = n <= a.max_qlen;
+  QTable T;
+  if (MEAS != M_FRECHET && use_table) qtable_build(T, A, n, reinterpret_cast<float4*>(smem_raw));
+  const float e2 = __fmul_ru(a.eps, 1.0f + 1.0f / 1048576.0f);
+  for (int e = blockIdx.x * kLb2Warps + warp; e < cnt; e += gridDim.x * kLb2Warps) {
+    const int c = a.list1[(size_t)q * a.C + e];
+    const float2* B = a.cpts + a.coff[c];
+    const int m = a.clen[c];
+    bool pass;
+    if (n <= 0 || m <= 0) {
+      pass = false;
+    } else if (MEAS != M_FRECHET && !use_table) {
+      pass = true;
+    } else if (MEAS == M_DTW) {
+      // banded LB_Keogh: column j costs at least the distance from c_j to the
+      // box of the query rows its band admits; columns 0 and m-1 are the
+      // cells (0,0) and (n-1,m-1) every path contains.
+      const int w = band_w(n, m, a.band_pct);
+      float acc = 0.0f;
+      bool feasible = true;
+      if (m == 1) {
+        if (lane == 0) {
+          float d = pd2_rd(A[0].x, A[0].y, B[0].x, B[0].y);
+          acc = a.cost ? __fsqrt_rd(d) : d;
+          if (n > 1) {
+            float d2 = pd2_rd(A[n - 1].x, A[n - 1].y, B[0].x, B[0].y);
+            acc = __fadd_rd(acc, a.cost ? __fsqrt_rd(d2) : d2);
+          }
+        }
+      } else {
+        if (lane == 0) {
+          float d0 = pd2_rd(A[0].x, A[0].y, B[0].x, B[0].y);
+          float d1 = pd2_rd(A[n - 1].x, A[n - 1].y, B[m - 1].x, B[m - 1].y);
+          acc = a.cost ? __fadd_rd(__fsqrt_rd(d0), __fsqrt_rd(d1)) : __fadd_rd(d0, d1);
+        }
+        // rows of column j: [ceil((j(n-1)-W)/(m-1)), floor((j(n-1)+W)/(m-1))]
+        const bool banded = w >= 0 && n > 1;
+        const int D = m - 1;
+        const long long W = banded ? (long long)w * (min(n, m) - 1) : 0;
+        FloorDiv lo_d, hi_d;
+        const int j0 = 1 + lane;
+        if (banded) {
+          lo_d.init((long long)j0 * (n - 1) - W + D - 1, D);
+          hi_d.init((long long)j0 * (n - 1) + W, D);
+        }
+        const long long inc = 32ll * (n - 1);
+        const int dq = (int)(inc / D), dr = (int)(inc % D);
+        for (int j = j0; j < m - 1; j += 32) {
+          int lo = 0, hi = n - 1;
+          if (banded) {
+            lo = max(lo_d.q, 0);
+            hi = min(hi_d.q, n - 1);
+            lo_d.step(dq, dr);
+            hi_d.step(dq, dr);
+          }
+          if (lo > hi) {
+            feasible = false;
+            break;
+          }
+          const float4 bx = qtable_box(T, lo, hi);
+          const float2 p = B[j];
+          float d = box_pt_d2_rd(bx.x, bx.y, bx.z, bx.w, p.x, p.y);
+          acc = __fadd_rd(acc, a.cost ? __fsqrt_rd(d) : d);
+        }
+      }
+      for (int o = 16; o; o >>= 1) acc = __fadd_rd(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+      feasible = __all_sync(0xffffffffu, feasible);
+      pass = feasible && acc <= t;
+    } else if (MEAS == M_FRECHET) {
+      // every point of either trajectory is coupled to some point of the
+      // other, so F^2 >= its squared distance to the other's box
+      const float4 cb = a.cbox[c];
+      float mx = 0.0f;
+      for (int j = lane; j < m; j += 32) {
+        float2 p = B[j];
+        mx = fmaxf(mx, box_pt_d2_rd(qb.x, qb.y, qb.z, qb.w, p.x, p.y));
+      }
+      for (int i = lane; i < n; i += 32) {
+        float2 p = A[i];
+        mx = fmaxf(mx, box_pt_d2_rd(cb.x, cb.y, cb.z, cb.w, p.x, p.y));
+      }
+      for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      pass = mx <= t;
+    } else {
+      // LCSS: candidate points that can match some query point of their
+      // window (rows [j-delta, j+delta]) inside the eps-inflated box
+      int count = 0;
+      for (int j = lane; j < m; j += 32) {
+        int lo = 0, hi = n - 1;
+        if (a.delta >= 0) {
+          lo = max(0, j - a.delta);
+          hi = min(n - 1, j + a.delta);
+        }
+        if (lo > hi) continue;
+        const float4 bx = qtable_box(T, lo, hi);
+        const float2 p = B[j];
+        if (p.x >= __fsub_rd(bx.x, e2) && p.x <= __fadd_ru(bx.z, e2) &&
+            p.y >= __fsub_rd(bx.y, e2) && p.y <= __fadd_ru(bx.w, e2))
+          ++count;
+      }
+      for (int o = 16; o; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
+      pass = (float)min(count, min(n, m)) >= t;
+    }
+    if (pass && lane == 0) {
+      int pos = atomicAdd(a.cnt2 + q, 1);
+      a.list2[(size_t)q * a.C + pos] = c;
+    }
+  }
+}
+
+// exclusive scan of cnt2 -> off2, total -> npairs (one CTA)
+__global__ void __launch_bounds__(1024) scan_kernel(KArgs a) {
+  __shared__ int part[1024];
+  const int per = (a.nq + 1023) / 1024;
+  const int b = threadIdx.x * per, e = min(a.nq, b + per);
+  int s = 0;
+  for (int i = b; i < e; ++i) s += a.cnt2[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = part[threadIdx.x] - s;
+  for (int i = b; i < e; ++i) {
+    a.off2[i] = run;
+    run += a.cnt2[i];
+  }
+  if (threadIdx.x == 1023) {
+    a.off2[a.nq] = part[1023];
+    *a.npairs = part[1023];
+  }
+}
+
+__global__ void flatten_kernel(KArgs a) {
+  const int q = blockIdx.y;
+  const int cnt = a.cnt2[q], base = a.off2[q];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += gridDim.x * blockDim.x)
+    a.flat[base + e] = make_int2(q, a.list2[(size_t)q * a.C + e]);
+}
+
+// ---------------------------------------------------------------------------
+// stage E: final selection, FP64 re-score, sort
+// ---------------------------------------------------------------------------
+template <int MEAS>
+__global__ void __launch_bounds__(kSelThreads) final_select_kernel(KArgs a) {
+  __shared__ unsigned long long red[33];
+  __shared__ unsigned long long sel[64];
+  __shared__ int rc;
+  const int q = blockIdx.x;
+  const int S = a.S, nf = a.cnt2[q], base = a.off2[q];
+  const int N = S + nf;
+  unsigned long long* keys = a.fkeys + (size_t)q * (a.S + a.C);
+  for (int i = threadIdx.x; i < N; i += kSelThreads) {
+    unsigned long long key = ~0ull;
+    if (i < S) {
+      int c = a.seeds[(size_t)q * S + i].y;
+      if (c >= 0) {
+        float v = a.seed_vals[(size_t)q * S + i];
+        key = pack_key(MEAS == M_LCSS ? -v : v, c);
+      }
+    } else {
+      float v = a.flat_vals[base + i - S];
+      int c = a.flat[base + i - S].y;
+      key = pack_key(MEAS == M_LCSS ? -v : v, c);
+    }
+    keys[i] = key;
+  }
+  if (threadIdx.x == 0) rc = 0;
+  __syncthreads();
+  block_select_k(keys, N, a.k, sel, red);
+  if (MEAS == M_LCSS) {
+    for (int i = threadIdx.x; i < a.k; i += kSelThreads) {
+      int c = key_index(sel[i]);
+      a.ids[(size_t)q * a.k + i] = c;
+      float cntv = c < 0 ? -1.0f : -ord2f((unsigned)(sel[i] >> 32));
+      a.dists[(size_t)q * a.k + i] = cntv;
+      if (a.dists64) a.dists64[(size_t)q * a.k + i] = cntv;
+    }
+    return;
+  }
+  // the k-th best FP32 value fixes the re-score set
+  const unsigned long long kth = sel[a.k - 1];
+  const float tk = kth == ~0ull ? TSIM_INF : ord2f((unsigned)(kth >> 32));
+  const bool finite = tk < TSIM_INF;
+  const float tr = widen(tk, gamma_dp(MEAS, a.qlen[q], a.max_clen));
+  // keys were consumed by the selection: rebuild membership from values
+  for (int i = threadIdx.x; i < N; i += kSelThreads) {
+    int c;
+    float v;
+    if (i < S) {
+      c = a.seeds[(size_t)q * S + i].y;
+      v = a.seed_vals[(size_t)q * S + i];
+    } else {
+      c = a.flat[base + i - S].y;
+      v = a.flat_vals[base + i - S];
+    }
+    if (c < 0) continue;
+    bool take = finite ? (v <= tr) : (pack_key(v, c) <= kth);
+    if (take) {
+      int p = atomicAdd(&rc, 1);
+      if (p < a.RC) a.rpairs[(size_t)q * a.RC + p] = make_int2(q, c);
+    }
+  }
+  __syncthreads();
+  for (int p = rc + threadIdx.x; p < a.RC; p += kSelThreads)
+    a.rpairs[(size_t)q * a.RC + p] = make_int2(q, -1);
+  if (threadIdx.x == 0) a.rcnt[q] = min(rc, a.RC);
+}
+
+// sort the re-scored pairs by (FP64 distance, index); one thread per query
+template <int MEAS>
+__global__ void final_sort_kernel(KArgs a) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= a.nq) return;
+  const int cnt = a.rcnt[q];
+  const int2* rp = a.rpairs + (size_t)q * a.RC;
+  const double* rv = a.r64 + (size_t)q * a.RC;
+  double last_d = -1.0;
+  int last_c = -1;
+  for (int e = 0; e < a.k; ++e) {
+    // selection of the next (d, c) after (last_d, last_c)
+    double bd = __longlong_as_double(0x7ff0000000000000ll);
+    int bc = -1;
+    bool found = false;
+    for (int i = 0; i < cnt; ++i) {
+      double d = rv[i];
+      if (MEAS == M_FRECHET) d = __dsqrt_rn(d);
+      const int c = rp[i].y;
+      const bool after = d > last_d || (d == last_d && c > last_c);
+      if (!after) continue;
+      if (!found || d < bd || (d == bd && c < bc)) {
+        bd = d;
+        bc = c;
+        found = true;
+      }
+    }
+    const size_t o = (size_t)q * a.k + e;
+    if (found) {
+      a.ids[o] = bc;
+      a.dists[o] = __double2float_rn(bd);
+      if (a.dists64) a.dists64[o] = bd;
+      last_d = bd;
+      last_c = bc;
+    } else {
+      a.ids[o] = -1;
+      a.dists[o] = TSIM_INF;
+      if (a.dists64) a.dists64[o] = __longlong_as_double(0x7ff0000000000000ll);
+    }
+  }
+}
+
+__global__ void clear_u32_kernel(unsigned* p, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    p[i] = 0;
+}
+
+template <int MEAS>
+int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stats* st) {
+  cudaStream_t s = ctx->stream;
+  const int nq = a.nq;
+  dim3 g1(a.nch, nq);
+  clear_u32_kernel<<<std::min<size_t>(((size_t)nq * a.Cw + 255) / 256, 4096), 256, 0, s>>>(
+      a.seedmap, (size_t)nq * a.Cw);
+  lb1_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
+  const size_t seed_smem = sizeof(unsigned long long) * (size_t)a.nch * a.T;
+  if (seed_smem > 48 * 1024)
+    TSIM_CUDA(cudaFuncSetAttribute(seed_kernel<MEAS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)seed_smem));
+  seed_kernel<MEAS><<<nq, kSelThreads, seed_smem, s>>>(a);
+  TSIM_CUDA(cudaGetLastError());
+
+  // representative launch shape for the DP: longest query against the
+  // average candidate
+  const int avg_m = std::max(1, a.max_clen > 0 ? (int)std::min<long long>(a.max_clen, 1 << 30) : 1);
+  DpArgs d{};
+  d.qpts = a.qpts;
+  d.qoff = a.qoff;
+  d.cpts = a.cpts;
+  d.coff = a.coff;
+  d.band_pct = MEAS == M_DTW ? a.band_pct : -1;
+  d.delta = a.delta;
+  d.eps = a.eps;
+  int G, R;
+  const int wd = MEAS == M_LCSS ? a.delta : band_w(max_qlen, avg_m, d.band_pct);
+  dp_shape(dp32, max_qlen, avg_m, wd, G, R);
+
+  d.pairs = a.seeds;
+  d.npairs = nq * a.S;
+  d.out = a.seed_vals;
+  TSIM_TRY(launch_dp(ctx, dp32, G, R, d, a.max_clen));
+
+  thresh_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+  compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
+  const int ch = std::max(1, std::min(64, (2 * ctx->num_sms * 4 + nq - 1) / nq));
+  size_t lb2_smem = MEAS == M_FRECHET ? 0 : qtable_bytes(max_qlen);
+  if (lb2_smem > 48 * 1024)
+    TSIM_CUDA(cudaFuncSetAttribute(lb2_kernel<MEAS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)lb2_smem));
+  lb2_kernel<MEAS><<<dim3(ch, nq), kLb2Warps * 32, lb2_smem, s>>>(a);
+  scan_kernel<<<1, 1024, 0, s>>>(a);
+  flatten_kernel<<<dim3(ch, nq), 256, 0, s>>>(a);
+  TSIM_CUDA(cudaGetLastError());
+
+  d.pairs = a.flat;
+  d.npairs = nq * a.C;
+  d.npairs_dev = a.npairs;
+  d.out = a.flat_vals;
+  d.thr = a.thr;
+  TSIM_TRY(launch_dp(ctx, dp32, G, R, d, a.max_clen));
+
+  final_select_kernel<MEAS><<<nq, kSelThreads, 0, s>>>(a);
+  TSIM_CUDA(cudaGetLastError());
+  if (MEAS != M_LCSS) {
+    DpArgs r{};
+    r.qpts = a.qpts;
+    r.qoff = a.qoff;
+    r.cpts = a.cpts;
+    r.coff = a.coff;
+    r.pairs = a.rpairs;
+    r.npairs = nq * a.RC;
+    r.out64 = a.r64;
+    r.band_pct = d.band_pct;
+    r.delta = -1;
+    int G64, R64;
+    dp_shape(dp64, max_qlen, avg_m, wd, G64, R64);
+    TSIM_TRY(launch_dp(ctx, dp64, G64, R64, r, a.max_clen));
+    final_sort_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+    TSIM_CUDA(cudaGetLastError());
+  }
+  (void)st;
+  return TSIM_OK;
+}
+
+}  // namespace
+
+int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
+        int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st) {
+  const int C = db->count;
+  TSIM_CHECK_ARG(C >= 1, "database is empty");
+  const int k = p->k;
+  KArgs a{};
+  a.nq = nq;
+  a.qpts = qpts;
+  a.qoff = qoff;
+  a.cpts = db->pts;
+  a.coff = db->off;
+  a.cbox = db->box;
+  a.cends = db->ends;
+  a.clen = db->len;
+  a.C = C;
+  a.max_clen = db->max_len;
+  a.max_qlen = max_qlen;
+  a.k = k;
+  a.S = std::min(C, std::min(64, std::max(2 * k, 16)));
+  a.nch = (C + kChunk - 1) / kChunk;
+  a.T = std::min(kChunk, std::max(1, (2 * a.S + a.nch - 1) / a.nch));
+  a.T = std::min(a.T, 64);
+  a.cost = p->cost;
+  a.band_pct = p->band_pct;
+  a.delta = p->delta;
+  a.eps = p->epsilon;
+  a.Cw = (C + 31) / 32;
+  a.RC = std::max(4 * k, 64);
+  a.ids = ids;
+  a.dists = dists;
+  a.dists64 = dists64;
+  TSIM_CHECK_ARG((size_t)a.nch * a.T * sizeof(unsigned long long) <= 200 * 1024,
+                 "database too large for one request (seed selection)");
+
+  const size_t nqC = (size_t)nq * C;
+  size_t need = align256(sizeof(float4) * nq) * 2 + align256(sizeof(int) * nq) +
+                align256(sizeof(float) * nqC) + align256(sizeof(int) * nq * a.nch * a.T) +
+                align256(sizeof(int2) * nq * a.S) + align256(sizeof(unsigned) * nq * a.Cw) +
+                align256(sizeof(float) * nq * a.S) + align256(sizeof(float) * nq) +
+                4 * align256(sizeof(int) * (nq + 1)) + 2 * align256(sizeof(int) * nqC) +
+                align256(sizeof(int) * 4) + align256(sizeof(int2) * nqC) +
+                align256(sizeof(float) * nqC) +
+                align256(sizeof(unsigned long long) * nq * (size_t)(a.S + C)) +
+                align256(sizeof(int2) * nq * a.RC) + align256(sizeof(double) * nq * a.RC);
+  TSIM_TRY(arena_reserve(ctx, need));
+  float4* qbox = arena_take<float4>(ctx, nq);
+  float4* qends = arena_take<float4>(ctx, nq);
+  int* qlen = arena_take<int>(ctx, nq);
+  a.qbox = qbox;
+  a.qends = qends;
+  a.qlen = qlen;
+  a.lb1 = arena_take<float>(ctx, nqC);
+  a.chunk_cand = arena_take<int>(ctx, (size_t)nq * a.nch * a.T);
+  a.seeds = arena_take<int2>(ctx, (size_t)nq * a.S);
+  a.seedmap = arena_take<unsigned>(ctx, (size_t)nq * a.Cw);
+  a.seed_vals = arena_take<float>(ctx, (size_t)nq * a.S);
+  a.thr = arena_take<float>(ctx, nq);
+  a.cnt1 = arena_take<int>(ctx, nq + 1);
+  a.cnt2 = arena_take<int>(ctx, nq + 1);
+  a.off2 = arena_take<int>(ctx, nq + 1);
+  a.rcnt = arena_take<int>(ctx, nq + 1);
+  a.list1 = arena_take<int>(ctx, nqC);
+  a.list2 = arena_take<int>(ctx, nqC);
+  a.npairs = arena_take<int>(ctx, 4);
+  a.flat = arena_take<int2>(ctx, nqC);
+  a.flat_vals = arena_take<float>(ctx, nqC);
+  a.fkeys = arena_take<unsigned long long>(ctx, (size_t)nq * (a.S + C));
+  a.rpairs = arena_take<int2>(ctx, (size_t)nq * a.RC);
+  a.r64 = arena_take<double>(ctx, (size_t)nq * a.RC);
+  if (!a.r64) return fail(TSIM_ERR_OUT_OF_MEMORY, "knn scratch carve failed");
+
+  TSIM_TRY(summarize(ctx, qpts, qoff, nq, qbox, qends, qlen));
+  switch (p->measure) {
+    case TSIM_DTW:
+      return run_knn<M_DTW>(ctx, a, max_qlen, p->cost ? DP_DTW_EU : DP_DTW_SQ,
+                            p->cost ? DP_DTW_EU64 : DP_DTW_SQ64, st);
+    case TSIM_LCSS:
+      return run_knn<M_LCSS>(ctx, a, max_qlen, DP_LCSS, DP_LCSS, st);
+    case TSIM_FRECHET:
+      a.band_pct = -1;
+      return run_knn<M_FRECHET>(ctx, a, max_qlen, DP_FRECHET_SQ, DP_FRECHET_SQ64, st);
+  }
+  return fail(TSIM_ERR_UNSUPPORTED, "measure not supported by this path");
+}
+
+}  // namespace tsim
+
+extern "C" int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
+                        const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
+                        float* d_dists, double* d_dists64, tsim_stats* stats) {
+  TSIM_CHECK_ARG(ctx && p && db, "NULL ctx, params or database");
+  TSIM_CHECK_ARG(nq >= 1 && max_qlen >= 1, "nq and max_qlen must be >= 1");
+  TSIM_CHECK_ARG(d_qpts && d_qoff && d_ids && d_dists, "NULL device pointer");
+  TSIM_CHECK_ARG(p->k >= 1 && p->k <= 64, "k must be in 1..64");
+  TSIM_CHECK_ARG(p->measure >= TSIM_DTW && p->measure <= TSIM_EUCLIDEAN, "unknown measure");
+  TSIM_CHECK_ARG(p->measure != TSIM_LCSS || p->epsilon >= 0.0f, "LCSS epsilon must be >= 0");
+  TSIM_CHECK_ARG(db->ctx == ctx, "database belongs to another context");
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  if (stats) {
+    *stats = tsim_stats{};
+    TSIM_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+  }
+  int s;
+  if (p->measure == TSIM_HAUSDORFF || p->measure == TSIM_EUCLIDEAN)
+    s = tsim::knn_pairwise(ctx, p, reinterpret_cast<const float2*>(d_qpts), d_qoff, nq, max_qlen,
+                           db, d_ids, d_dists, d_dists64, stats);
+  else
+    s = tsim::knn(ctx, p, reinterpret_cast<const float2*>(d_qpts), d_qoff, nq, max_qlen, db, d_ids,
+                  d_dists, d_dists64, stats);
+  if (s != TSIM_OK) return s;
+  if (stats) {
+    TSIM_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    TSIM_CUDA(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.0f;
+    TSIM_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    stats->ms = ms;
+    stats->pairs = (int64_t)nq * db->count;
+  }
+  return TSIM_OK;
+}
+
+extern "C" int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_point* h_qpts,
+                             const int64_t* h_qoff, int nq, tsim_db* db, int* h_ids,
+                             float* h_dists, tsim_stats* stats) {
+  TSIM_CHECK_ARG(ctx && p && db && h_qpts && h_qoff && h_ids && h_dists, "NULL argument");
+  TSIM_CHECK_ARG(nq >= 1 && p->k >= 1 && p->k <= 64, "bad nq or k");
+  TSIM_CHECK_ARG(h_qoff[0] == 0, "query offsets must start at 0");
+  int max_qlen = 0;
+  for (int i = 0; i < nq; ++i) {
+    TSIM_CHECK_ARG(h_qoff[i + 1] > h_qoff[i], "queries must be non-empty");
+    max_qlen = std::max<int64_t>(max_qlen, h_qoff[i + 1] - h_qoff[i]);
+  }
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  const size_t npts = (size_t)h_qoff[nq];
+  const size_t in_bytes = tsim::align256(sizeof(tsim_point) * npts) + tsim::align256(8 * (nq + 1));
+  const size_t out_bytes = tsim::align256(sizeof(int) * nq * p->k) + tsim::align256(sizeof(float) * nq * p->k);
+  TSIM_TRY(tsim::pinned_reserve(ctx, in_bytes + out_bytes));
+  // device staging lives in a separate allocation (the arena is reset by the knn call)
+  static thread_local void* dbuf = nullptr;
+  static thread_local size_t dcap = 0;
+  static thread_local int ddev = -1;
+  if (dcap < in_bytes + out_bytes || ddev != ctx->device) {
+    if (dbuf && ddev == ctx->device) cudaFree(dbuf);
+    dbuf = nullptr;
+    TSIM_CUDA(cudaMalloc(&dbuf, in_bytes + out_bytes));
+    dcap = in_bytes + out_bytes;
+    ddev = ctx->device;
+  }
+  char* hp = (char*)ctx->pinned;
+  char* dp = (char*)dbuf;
+  memcpy(hp, h_qpts, sizeof(tsim_point) * npts);
+  memcpy(hp + tsim::align256(sizeof(tsim_point) * npts), h_qoff, 8 * (nq + 1));
+  TSIM_CUDA(cudaMemcpyAsync(dp, hp, in_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  int* d_ids = (int*)(dp + in_bytes);
+  float* d_d = (float*)(dp + in_bytes + tsim::align256(sizeof(int) * nq * p->k));
+  TSIM_TRY(tsim_knn(ctx, p, (const tsim_point*)dp,
+                    (const int64_t*)(dp + tsim::align256(sizeof(tsim_point) * npts)), nq, max_qlen,
+                    db, d_ids, d_d, nullptr, stats));
+  TSIM_CUDA(cudaMemcpyAsync(hp + in_bytes, dp + in_bytes, out_bytes, cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+  memcpy(h_ids, hp + in_bytes, sizeof(int) * nq * p->k);
+  memcpy(h_dists, hp + in_bytes + tsim::align256(sizeof(int) * nq * p->k), sizeof(float) * nq * p->k);
+  return TSIM_OK;
+}

@@ -1,0 +1,336 @@
+// pairwise.cu -- tiled pairwise-distance reductions: symmetric Hausdorff
+// (max-min), lock-step Euclidean (sum), and the bounding-box candidate
+// generator that stands in for the reference's Boost R-tree.
+#include "topk.cuh"
+#include "tsim_internal.cuh"
+
+namespace tsim {
+
+// squared point distance without FMA: the reference CPU arithmetic
+// (hausdorff.cpp:77-79), so values match it bit for bit
+__device__ __forceinline__ float d2_exact(float ax, float ay, float bx, float by) {
+  float dx = ax - bx, dy = ay - by;
+  return __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+}
+
+namespace {
+
+constexpr int kHdThreads = 256;
+constexpr int kHdA = 4;  // source points per thread per pass
+
+// max over a in S of min over b in T of |a-b|^2, S and T in shared memory.
+// Stops early once the running max reaches `stop` (the pair cannot win).
+__device__ float directed_max_min(const float2* S, int ns, const float2* T, int nt, float seed,
+                                  const unsigned* best_bits, float* red) {
+  float run = seed;
+  for (int base = 0; base < ns; base += kHdThreads * kHdA) {
+    float ax[kHdA], ay[kHdA], mn[kHdA];
+#pragma unroll
+    for (int u = 0; u < kHdA; ++u) {
+      int i = base + u * kHdThreads + threadIdx.x;
+      float2 p = i < ns ? S[i] : S[0];
+      ax[u] = p.x;
+      ay[u] = p.y;
+      mn[u] = TSIM_INF;
+    }
+    for (int j = 0; j < nt; ++j) {
+      const float2 b = T[j];
+#pragma unroll
+      for (int u = 0; u < kHdA; ++u) mn[u] = fminf(mn[u], d2_exact(ax[u], ay[u], b.x, b.y));
+    }
+    float loc = 0.0f;
+#pragma unroll
+    for (int u = 0; u < kHdA; ++u)
+      if (base + u * kHdThreads + threadIdx.x < ns) loc = fmaxf(loc, mn[u]);
+    for (int o = 16; o; o >>= 1) loc = fmaxf(loc, __shfl_xor_sync(0xffffffffu, loc, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = loc;
+    __syncthreads();
+    float blk = run;
+    for (int w = 0; w < kHdThreads / 32; ++w) blk = fmaxf(blk, red[w]);
+    run = blk;
+    // a pair whose partial max already exceeds the query's best cannot win;
+    // thread 0 reads the (concurrently updated) best once for the whole CTA
+    if (threadIdx.x == 0)
+      red[kHdThreads / 32] =
+          (best_bits && run > __uint_as_float(*(volatile const unsigned*)best_bits)) ? 1.0f : 0.0f;
+    __syncthreads();
+    const bool stop = red[kHdThreads / 32] != 0.0f;
+    __syncthreads();
+    if (stop) return run;
+  }
+  return run;
+}
+
+// One CTA per (query, candidate slot): both trajectories in shared memory,
+// symmetric Hausdorff^2 = max(h(A,B), h(B,A)), atomic min into the query's
+// best (non-negative floats order like their bit patterns).
+__global__ void __launch_bounds__(kHdThreads)
+    hausdorff_cands_kernel(const float2* __restrict__ t1, int n, const float2* __restrict__ t2,
+                           int num_t2, int m, const int* __restrict__ cand, int top_k,
+                           unsigned* __restrict__ best_bits) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ float red[kHdThreads / 32 + 1];
+  float2* A = reinterpret_cast<float2*>(smem_raw);
+  float2* B = A + n;
+  const int q = blockIdx.x / top_k;
+  const int c = cand[blockIdx.x];
+  if (c < 0 || c >= num_t2) return;  // out-of-range candidate slots are ignored
+  const float2* ga = t1 + (size_t)q * n;
+  const float2* gb = t2 + (size_t)c * m;
+  for (int i = threadIdx.x; i < n; i += kHdThreads) A[i] = ga[i];
+  for (int i = threadIdx.x; i < m; i += kHdThreads) B[i] = gb[i];
+  __syncthreads();
+  float h1 = directed_max_min(A, n, B, m, 0.0f, best_bits + q, red);
+  float h = directed_max_min(B, m, A, n, h1, best_bits + q, red);
+  if (threadIdx.x == 0) atomicMin(best_bits + q, __float_as_uint(h));
+}
+
+__global__ void init_bits_kernel(unsigned* p, int count, unsigned v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) p[i] = v;
+}
+
+__global__ void sqrt_bits_kernel(const unsigned* bits, float* out, int count) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) out[i] = __fsqrt_rn(__uint_as_float(bits[i]));
+}
+
+// ---- lock-step Euclidean -----------------------------------------------------
+constexpr int kEuThreads = 128;
+
+// TwoSum: s + e == a + b exactly (Knuth)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Warp per CSR entry: compensated FP32 sum of squared point differences.
+__global__ void __launch_bounds__(kEuThreads)
+    euclid_cands_kernel(const float2* __restrict__ t1, const float2* __restrict__ t2,
+                        const int* __restrict__ cand, const int* __restrict__ off, int num_t, int n,
+                        int total, float* __restrict__ s32) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int e = gw; e < total; e += nw) {
+    // query owning entry e: binary search in off
+    int lo = 0, hi = num_t;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (off[mid] <= e) lo = mid; else hi = mid;
+    }
+    const int ce = cand[e];
+    if (ce < 0 || ce >= num_t) {  // out-of-range candidates never win
+      if (lane == 0) s32[e] = TSIM_INF;
+      continue;
+    }
+    const float2* a = t1 + (size_t)lo * n;
+    const float2* b = t2 + (size_t)ce * n;
+    float s = 0.0f, c = 0.0f;
+    for (int i = lane; i < n; i += 32) {
+      float2 p = a[i], r = b[i];
+      float dx = p.x - r.x, dy = p.y - r.y;
+      float t = fmaf(dy, dy, dx * dx);
+      float ns, err;
+      two_sum(s, t, ns, err);
+      s = ns;
+      c += err;
+    }
+    for (int o = 16; o; o >>= 1) {
+      float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+      float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+      float ns, err;
+      two_sum(s, s2, ns, err);
+      s = ns;
+      c = c + c2 + err;
+    }
+    if (lane == 0) s32[e] = s + c;
+  }
+}
+
+// Warp per query: candidates whose compensated FP32 sum lies within the
+// rigorous error margin of the smallest are re-scored in FP64, left to right
+// exactly like calc_exact_dist_sq (euclidean.cpp:27-40); out = (float)sqrt.
+__global__ void euclid_rescore_kernel(const float2* __restrict__ t1,
+                                      const float2* __restrict__ t2,
+                                      const int* __restrict__ cand, const int* __restrict__ off,
+                                      const float* __restrict__ s32, int num_t, int n, int total,
+                                      float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= num_t) return;
+  // clamp caller offsets into [0, total] so a malformed CSR cannot read out of bounds
+  const int b = min(max(off[q], 0), total), e = max(min(off[q + 1], total), b);
+  float mn = TSIM_INF;
+  for (int i = b + lane; i < e; i += 32) mn = fminf(mn, s32[i]);
+  for (int o = 16; o; o >>= 1) mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+  // |s32 - exact| <= g * exact with g = 2^-20 (terms 2u, TwoSum chain ~2u,
+  // final fold ~2u, n*u^2 negligible for n < 2^20)
+  const double g = 1.0 / (1 << 20);
+  const double thr = (double)mn * (1.0 + g) / (1.0 - g);
+  double best = 1.7976931348623157e308;
+  for (int i = b + lane; i < e; i += 32) {
+    if ((double)s32[i] > thr || cand[i] < 0 || cand[i] >= num_t) continue;
+    const float2* A = t1 + (size_t)q * n;
+    const float2* B = t2 + (size_t)cand[i] * n;
+    double s = 0.0;
+    for (int k = 0; k < n; ++k) {
+      double dx = (double)A[k].x - (double)B[k].x;
+      double dy = (double)A[k].y - (double)B[k].y;
+      s = __dadd_rn(s, __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    }
+    best = s < best ? s : best;
+  }
+  for (int o = 16; o; o >>= 1) {
+    double w = __shfl_xor_sync(0xffffffffu, best, o);
+    best = w < best ? w : best;
+  }
+  if (lane == 0) out[q] = e > b ? __double2float_rn(__dsqrt_rn(best)) : __double2float_rn(__dsqrt_rn(1.7976931348623157e308));
+}
+
+// ---- bounding boxes and box nearest neighbours --------------------------------
+__global__ void boxes_kernel(const float2* __restrict__ t, int count, int len,
+                             float4* __restrict__ box) {
+  const int lane = threadIdx.x & 31;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= count) return;
+  const float2* p = t + (size_t)w * len;
+  // sequential min/max semantics do not matter for the value of a min/max
+  float x0 = TSIM_INF, y0 = TSIM_INF, x1 = -TSIM_INF, y1 = -TSIM_INF;
+  for (int i = lane; i < len; i += 32) {
+    float2 v = p[i];
+    x0 = fminf(x0, v.x);
+    x1 = fmaxf(x1, v.x);
+    y0 = fminf(y0, v.y);
+    y1 = fmaxf(y1, v.y);
+  }
+  for (int o = 16; o; o >>= 1) {
+    x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+    y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+    x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+    y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+  }
+  if (lane == 0) box[w] = make_float4(x0, y0, x1, y1);
+}
+
+__device__ __forceinline__ float smaxf(float a, float b) { return (a < b) ? b : a; }
+
+__device__ __forceinline__ float box_box_d2(float4 a, float4 b) {
+  float dx = smaxf(0.0f, smaxf(__fsub_rn(a.x, b.z), __fsub_rn(b.x, a.z)));
+  float dy = smaxf(0.0f, smaxf(__fsub_rn(a.y, b.w), __fsub_rn(b.y, a.w)));
+  return __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+}
+
+constexpr int kSelThreads = 256;
+
+__global__ void __launch_bounds__(kSelThreads)
+    mbr_knn_kernel(const float4* __restrict__ qbox, const float4* __restrict__ cbox, int num_t2,
+                   int k, unsigned long long* __restrict__ gkeys, int* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long red[33];
+  const int q = blockIdx.x;
+  unsigned long long* keys =
+      gkeys ? gkeys + (size_t)q * num_t2 : reinterpret_cast<unsigned long long*>(smem_raw);
+  unsigned long long* sel =
+      reinterpret_cast<unsigned long long*>(smem_raw + (gkeys ? 0 : (size_t)num_t2 * 8));
+  const float4 a = qbox[q];
+  for (int j = threadIdx.x; j < num_t2; j += kSelThreads) keys[j] = pack_key(box_box_d2(a, cbox[j]), j);
+  __syncthreads();
+  block_select_k(keys, num_t2, min(k, num_t2), sel, red);
+  const int got = min(k, num_t2);
+  for (int e = threadIdx.x; e < k; e += kSelThreads)
+    out[(size_t)q * k + e] = e < got ? key_index(sel[e]) : (got > 0 ? key_index(sel[got - 1]) : 0);
+}
+
+}  // namespace
+
+int hausdorff_cands(tsim_ctx* ctx, const float2* t1, int num_t1, int n, const float2* t2, int num_t2,
+                    int m, const int* cand, int top_k, float* out) {
+  TSIM_TRY(arena_reserve(ctx, align256(sizeof(unsigned) * num_t1)));
+  unsigned* best = arena_take<unsigned>(ctx, num_t1);
+  init_bits_kernel<<<(num_t1 + 255) / 256, 256, 0, ctx->stream>>>(best, num_t1, 0x7f800000u);
+  size_t smem = sizeof(float2) * ((size_t)n + m);
+  TSIM_CHECK_ARG(smem <= 200 * 1024, "trajectories too long for the shared-memory Hausdorff kernel");
+  if (smem > 48 * 1024)
+    TSIM_CUDA(cudaFuncSetAttribute(hausdorff_cands_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if ((long long)num_t1 * top_k > 0)
+    hausdorff_cands_kernel<<<num_t1 * top_k, kHdThreads, smem, ctx->stream>>>(t1, n, t2, num_t2, m,
+                                                                              cand, top_k, best);
+  sqrt_bits_kernel<<<(num_t1 + 255) / 256, 256, 0, ctx->stream>>>(best, out, num_t1);
+  TSIM_CUDA(cudaGetLastError());
+  return TSIM_OK;
+}
+
+int euclid_cands(tsim_ctx* ctx, const float2* t1, const float2* t2, const int* cand, const int* off,
+                 int num_t, int n, int total, float* out) {
+  TSIM_TRY(arena_reserve(ctx, align256(sizeof(float) * std::max(total, 1))));
+  float* s32 = arena_take<float>(ctx, std::max(total, 1));
+  if (total > 0) {
+    int blocks = std::min((total + 3) / 4, ctx->num_sms * 16);
+    euclid_cands_kernel<<<blocks, kEuThreads, 0, ctx->stream>>>(t1, t2, cand, off, num_t, n, total,
+                                                               s32);
+  }
+  euclid_rescore_kernel<<<(num_t + 3) / 4, 128, 0, ctx->stream>>>(t1, t2, cand, off, s32, num_t, n,
+                                                                  total, out);
+  TSIM_CUDA(cudaGetLastError());
+  return TSIM_OK;
+}
+
+int mbr_knn(tsim_ctx* ctx, const float2* t1, int num_t1, int n, const float2* t2, int num_t2, int m,
+            int k, int* out) {
+  size_t key_bytes = sizeof(unsigned long long) * (size_t)num_t2;
+  bool in_smem = key_bytes + 64 * sizeof(unsigned long long) <= 200 * 1024;
+  size_t need = align256(sizeof(float4) * num_t1) + align256(sizeof(float4) * num_t2) +
+                (in_smem ? 0 : align256(key_bytes * num_t1) + align256((size_t)k * 4 * num_t1));
+  TSIM_TRY(arena_reserve(ctx, need));
+  float4* qb = arena_take<float4>(ctx, num_t1);
+  float4* cb = arena_take<float4>(ctx, num_t2);
+  unsigned long long* gkeys = in_smem ? nullptr : arena_take<unsigned long long>(ctx, (size_t)num_t2 * num_t1);
+  boxes_kernel<<<(num_t1 + 3) / 4, 128, 0, ctx->stream>>>(t1, num_t1, n, qb);
+  boxes_kernel<<<(num_t2 + 3) / 4, 128, 0, ctx->stream>>>(t2, num_t2, m, cb);
+  size_t smem = (in_smem ? key_bytes : 0) + 64 * sizeof(unsigned long long);
+  TSIM_CUDA(cudaFuncSetAttribute(mbr_knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  mbr_knn_kernel<<<num_t1, kSelThreads, smem, ctx->stream>>>(qb, cb, num_t2, k, gkeys, out);
+  TSIM_CUDA(cudaGetLastError());
+  return TSIM_OK;
+}
+
+}  // namespace tsim
+
+extern "C" {
+
+int tsim_hausdorff_cands(tsim_ctx* ctx, const tsim_point* d_t1, int num_t1, int n,
+                         const tsim_point* d_t2, int num_t2, int m, const int* d_cand, int top_k,
+                         float* d_out) {
+  TSIM_CHECK_ARG(ctx != nullptr, "ctx is NULL");
+  TSIM_CHECK_ARG(num_t1 >= 1 && num_t2 >= 1 && n >= 1 && m >= 1 && top_k >= 1, "sizes must be >= 1");
+  TSIM_CHECK_ARG(d_t1 && d_t2 && d_cand && d_out, "NULL device pointer");
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  return tsim::hausdorff_cands(ctx, (const float2*)d_t1, num_t1, n, (const float2*)d_t2, num_t2, m,
+                               d_cand, top_k, d_out);
+}
+
+int tsim_euclid_cands(tsim_ctx* ctx, const tsim_point* d_t1, const tsim_point* d_t2,
+                      const int* d_cand, const int* d_off, int num_t, int n, int total,
+                      float* d_out) {
+  TSIM_CHECK_ARG(ctx != nullptr, "ctx is NULL");
+  TSIM_CHECK_ARG(num_t >= 1 && n >= 1 && total >= 0, "bad sizes");
+  TSIM_CHECK_ARG(d_t1 && d_t2 && d_off && d_out && (total == 0 || d_cand), "NULL device pointer");
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  return tsim::euclid_cands(ctx, (const float2*)d_t1, (const float2*)d_t2, d_cand, d_off, num_t, n,
+                            total, d_out);
+}
+
+int tsim_mbr_knn(tsim_ctx* ctx, const tsim_point* d_t1, int num_t1, int n, const tsim_point* d_t2,
+                 int num_t2, int m, int k, int* d_out) {
+  TSIM_CHECK_ARG(ctx != nullptr, "ctx is NULL");
+  TSIM_CHECK_ARG(num_t1 >= 1 && num_t2 >= 1 && n >= 1 && m >= 1 && k >= 1 && k <= 64,
+                 "sizes must be >= 1 and k <= 64");
+  TSIM_CHECK_ARG(d_t1 && d_t2 && d_out, "NULL device pointer");
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  return tsim::mbr_knn(ctx, (const float2*)d_t1, num_t1, n, (const float2*)d_t2, num_t2, m, k, d_out);
+}
+
+}  // extern "C"

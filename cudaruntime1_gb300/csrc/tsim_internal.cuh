@@ -1,0 +1,201 @@
+// tsim_internal.cuh -- shared host/device internals of libtsim.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cfloat>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/tsim.h"
+
+#define TSIM_INF __int_as_float(0x7f800000)
+
+// ---------------------------------------------------------------------------
+// error reporting (host)
+// ---------------------------------------------------------------------------
+namespace tsim {
+
+void set_error(const std::string& msg);
+int fail(int status, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+}  // namespace tsim
+
+#define TSIM_CUDA(call)                                                       \
+  do {                                                                        \
+    cudaError_t _e = (call);                                                  \
+    if (_e != cudaSuccess) return tsim::cuda_fail(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define TSIM_CHECK_ARG(cond, msg)                                               \
+  do {                                                                          \
+    if (!(cond)) return tsim::fail(TSIM_ERR_INVALID_ARG, std::string(__func__) + ": " + (msg)); \
+  } while (0)
+
+#define TSIM_TRY(call)            \
+  do {                            \
+    int _s = (call);              \
+    if (_s != TSIM_OK) return _s; \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// context: device, stream and a grow-only scratch arena
+// ---------------------------------------------------------------------------
+struct tsim_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool owns_stream = false;
+  int num_sms = 0;
+  // scratch arena: one device block, bump-allocated per call, reset per call
+  char* arena = nullptr;
+  size_t arena_cap = 0;
+  size_t arena_used = 0;
+  // pinned host staging for the host-pointer entry points
+  void* pinned = nullptr;
+  size_t pinned_cap = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+struct tsim_db {
+  tsim_ctx* ctx = nullptr;
+  int count = 0;
+  int64_t total = 0;
+  int max_len = 0;
+  bool owns = false;
+  float2* pts = nullptr;      // device [total]
+  int64_t* off = nullptr;     // device [count+1]
+  float4* box = nullptr;      // device [count] (x0, y0, x1, y1)
+  float4* ends = nullptr;     // device [count] (first.x, first.y, last.x, last.y)
+  int* len = nullptr;         // device [count]
+  std::vector<int64_t> h_off; // host copy of offsets (lengths for scheduling)
+};
+
+namespace tsim {
+
+// Reserve `bytes` (256-byte aligned) of arena scratch.  The arena only grows
+// between calls (arena_reserve); inside a call, allocation never reallocates.
+int arena_reserve(tsim_ctx* ctx, size_t bytes);
+template <class T>
+T* arena_take(tsim_ctx* ctx, size_t count) {
+  size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+  if (ctx->arena_used + bytes > ctx->arena_cap) return nullptr;
+  T* p = reinterpret_cast<T*>(ctx->arena + ctx->arena_used);
+  ctx->arena_used += bytes;
+  return p;
+}
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+int pinned_reserve(tsim_ctx* ctx, size_t bytes);
+
+// ---------------------------------------------------------------------------
+// band geometry (host + device), identical to oracle/oracle.c orc_band_*
+// ---------------------------------------------------------------------------
+__host__ __device__ inline int band_w(int n, int m, int band_pct) {
+  if (band_pct < 0) return -1;
+  int L = n > m ? n : m;
+  return (int)(((long long)band_pct * L + 99) / 100);
+}
+
+__host__ __device__ inline long long floordiv_ll(long long a, long long b) {
+  long long q = a / b;
+  if ((a % b != 0) && ((a < 0) != (b < 0))) q--;
+  return q;
+}
+
+// Columns of row i inside |i*(m-1) - j*(n-1)| <= w*(min(n,m)-1); hi < lo when
+// empty; w < 0 gives the whole row.
+__host__ __device__ inline void band_row(int i, int n, int m, int w, int& lo, int& hi) {
+  if (w < 0 || n <= 1) {
+    lo = 0;
+    hi = m - 1;
+    return;
+  }
+  long long mn = (n < m ? n : m) - 1;
+  long long W = (long long)w * mn;
+  long long c = (long long)i * (m - 1);
+  long long l = -floordiv_ll(-(c - W), n - 1);
+  long long h = floordiv_ll(c + W, n - 1);
+  lo = (int)(l < 0 ? 0 : l);
+  hi = (int)(h > m - 1 ? m - 1 : h);
+}
+
+// LCSS index window |i-j| <= delta (delta < 0: whole row)
+__host__ __device__ inline void window_row(int i, int m, int delta, int& lo, int& hi) {
+  if (delta < 0) {
+    lo = 0;
+    hi = m - 1;
+    return;
+  }
+  lo = i - delta < 0 ? 0 : i - delta;
+  hi = i + delta > m - 1 ? m - 1 : i + delta;
+}
+
+// order-preserving float -> uint32 (total order for non-NaN floats)
+__host__ __device__ inline unsigned f2ord(float f) {
+#ifdef __CUDA_ARCH__
+  unsigned u = __float_as_uint(f);
+#else
+  unsigned u;
+  memcpy(&u, &f, 4);
+#endif
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ inline float ord2f(unsigned u) {
+  u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers implemented in the .cu files
+// ---------------------------------------------------------------------------
+struct DpArgs {
+  const float2* qpts;
+  const int64_t* qoff;
+  const float2* cpts;
+  const int64_t* coff;
+  const int2* pairs;  // (query, candidate)
+  int npairs;
+  float* out;         // per pair: distance (FP32 domain) or LCSS count
+  double* out64;      // per pair, FP64 kinds
+  const int* npairs_dev;  // when set, the pair count is min(*npairs_dev, npairs)
+  const float* thr;   // per query abandon threshold, or null
+  int band_pct;       // DTW/Frechet band, <0 none
+  int delta;          // LCSS window, <0 none
+  float eps;          // LCSS threshold
+  int buf_len;        // shared-memory values per segment (>= max candidate length)
+};
+
+enum DpKind {
+  DP_DTW_REF = 0,   // Euclidean cost, no FMA: the reference's dtw.cpp arithmetic
+  DP_FRECHET_REF,   // Euclidean distance, no FMA: frechet.cpp arithmetic
+  DP_LCSS,          // integer LCSS, strict |d| < eps per coordinate
+  DP_DTW_SQ,        // squared cost, FMA (error bounded, FP64 re-score after)
+  DP_DTW_EU,        // Euclidean cost, FMA
+  DP_FRECHET_SQ,    // squared-domain Frechet, FMA
+  DP_DTW_SQ64,      // FP64 re-score kinds: the FP64 oracle's arithmetic
+  DP_DTW_EU64,
+  DP_FRECHET_SQ64,
+  DP_NUM_KINDS
+};
+
+int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
+        int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st);
+int knn_pairwise(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff,
+                 int nq, int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64,
+                 tsim_stats* st);
+
+// G lanes per pair (4, 8, 16 or 32), R rows per lane (1, 2, 4 or 8).
+int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a, int max_m);
+// choose (G, R) for pairs of shape n x m under band w
+void dp_shape(int kind, int n, int m, int band_w_or_delta, int& G, int& R);
+
+}  // namespace tsim

@@ -1,0 +1,166 @@
+/*
+ * tsim.h -- C ABI of the GB300 trajectory-similarity kNN engine (libtsim.so).
+ *
+ * Plain C: pointers, sizes and status codes; no C++ or torch types.  Every
+ * entry point returns a tsim_status; tsim_last_error() gives the message of
+ * the last failure on the calling thread.  Nothing here ever calls exit():
+ * the reference's CHECK macro (CudaRuntime1/common.cuh:14-22) terminates the
+ * process, this ABI reports instead.
+ *
+ * Points are `tsim_point {float x, y;}`, the same 8-byte layout as the
+ * reference's `struct Point` (CudaRuntime1/common.cuh:9-11).  Trajectory sets
+ * are CSR: points[off[t] .. off[t+1]) is trajectory t.
+ *
+ * Two families of entry points:
+ *  - reference-semantics batch calls (tsim_ref_*), one value per query,
+ *    reproducing the reference's filter -> top-10 -> refine -> reduce
+ *    results bit for bit (DTW, LCSS, Frechet) or from given candidates
+ *    (Hausdorff, Euclidean); the reference-named C++ functions in
+ *    include/compat/ are thin wrappers over these;
+ *  - exact kNN (tsim_knn*): rectangular query x database, variable lengths,
+ *    top-k ids and distances, lower-bound pruning that never drops a true
+ *    neighbour, FP64 re-score of the survivors; ids ranked by
+ *    (distance, candidate index), LCSS by (count descending, index).
+ */
+#ifndef TSIM_H
+#define TSIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define TSIM_API __attribute__((visibility("default")))
+#else
+#define TSIM_API
+#endif
+
+typedef struct tsim_point {
+  float x, y;
+} tsim_point;
+
+typedef enum tsim_status {
+  TSIM_OK = 0,
+  TSIM_ERR_INVALID_ARG = 1,
+  TSIM_ERR_CUDA = 2,
+  TSIM_ERR_OUT_OF_MEMORY = 3,
+  TSIM_ERR_TIMEOUT = 4, /* a bounded device-side wait ran out */
+  TSIM_ERR_UNSUPPORTED = 5,
+  TSIM_ERR_BUDGET = 6 /* request exceeds the admission budget */
+} tsim_status;
+
+typedef enum tsim_measure {
+  TSIM_DTW = 0,
+  TSIM_LCSS = 1,
+  TSIM_FRECHET = 2,
+  TSIM_HAUSDORFF = 3,
+  TSIM_EUCLIDEAN = 4
+} tsim_measure;
+
+typedef enum tsim_cost {
+  TSIM_COST_SQEUCLID = 0, /* DTW cell cost |a-b|^2 */
+  TSIM_COST_EUCLID = 1    /* DTW cell cost |a-b| (the reference's, dtw.cpp:90) */
+} tsim_cost;
+
+/* tsim_params.flags */
+#define TSIM_FLAG_NO_PRUNE 0x1u /* compute every pair (no lower bounds) */
+#define TSIM_FLAG_PLAIN 0x2u    /* "plain" form: one DP pair per kernel launch */
+#define TSIM_FLAG_NO_GRAPH 0x4u /* do not replay through a captured CUDA graph */
+
+typedef struct tsim_params {
+  int measure;    /* tsim_measure */
+  int k;          /* neighbours per query, 1..64 */
+  int cost;       /* DTW only: tsim_cost */
+  int band_pct;   /* DTW only: Sakoe-Chiba band, percent of max(n,m); <0 = none */
+  float epsilon;  /* LCSS only: per-coordinate match threshold, |dx| < eps */
+  int delta;      /* LCSS only: index window |i-j| <= delta; <0 = none */
+  unsigned flags; /* TSIM_FLAG_* */
+} tsim_params;
+
+typedef struct tsim_stats {
+  double ms;              /* device time of the call (CUDA events) */
+  int64_t pairs;          /* query x candidate pairs in the request */
+  int64_t pairs_refined;  /* pairs that reached the exact DP / distance */
+  int64_t cells;          /* DP cells (or point pairs) actually computed */
+  int64_t cells_unpruned; /* DP cells (or point pairs) of all pairs, in band */
+  int64_t rescored;       /* pairs re-scored in FP64 */
+  int32_t launches;       /* kernels launched (graph replays count their nodes) */
+  int32_t graph_replay;   /* 1 when the call replayed a captured graph */
+} tsim_stats;
+
+typedef struct tsim_ctx tsim_ctx; /* device, stream, scratch, tuning cache */
+typedef struct tsim_db tsim_db;   /* device-resident candidate set + summaries */
+
+TSIM_API const char* tsim_status_string(int status);
+TSIM_API const char* tsim_last_error(void);
+TSIM_API int tsim_version(void);
+
+/* ---- context ------------------------------------------------------------ */
+/* stream: a cudaStream_t, or NULL for a stream the context creates. */
+TSIM_API int tsim_ctx_create(int device, void* stream, tsim_ctx** out);
+TSIM_API int tsim_ctx_destroy(tsim_ctx* ctx);
+TSIM_API int tsim_ctx_set_stream(tsim_ctx* ctx, void* stream);
+TSIM_API int tsim_ctx_synchronize(tsim_ctx* ctx);
+/* bytes of device scratch the context currently holds */
+TSIM_API int64_t tsim_ctx_scratch_bytes(const tsim_ctx* ctx);
+
+/* ---- device-resident candidate database ---------------------------------- */
+/* Copies host points/offsets to the device and builds per-trajectory
+ * summaries (bounding box, first/last point). */
+TSIM_API int tsim_db_create(tsim_ctx* ctx, const tsim_point* host_pts, const int64_t* host_off,
+                            int count, tsim_db** out);
+/* Wraps device-resident points/offsets (not copied, caller keeps them alive). */
+TSIM_API int tsim_db_wrap_device(tsim_ctx* ctx, const tsim_point* dev_pts,
+                                 const int64_t* dev_off, int count, int max_len, tsim_db** out);
+TSIM_API int tsim_db_destroy(tsim_db* db);
+TSIM_API int tsim_db_count(const tsim_db* db);
+TSIM_API int64_t tsim_db_device_bytes(const tsim_db* db);
+
+/* ---- exact kNN ------------------------------------------------------------ */
+/* Device pointers; results d_ids[nq*k], d_dists[nq*k] (float, from the FP64
+ * re-score), d_dists64 optional (may be NULL).  LCSS distances are the
+ * integer match counts.  Asynchronous on the context stream unless stats is
+ * non-NULL (then the call synchronises to fill it). */
+TSIM_API int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
+                      const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
+                      float* d_dists, double* d_dists64, tsim_stats* stats);
+/* Host pointers end to end: copies the queries in and the results out. */
+TSIM_API int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_point* h_qpts,
+                           const int64_t* h_qoff, int nq, tsim_db* db, int* h_ids,
+                           float* h_dists, tsim_stats* stats);
+
+/* ---- reference-semantics batch calls (device pointers) -------------------- */
+/* DTW (Euclidean cell cost), LCSS (count/min(n,m)), Frechet: num_t queries of
+ * length n against num_t candidates of length m, out[num_t].  The r=5
+ * envelope bound ranks all candidates, the K=min(10,num_t) best by (bound,
+ * index) (LCSS: bound descending, then index) are refined exactly, out[i] is
+ * the best refined value (CudaRuntime1/dtw.cpp:14-113, lcss.cpp:13-115,
+ * frechet.cpp:13-124). */
+TSIM_API int tsim_ref_batch(tsim_ctx* ctx, int measure, const tsim_point* d_t1,
+                            const tsim_point* d_t2, int num_t, int n, int m, float epsilon,
+                            float* d_out);
+/* Min over the given candidates of the symmetric Hausdorff distance
+ * (CudaRuntime1/hausdorff.cu:84-122). d_cand[num_t1*top_k]. */
+TSIM_API int tsim_hausdorff_cands(tsim_ctx* ctx, const tsim_point* d_t1, int num_t1, int n,
+                                  const tsim_point* d_t2, int num_t2, int m, const int* d_cand,
+                                  int top_k, float* d_out);
+/* Min over CSR candidates of the lock-step Euclidean distance
+ * (CudaRuntime1/euclidean.cu:17-73); bit-identical to the FP64 CPU path
+ * (euclidean.cpp:27-40): FP32 compensated sums rank, FP64 re-scores. */
+TSIM_API int tsim_euclid_cands(tsim_ctx* ctx, const tsim_point* d_t1, const tsim_point* d_t2,
+                               const int* d_cand, const int* d_off, int num_t, int n,
+                               int total_candidates, float* d_out);
+/* Bounding-box nearest neighbours, the candidate generator that replaces the
+ * reference's Boost R-tree query (hausdorff_rtree.cpp:38-69,
+ * euclidean_rtree.cpp:49-69): the k nearest boxes by squared box-box
+ * distance, ties by index, padded with the last one when num_t2 < k. */
+TSIM_API int tsim_mbr_knn(tsim_ctx* ctx, const tsim_point* d_t1, int num_t1, int n,
+                          const tsim_point* d_t2, int num_t2, int m, int k, int* d_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

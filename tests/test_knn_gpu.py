@@ -1,0 +1,107 @@
+"""Exact kNN on the GPU against the FP64 brute-force oracle: ids bit-exact
+(ties by candidate index), FP64 distances bit-identical, float distances
+within 1e-5 relative (they are the FP64 values rounded once)."""
+import numpy as np
+import pytest
+
+from cudaruntime1_gb300 import datagen as G
+
+pytestmark = pytest.mark.gpu
+REL_TOL = 1e-5
+
+
+def _db(nc, lo, hi, seed, step="normal"):
+    lens = G.uniform_lengths(nc, lo, hi, seed)
+    return G.random_walks(nc, lens, seed + 1, step=step)
+
+
+def _device_knn(tsim, ctx, db, qp, qo, measure, k, **kw):
+    import torch
+    qpt = torch.from_numpy(qp).cuda()
+    qot = torch.from_numpy(np.asarray(qo, np.int64)).cuda()
+    nq = len(qo) - 1
+    ids = torch.empty(nq * k, dtype=torch.int32, device="cuda")
+    d = torch.empty(nq * k, dtype=torch.float32, device="cuda")
+    d64 = torch.empty(nq * k, dtype=torch.float64, device="cuda")
+    maxq = int(np.max(np.diff(qo)))
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    st = tsim.knn_device(ctx, db, qpt.data_ptr(), qot.data_ptr(), nq, maxq, ids.data_ptr(),
+                         d.data_ptr(), d64.data_ptr(), measure, k, stats=True, **kw)
+    torch.cuda.synchronize()
+    return (ids.cpu().numpy().reshape(nq, k), d.cpu().numpy().reshape(nq, k),
+            d64.cpu().numpy().reshape(nq, k), st)
+
+
+CASES = [
+    ("dtw", dict(band_pct=10, cost=0)),
+    ("dtw", dict(band_pct=-1, cost=0)),
+    ("dtw", dict(band_pct=20, cost=1)),
+    ("lcss", dict(epsilon=0.5, delta=5)),
+    ("lcss", dict(epsilon=0.25, delta=-1)),
+    ("frechet", dict()),
+]
+
+
+@pytest.mark.parametrize("measure,kw", CASES)
+def test_knn_matches_fp64_oracle(tsim, cuda_ctx, oracle, measure, kw):
+    cp, co = _db(700, 16, 120, 100)
+    ql = G.uniform_lengths(9, 16, 120, 7)
+    qp, qo = G.random_walks(9, ql, 8)
+    k = 10
+    db = tsim.Database(cuda_ctx, cp, co)
+    okw = dict(kw)
+    if "epsilon" in okw:
+        okw["eps"] = okw.pop("epsilon")
+    want_ids, want_d = oracle.knn(measure, qp, qo, cp, co, k, **okw)
+    ids, d, d64, st = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, k, **kw)
+    assert np.array_equal(ids, want_ids), (ids, want_ids)
+    if measure == "lcss":
+        assert np.array_equal(d.astype(np.float64), want_d)
+    else:
+        assert np.array_equal(d64, want_d)
+        fin = np.isfinite(want_d)
+        rel = np.abs(d.astype(np.float64)[fin] - want_d[fin]) / np.maximum(want_d[fin], 1e-30)
+        assert rel.max() <= REL_TOL
+    # the host-pointer entry point gives the same answer
+    ids_h, d_h, _ = tsim.knn(cuda_ctx, db, qp, qo, measure, k, **kw)
+    assert np.array_equal(ids_h, ids) and np.array_equal(d_h, d)
+    db.close()
+
+
+def test_knn_edge_cases(tsim, cuda_ctx, oracle):
+    # fewer candidates than k; single-point trajectories; duplicates (ties)
+    cp, co = _db(5, 1, 6, 300)
+    qp, qo = G.random_walks(3, [1, 4, 6], 301)
+    db = tsim.Database(cuda_ctx, cp, co)
+    for measure, kw, okw in [("dtw", dict(band_pct=10), dict(band_pct=10)),
+                             ("frechet", {}, {}),
+                             ("lcss", dict(epsilon=30.0, delta=2), dict(eps=30.0, delta=2))]:
+        want_ids, want_d = oracle.knn(measure, qp, qo, cp, co, 8, **okw)
+        ids, d, d64, _ = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 8, **kw)
+        assert np.array_equal(ids, want_ids), (measure, ids, want_ids)
+    db.close()
+    # exact duplicates in the database: ties broken by index
+    base, bo = G.random_walks(4, 30, 400)
+    cp = np.concatenate([base, base[bo[1]:bo[2]], base[bo[1]:bo[2]]])
+    co = np.concatenate([bo, [bo[-1] + 30, bo[-1] + 60]])
+    db = tsim.Database(cuda_ctx, cp, co)
+    qp = base[bo[1]:bo[2]].copy()
+    qo = np.array([0, 30])
+    for measure in ("dtw", "frechet", "lcss"):
+        want_ids, _ = oracle.knn(measure, qp, qo, cp, co, 6)
+        ids, _, _, _ = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 6)
+        assert np.array_equal(ids, want_ids), (measure, ids, want_ids)
+        assert list(ids[0][:3]) == [1, 4, 5]
+    db.close()
+
+
+def test_knn_longer_queries_than_candidates(tsim, cuda_ctx, oracle):
+    cp, co = _db(300, 10, 40, 500)
+    qp, qo = G.random_walks(4, [200, 150, 90, 300], 501)
+    db = tsim.Database(cuda_ctx, cp, co)
+    for measure, kw, okw in [("dtw", dict(band_pct=30), dict(band_pct=30)),
+                             ("lcss", dict(epsilon=1.0, delta=4), dict(eps=1.0, delta=4))]:
+        want_ids, want_d = oracle.knn(measure, qp, qo, cp, co, 5, **okw)
+        ids, d, d64, _ = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 5, **kw)
+        assert np.array_equal(ids, want_ids), measure
+    db.close()
