@@ -1,0 +1,342 @@
+"""Benchmark: exact batched DTW kNN on one GB300 (the batched uneven DTW workload).
+
+Workload: 64 query trajectories x 16,384 candidate trajectories, 2-D float32
+random walks (start uniform in [0,100)^2, N(0,1) steps), lengths uniform in
+[64, 512]; DTW with squared-Euclidean cell cost, Sakoe-Chiba band of 10% of
+the longer length, LB_Kim + LB_Keogh pruning, top-10 per query.  One step =
+one exact kNN pass of all 64 queries over the device-resident database.
+
+Reported: kNN queries/s of the batched form (device-resident inputs, CUDA
+events), end-to-end queries/s through the host-pointer C-ABI entry point
+(tsim_knn_host: H2D of the queries and D2H of ids/distances inside the timed
+region), queries/s of the plain one-pair-per-launch form (same algorithm,
+bounded sample), GCUPS, the roofline of the dominant kernel, measured error
+against the FP64 CPU oracle, and the CPU baseline (oracle port, all cores).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DTW kNN queries/s (batched, exact top-10, <=1e-5 rel err vs FP64)"
+UNIT = "queries/s"
+WORKLOAD = dict(workload="dtw_knn_batched_uneven", queries=64, candidates=16384, len_lo=64,
+                len_hi=512, band_pct=10, cost="squared_euclidean", k=10, seed=2024)
+DP_FLOPS_PER_CELL = 8  # 2 sub, mul, fma (2), 2 min, add
+L2_FLUSH_BYTES = 512 << 20
+
+
+def make_data(w=WORKLOAD):
+    from cudaruntime1_gb300 import datagen as G
+    s = w["seed"]
+    cl = G.uniform_lengths(w["candidates"], w["len_lo"], w["len_hi"], s)
+    ql = G.uniform_lengths(w["queries"], w["len_lo"], w["len_hi"], s + 1)
+    cp, co = G.random_walks(w["candidates"], cl, s + 2)
+    qp, qo = G.random_walks(w["queries"], ql, s + 3)
+    return qp, qo, cp, co
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_baseline(qp, qo, cp, co, w, min_seconds=10.0):
+    """The oracle's exact pruned DTW kNN (the reference's CPU algorithm made
+    exact and rectangular), all host threads, repeated to ~10 s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build(ref=False)
+    threads = O.num_threads()
+    runs, t0 = 0, time.perf_counter()
+    while True:
+        ids, d, cells = O.dtw_knn_pruned(qp, qo, cp, co, w["k"], band_pct=w["band_pct"],
+                                         cost=O.COST_SQEUCLID, nthreads=threads)
+        runs += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or runs >= 50:
+            break
+    qps = runs * (len(qo) - 1) / el
+    return {"value": qps, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{runs} full passes of {len(qo) - 1} queries x {len(co) - 1} candidates "
+                      f"(oracle dtw_knn_pruned, FP64, OpenMP), {el:.1f} s"}, ids, d, cells
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+    return rank, ws, local
+
+
+def run_reference(args):
+    rank, ws, _ = dist_init()
+    if rank != 0:
+        return
+    qp, qo, cp, co = make_data()
+    base, _, _, _ = cpu_baseline(qp, qo, cp, co, WORKLOAD, min_seconds=max(5.0, 2.0 * args.steps))
+    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": dict(WORKLOAD),
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="only the warm-up and timed steps (for profiler launch lists)")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+
+    import cudaruntime1_gb300 as T
+    from cudaruntime1_gb300 import api
+
+    rank, ws, local = dist_init()
+    dev = local
+    torch.cuda.set_device(dev)
+    T.build()
+    # an explicit stream: the library, torch's events and the L2 flush all use it
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    w = WORKLOAD
+    qp, qo, cp, co = make_data()
+    nq, k = len(qo) - 1, w["k"]
+    ctx = T.Context(dev, stream.cuda_stream)
+    db = T.Database(ctx, cp, co)
+    qpt = torch.from_numpy(qp).to(f"cuda:{dev}")
+    qot = torch.from_numpy(qo).to(f"cuda:{dev}")
+    ids = torch.empty(nq * k, dtype=torch.int32, device=f"cuda:{dev}")
+    dd = torch.empty(nq * k, dtype=torch.float32, device=f"cuda:{dev}")
+    d64 = torch.empty(nq * k, dtype=torch.float64, device=f"cuda:{dev}")
+    maxq = int(np.max(np.diff(qo)))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    kw = dict(band_pct=w["band_pct"], cost=api.COST_SQEUCLID)
+
+    def step():
+        api.knn_device(ctx, db, qpt.data_ptr(), qot.data_ptr(), nq, maxq, ids.data_ptr(),
+                       dd.data_ptr(), d64.data_ptr(), "dtw", k, **kw)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ctx.counters(reset=True)
+
+    # ---- timed region: device-resident inputs, L2 flushed before every step
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for s, e in evs:
+            flush.zero_()
+            s.record(stream)
+            step()
+            e.record(stream)
+        torch.cuda.synchronize()
+    step_ms = [s.elapsed_time(e) for s, e in evs]
+    total_ms = sum(step_ms)
+    cnt = ctx.counters(reset=True)
+    launches = cnt["launches"]
+    if ws > 1:
+        t = torch.tensor([total_ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ws * nq * args.steps / (total_ms / 1e3)
+    res_ids = ids.cpu().numpy().reshape(nq, k)
+    res_d64 = d64.cpu().numpy().reshape(nq, k)
+    if args.kernels_only:
+        print(json.dumps({"kernels_only": True, "ms_per_step": total_ms / args.steps,
+                          "launches": launches}))
+        return
+
+    # ---- per-stage device times (CUDA events on the launching stream)
+    ctx.set_profiling(True)
+    prof_steps = 5
+    for _ in range(prof_steps):
+        flush.zero_()
+        step()
+    prof = ctx.counters(reset=True)
+    ctx.set_profiling(False)
+    stage_ms = {s: v / prof_steps for s, v in prof["stage_ms"].items() if v > 0}
+    dp_cells = prof["dp_cells"] / prof_steps
+    dp_launch_ms = stage_ms.get("dp", 0.0) / max(1, prof["stage_calls"]["dp"] / prof_steps)
+    band_cells = api.band_cells(ctx, db, qpt.data_ptr(), qot.data_ptr(), nq, "dtw",
+                                band_pct=w["band_pct"])
+    fp32_peak = ctx.probe_fp32_tflops()
+
+    # ---- plain form: one DP pair per kernel launch, bounded sample of queries
+    nplain = 4
+    qo_p = qo[:nplain + 1]
+    qp_p = qp[:qo_p[-1]]
+    ids_p, _, _ = T.knn(ctx, db, qp_p, qo_p, "dtw", k, flags=api.FLAG_PLAIN, **kw)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ids_p, _, st_p = T.knn(ctx, db, qp_p, qo_p, "dtw", k, flags=api.FLAG_PLAIN, **kw)
+    plain_s = time.perf_counter() - t0
+    plain_qps = nplain / plain_s
+    plain_ok = bool(np.array_equal(ids_p, res_ids[:nplain]))
+    ctx.counters(reset=True)
+
+    # ---- end to end: host arrays through the C-ABI host entry point
+    h2d = qp.nbytes + qo.nbytes
+    d2h = nq * k * (4 + 4)
+    for _ in range(2):
+        T.knn(ctx, db, qp, qo, "dtw", k, **kw)
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        T.knn(ctx, db, qp, qo, "dtw", k, **kw)
+        e2e_ms += (time.perf_counter() - t0) * 1e3
+    e2e_qps = ws * nq * args.steps / (e2e_ms / 1e3)
+
+    line = None
+    if rank == 0:
+        # ---- CPU baseline and parity against the FP64 oracle on this workload
+        base = None
+        ids_match = None
+        max_rel = None
+        if not args.no_cpu:
+            base, oids, od, ocells = cpu_baseline(qp, qo, cp, co, w)
+            ids_match = bool(np.array_equal(oids, res_ids))
+            fin = np.isfinite(od)
+            max_rel = float(np.max(np.abs(res_d64[fin] - od[fin]) / np.maximum(od[fin], 1e-300)))
+            dd_f = dd.cpu().numpy().reshape(nq, k).astype(np.float64)
+            max_rel = max(max_rel, float(np.max(np.abs(dd_f[fin] - od[fin]) / od[fin])))
+        peaks = measured_peaks()
+        step_s = total_ms / args.steps / 1e3
+        dominant = max(stage_ms, key=stage_ms.get) if stage_ms else "dp"
+        achieved = dp_cells * DP_FLOPS_PER_CELL / (dp_launch_ms * 1e-3) / 1e12 if dp_launch_ms else 0
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(w, l2="flushed before every timed step (512 MiB write)",
+                           inputs_bytes=int(cp.nbytes + co.nbytes + qp.nbytes)),
+            "gcups": dp_cells / (step_s * 1e9),
+            "gcups_effective": band_cells / (step_s * 1e9),
+            "dp_cells_per_step": dp_cells, "band_cells_per_step": band_cells,
+            "survivor_cell_frac": dp_cells / band_cells if band_cells else None,
+            "stage_ms": stage_ms, "dominant_stage": dominant,
+            "plain": {"value": plain_qps, "unit": UNIT, "sample_queries": nplain,
+                      "ids_match_batched": plain_ok},
+            "batched_vs_plain": value / plain_qps if plain_qps else None,
+            "parity": {"ids_bit_exact_vs_fp64_oracle": ids_match, "max_rel_err": max_rel},
+            "roofline": {
+                "kernel": "dp_pairs_kernel (FP32 wavefront DTW of the surviving pairs)",
+                "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                "peak_source": "measured FP32 FMA probe kernel on this GPU (tsim_probe_fp32_tflops)",
+                "flops_per_cell": DP_FLOPS_PER_CELL,
+                "dp_launch_ms": dp_launch_ms},
+            "cpu_baseline": base,
+            "e2e": {"value": e2e_qps, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "hbm_peak_gbs": peaks.get("hbm_gbs"),
+        }
+        print(json.dumps(line))
+    db.close()
+    ctx.close()
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

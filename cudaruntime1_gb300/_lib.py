@@ -21,6 +21,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device mem
 DTW, LCSS, FRECHET, HAUSDORFF, EUCLIDEAN = range(5)
 COST_SQEUCLID, COST_EUCLID = 0, 1
 FLAG_NO_PRUNE, FLAG_PLAIN, FLAG_NO_GRAPH = 1, 2, 4
+STAGES = ["summary", "lb1", "seed", "filter", "dp", "select", "rescore", "ref"]
 
 _vp = C.c_void_p
 _ip = C.POINTER(C.c_int)
@@ -90,6 +91,12 @@ def load(build_if_missing: bool = False):
                                   C.c_int),
             "tsim_mbr_knn": ([_vp, _vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, C.c_int, _vp],
                              C.c_int),
+            "tsim_ctx_set_profiling": ([_vp, C.c_int], C.c_int),
+            "tsim_ctx_counters": ([_vp, C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int], C.c_int),
+            "tsim_probe_fp32_tflops": ([_vp, C.POINTER(C.c_double)], C.c_int),
+            "tsim_band_cells": ([_vp, C.POINTER(TsimParams), _vp, _vp, C.c_int, _vp,
+                                 C.POINTER(C.c_int64)], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

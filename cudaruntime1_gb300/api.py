@@ -142,6 +142,28 @@ class Context:
     def scratch_bytes(self) -> int:
         return self.L.tsim_ctx_scratch_bytes(self.h)
 
+    def set_profiling(self, on: bool):
+        """Per-stage CUDA-event timing on the context stream."""
+        check(self.L.tsim_ctx_set_profiling(self.h, 1 if on else 0))
+
+    def counters(self, reset: bool = True) -> dict:
+        """Stage times (ms), stage calls, kernels launched, DP cells computed
+        since the last reset (synchronises the stream)."""
+        n = len(_lib.STAGES)
+        ms = (C.c_double * n)()
+        calls = (C.c_int64 * n)()
+        launches, cells = C.c_int64(), C.c_int64()
+        check(self.L.tsim_ctx_counters(self.h, ms, calls, C.byref(launches), C.byref(cells),
+                                       1 if reset else 0))
+        return {"stage_ms": {s: ms[i] for i, s in enumerate(_lib.STAGES)},
+                "stage_calls": {s: calls[i] for i, s in enumerate(_lib.STAGES)},
+                "launches": launches.value, "dp_cells": cells.value}
+
+    def probe_fp32_tflops(self) -> float:
+        v = C.c_double()
+        check(self.L.tsim_probe_fp32_tflops(self.h, C.byref(v)))
+        return v.value
+
     def close(self):
         if getattr(self, "h", None):
             self.L.tsim_ctx_destroy(self.h)
@@ -234,3 +256,13 @@ def ref_batch_device(ctx: Context, measure: str, t1_ptr: int, t2_ptr: int, num_t
                      m: int, out_ptr: int, epsilon: float = 0.5):
     check(ctx.L.tsim_ref_batch(ctx.h, MEASURES[measure], C.c_void_p(t1_ptr), C.c_void_p(t2_ptr),
                                num_t, n, m, C.c_float(epsilon), C.c_void_p(out_ptr)))
+
+
+def band_cells(ctx: Context, db: Database, qpts_ptr: int, qoff_ptr: int, nq: int, measure: str,
+               **kw) -> int:
+    """Band cells of every query x database pair (the unpruned DP work)."""
+    p = make_params(measure, 1, **kw)
+    v = C.c_int64()
+    check(ctx.L.tsim_band_cells(ctx.h, C.byref(p), C.c_void_p(qpts_ptr), C.c_void_p(qoff_ptr), nq,
+                                db.h, C.byref(v)))
+    return v.value

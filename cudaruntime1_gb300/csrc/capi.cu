@@ -100,6 +100,7 @@ int summarize(tsim_ctx* ctx, const float2* pts, const int64_t* off, int count, f
   int blocks = std::min((count + 7) / 8, ctx->num_sms * 16);
   summarize_kernel<<<blocks, 256, 0, ctx->stream>>>(pts, off, count, box, ends, len);
   TSIM_CUDA(cudaGetLastError());
+  launched(ctx);
   return TSIM_OK;
 }
 
@@ -112,9 +113,109 @@ int db_summarize(tsim_db* db) {
   return TSIM_OK;
 }
 
+void stage_begin(tsim_ctx* ctx, int stage) {
+  if (!ctx->profiling) return;
+  if (ctx->nstage_ev >= 64) stage_collect(ctx);
+  const int i = ctx->nstage_ev;
+  for (int e = 2 * i; e < 2 * i + 2; ++e)
+    if (!ctx->stage_ev[e]) cudaEventCreate(&ctx->stage_ev[e]);
+  ctx->stage_id[i] = stage;
+  cudaEventRecord(ctx->stage_ev[2 * i], ctx->stream);
+}
+
+void stage_end(tsim_ctx* ctx) {
+  if (!ctx->profiling) return;
+  cudaEventRecord(ctx->stage_ev[2 * ctx->nstage_ev + 1], ctx->stream);
+  ctx->nstage_ev++;
+}
+
+int stage_collect(tsim_ctx* ctx) {
+  if (ctx->nstage_ev == 0) return TSIM_OK;
+  TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int i = 0; i < ctx->nstage_ev; ++i) {
+    float ms = 0.0f;
+    TSIM_CUDA(cudaEventElapsedTime(&ms, ctx->stage_ev[2 * i], ctx->stage_ev[2 * i + 1]));
+    ctx->stage_ms[ctx->stage_id[i]] += ms;
+    ctx->stage_calls[ctx->stage_id[i]] += 1;
+  }
+  ctx->nstage_ev = 0;
+  return TSIM_OK;
+}
+
+namespace {
+
+// Independent FMA chains per thread; the result is stored so nothing is
+// eliminated.  flops = 2 * kChains * iters per thread.
+constexpr int kChains = 16;
+__global__ void __launch_bounds__(256) fp32_probe_kernel(float* out, int iters, float a, float b) {
+  float v[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) v[c] = threadIdx.x * 1e-3f + c;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) v[c] = fmaf(v[c], a, b);
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) s += v[c];
+  if (s == 123.456f) out[0] = s;
+}
+
+}  // namespace
+
 }  // namespace tsim
 
 using namespace tsim;
+
+extern "C" int tsim_ctx_set_profiling(tsim_ctx* ctx, int on) {
+  TSIM_CHECK_ARG(ctx != nullptr, "ctx is NULL");
+  if (!on) TSIM_TRY(stage_collect(ctx));
+  ctx->profiling = on != 0;
+  return TSIM_OK;
+}
+
+extern "C" int tsim_ctx_counters(tsim_ctx* ctx, double* ms, int64_t* calls, int64_t* launches,
+                                 int64_t* dp_cells, int reset) {
+  TSIM_CHECK_ARG(ctx != nullptr, "ctx is NULL");
+  TSIM_TRY(stage_collect(ctx));
+  TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int s = 0; s < TSIM_STAGE_COUNT; ++s) {
+    if (ms) ms[s] = ctx->stage_ms[s];
+    if (calls) calls[s] = ctx->stage_calls[s];
+  }
+  if (launches) *launches = ctx->launches;
+  unsigned long long cells = 0;
+  TSIM_CUDA(cudaMemcpy(&cells, ctx->dcounters, sizeof(cells), cudaMemcpyDeviceToHost));
+  if (dp_cells) *dp_cells = (int64_t)cells;
+  if (reset) {
+    for (int s = 0; s < TSIM_STAGE_COUNT; ++s) {
+      ctx->stage_ms[s] = 0.0;
+      ctx->stage_calls[s] = 0;
+    }
+    ctx->launches = 0;
+    TSIM_CUDA(cudaMemsetAsync(ctx->dcounters, 0, 64, ctx->stream));
+    TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  return TSIM_OK;
+}
+
+extern "C" int tsim_probe_fp32_tflops(tsim_ctx* ctx, double* tflops) {
+  TSIM_CHECK_ARG(ctx && tflops, "NULL argument");
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  const int blocks = ctx->num_sms * 8, threads = 256, iters = 4096;
+  float* out = reinterpret_cast<float*>(ctx->dcounters) + 8;
+  fp32_probe_kernel<<<blocks, threads, 0, ctx->stream>>>(out, 64, 1.0000001f, 1e-7f);  // warm
+  TSIM_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+  fp32_probe_kernel<<<blocks, threads, 0, ctx->stream>>>(out, iters, 1.0000001f, 1e-7f);
+  TSIM_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+  TSIM_CUDA(cudaEventSynchronize(ctx->ev1));
+  float ms = 0.0f;
+  TSIM_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  launched(ctx, 2);
+  const double flops = 2.0 * kChains * iters * (double)blocks * threads;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return TSIM_OK;
+}
 
 extern "C" {
 
@@ -163,6 +264,13 @@ int tsim_ctx_create(int device, void* stream, tsim_ctx** out) {
   }
   cudaEventCreate(&c->ev0);
   cudaEventCreate(&c->ev1);
+  e = cudaMalloc(&c->dcounters, 64 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(c->dcounters, 0, 64 * sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    if (c->owns_stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return cuda_fail(e, "tsim_ctx_create counters", __FILE__, __LINE__);
+  }
   *out = c;
   return TSIM_OK;
 }
@@ -175,6 +283,9 @@ int tsim_ctx_destroy(tsim_ctx* c) {
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (auto& ev : c->stage_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->dcounters) cudaFree(c->dcounters);
   if (c->owns_stream) cudaStreamDestroy(c->stream);
   delete c;
   return TSIM_OK;

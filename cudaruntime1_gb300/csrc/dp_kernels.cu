@@ -215,8 +215,9 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
 
   const int npairs = a.npairs_dev ? min(*a.npairs_dev, a.npairs) : a.npairs;
   for (int base = gw * SEGS; base < npairs; base += nw * SEGS) {
-    const int pid = base + seg;
-    const bool has = pid < npairs && a.pairs[pid].y >= 0;
+    const int wid = base + seg;
+    const int pid = (wid < npairs && a.order) ? a.order[wid] : wid;
+    const bool has = wid < npairs && a.pairs[pid].y >= 0;
     int n = 0, m = 0, q = 0;
     const float2* A = a.qpts;
     const float2* B = a.cpts;
@@ -242,6 +243,7 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
     bool alive = has;
     V result = P::border();
     bool holds_result = false;
+    long long cells = 0;  // band cells this lane computed for the pair
     // default result (pairs with an empty trajectory compute nothing); the
     // lane that captures the real value writes after this in program order
     if (has && sl == 0) store_result(a, pid, P::border());
@@ -290,6 +292,11 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
         }
       }
       float bmin = TSIM_INF;
+      if (act && a.cells) {
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+          if (jlo[k] != kNoColumn) cells += jhi[k] - jlo[k] + 1;
+      }
 
       for (int s = 0; s < Smax; ++s) {
         const int j = rlo + s - sl;
@@ -338,6 +345,10 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
         prev_hi = h0;
       }
     }
+    if (a.cells) {
+      for (int o = G >> 1; o; o >>= 1) cells += __shfl_xor_sync(0xffffffffu, cells, o, G);
+      if (has && sl == 0) atomicAdd(a.cells, (unsigned long long)cells);
+    }
     if (has && holds_result) store_result(a, pid, alive ? result : P::border());
     if (has && !alive && sl == 0) store_result(a, pid, P::border());
     __syncwarp();
@@ -361,6 +372,7 @@ int launch_one(tsim_ctx* ctx, const DpArgs& a) {
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, kDpThreads, smem, ctx->stream>>>(a);
   TSIM_CUDA(cudaGetLastError());
+  launched(ctx);
   return TSIM_OK;
 }
 

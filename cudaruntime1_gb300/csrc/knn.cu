@@ -61,6 +61,7 @@ struct KArgs {
   int max_qlen;  // shared-memory tables are sized for this query length
   // parameters
   int k, S, T, nch;
+  int plain;  // one DP pair per kernel launch (the unbatched comparison form)
   int cost;  // DTW: 0 squared, 1 Euclidean
   int band_pct;
   int delta;
@@ -80,6 +81,8 @@ struct KArgs {
   int* off2;                // [nq+1]
   int* npairs;              // [1]
   int2* flat;               // [nq*C]
+  int* order;               // [nq*C] shape-sorted schedule of flat
+  int* shape_cnt;           // [kNumShapes]
   float* flat_vals;         // [nq*C]
   unsigned long long* fkeys;  // [nq*(S+C)]
   int RC;
@@ -462,6 +465,58 @@ __global__ void flatten_kernel(KArgs a) {
     a.flat[base + e] = make_int2(q, a.list2[(size_t)q * a.C + e]);
 }
 
+// Shape-sorted schedule of the survivor pairs: counting sort by (query
+// length / 16, candidate length / 16), longest first, so that the pairs
+// sharing a warp have similar shapes (a warp runs as long as its longest
+// pair) and the long pairs do not form the tail of the launch.
+constexpr int kShapeBits = 7;  // 128 length buckets of 16 points per side
+constexpr int kNumShapes = 1 << (2 * kShapeBits);
+
+__device__ __forceinline__ int shape_key(int n, int m) {
+  return (min(n >> 4, (1 << kShapeBits) - 1) << kShapeBits) | min(m >> 4, (1 << kShapeBits) - 1);
+}
+
+__global__ void shape_hist_kernel(KArgs a) {
+  const int np = *a.npairs;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    const int2 pr = a.flat[i];
+    atomicAdd(a.shape_cnt + (kNumShapes - 1 - shape_key(a.qlen[pr.x], a.clen[pr.y])), 1);
+  }
+}
+
+// exclusive scan of the shape histogram in place (one CTA of 1024 threads)
+__global__ void __launch_bounds__(1024) shape_scan_kernel(KArgs a) {
+  __shared__ int part[1024];
+  constexpr int per = kNumShapes / 1024;
+  int loc[per], s = 0;
+  for (int i = 0; i < per; ++i) {
+    loc[i] = a.shape_cnt[threadIdx.x * per + i];
+    s += loc[i];
+  }
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = part[threadIdx.x] - s;
+  for (int i = 0; i < per; ++i) {
+    a.shape_cnt[threadIdx.x * per + i] = run;
+    run += loc[i];
+  }
+}
+
+__global__ void shape_scatter_kernel(KArgs a) {
+  const int np = *a.npairs;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    const int2 pr = a.flat[i];
+    const int pos = atomicAdd(a.shape_cnt + (kNumShapes - 1 - shape_key(a.qlen[pr.x], a.clen[pr.y])), 1);
+    a.order[pos] = i;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // stage E: final selection, FP64 re-score, sort
 // ---------------------------------------------------------------------------
@@ -584,19 +639,22 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stat
   cudaStream_t s = ctx->stream;
   const int nq = a.nq;
   dim3 g1(a.nch, nq);
+  stage_begin(ctx, TSIM_STAGE_LB1);
   clear_u32_kernel<<<std::min<size_t>(((size_t)nq * a.Cw + 255) / 256, 4096), 256, 0, s>>>(
       a.seedmap, (size_t)nq * a.Cw);
   lb1_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
+  stage_end(ctx);
+  launched(ctx, 2);
+  stage_begin(ctx, TSIM_STAGE_SEED);
   const size_t seed_smem = sizeof(unsigned long long) * (size_t)a.nch * a.T;
   if (seed_smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(seed_kernel<MEAS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)seed_smem));
   seed_kernel<MEAS><<<nq, kSelThreads, seed_smem, s>>>(a);
   TSIM_CUDA(cudaGetLastError());
+  launched(ctx);
 
-  // representative launch shape for the DP: longest query against the
-  // average candidate
-  const int avg_m = std::max(1, a.max_clen > 0 ? (int)std::min<long long>(a.max_clen, 1 << 30) : 1);
+  // launch shape of the DP: longest query against the longest candidate
   DpArgs d{};
   d.qpts = a.qpts;
   d.qoff = a.qoff;
@@ -605,15 +663,32 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stat
   d.band_pct = MEAS == M_DTW ? a.band_pct : -1;
   d.delta = a.delta;
   d.eps = a.eps;
+  d.cells = ctx->dcounters;
   int G, R;
-  const int wd = MEAS == M_LCSS ? a.delta : band_w(max_qlen, avg_m, d.band_pct);
-  dp_shape(dp32, max_qlen, avg_m, wd, G, R);
+  const int wd = MEAS == M_LCSS ? a.delta : band_w(max_qlen, a.max_clen, d.band_pct);
+  dp_shape(dp32, max_qlen, a.max_clen, wd, G, R);
 
   d.pairs = a.seeds;
   d.npairs = nq * a.S;
   d.out = a.seed_vals;
-  TSIM_TRY(launch_dp(ctx, dp32, G, R, d, a.max_clen));
+  // few pairs: one pair per warp, one row per lane (the shortest dependency
+  // chain per step; throughput is irrelevant at this size)
+  const int Gs = 32, Rs = 1;
+  if (a.plain) {
+    // the plain form: every pair its own kernel launch from the host
+    for (int i = 0; i < nq * a.S; ++i) {
+      DpArgs one = d;
+      one.pairs = a.seeds + i;
+      one.npairs = 1;
+      one.out = a.seed_vals + i;
+      TSIM_TRY(launch_dp(ctx, dp32, Gs, Rs, one, a.max_clen));
+    }
+  } else {
+    TSIM_TRY(launch_dp(ctx, dp32, Gs, Rs, d, a.max_clen));
+  }
+  stage_end(ctx);
 
+  stage_begin(ctx, TSIM_STAGE_FILTER);
   thresh_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
   compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
   const int ch = std::max(1, std::min(64, (2 * ctx->num_sms * 4 + nq - 1) / nq));
@@ -624,18 +699,47 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stat
   lb2_kernel<MEAS><<<dim3(ch, nq), kLb2Warps * 32, lb2_smem, s>>>(a);
   scan_kernel<<<1, 1024, 0, s>>>(a);
   flatten_kernel<<<dim3(ch, nq), 256, 0, s>>>(a);
+  TSIM_CUDA(cudaMemsetAsync(a.shape_cnt, 0, sizeof(int) * kNumShapes, s));
+  const int sb = ctx->num_sms * 4;
+  shape_hist_kernel<<<sb, 256, 0, s>>>(a);
+  shape_scan_kernel<<<1, 1024, 0, s>>>(a);
+  shape_scatter_kernel<<<sb, 256, 0, s>>>(a);
   TSIM_CUDA(cudaGetLastError());
+  launched(ctx, 8);
+  stage_end(ctx);
 
+  stage_begin(ctx, TSIM_STAGE_DP);
   d.pairs = a.flat;
   d.npairs = nq * a.C;
   d.npairs_dev = a.npairs;
   d.out = a.flat_vals;
   d.thr = a.thr;
-  TSIM_TRY(launch_dp(ctx, dp32, G, R, d, a.max_clen));
+  d.order = a.order;
+  if (a.plain) {
+    int npairs = 0;
+    TSIM_CUDA(cudaMemcpyAsync(&npairs, a.npairs, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TSIM_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < npairs; ++i) {
+      DpArgs one = d;
+      one.pairs = a.flat + i;
+      one.npairs = 1;
+      one.npairs_dev = nullptr;
+      one.order = nullptr;
+      one.out = a.flat_vals + i;
+      TSIM_TRY(launch_dp(ctx, dp32, Gs, Rs, one, a.max_clen));
+    }
+  } else {
+    TSIM_TRY(launch_dp(ctx, dp32, G, R, d, a.max_clen));
+  }
+  stage_end(ctx);
 
+  stage_begin(ctx, TSIM_STAGE_SELECT);
   final_select_kernel<MEAS><<<nq, kSelThreads, 0, s>>>(a);
   TSIM_CUDA(cudaGetLastError());
+  launched(ctx);
+  stage_end(ctx);
   if (MEAS != M_LCSS) {
+    stage_begin(ctx, TSIM_STAGE_RESCORE);
     DpArgs r{};
     r.qpts = a.qpts;
     r.qoff = a.qoff;
@@ -646,17 +750,81 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stat
     r.out64 = a.r64;
     r.band_pct = d.band_pct;
     r.delta = -1;
-    int G64, R64;
-    dp_shape(dp64, max_qlen, avg_m, wd, G64, R64);
-    TSIM_TRY(launch_dp(ctx, dp64, G64, R64, r, a.max_clen));
+    TSIM_TRY(launch_dp(ctx, dp64, 32, 1, r, a.max_clen));
     final_sort_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
     TSIM_CUDA(cudaGetLastError());
+    launched(ctx);
+    stage_end(ctx);
   }
-  (void)st;
+  if (st) {
+    // counts for the caller (synchronises)
+    int npairs = 0;
+    TSIM_CUDA(cudaMemcpyAsync(&npairs, a.npairs, sizeof(int), cudaMemcpyDeviceToHost, s));
+    std::vector<int> rc(nq);
+    TSIM_CUDA(cudaMemcpyAsync(rc.data(), a.rcnt, sizeof(int) * nq, cudaMemcpyDeviceToHost, s));
+    TSIM_CUDA(cudaStreamSynchronize(s));
+    st->pairs_refined = (int64_t)npairs + (int64_t)nq * a.S;
+    int64_t r = 0;
+    for (int v : rc) r += v;
+    st->rescored = MEAS == M_LCSS ? 0 : r;
+  }
   return TSIM_OK;
 }
 
+// Band cells of every (query, candidate) pair: sum over rows of the row's
+// band width (DTW), window width (LCSS) or m (Frechet).
+__global__ void band_cells_kernel(KArgs a, int meas, unsigned long long* out) {
+  const int q = blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  long long cells = 0;
+  if (c < a.C) {
+    const int n = a.qlen[q], m = a.clen[c];
+    if (meas == M_FRECHET || (meas == M_DTW && a.band_pct < 0) || (meas == M_LCSS && a.delta < 0)) {
+      cells = (long long)n * m;
+    } else if (meas == M_LCSS) {
+      for (int i = 0; i < n; ++i) {
+        int lo = max(0, i - a.delta), hi = min(m - 1, i + a.delta);
+        if (hi >= lo) cells += hi - lo + 1;
+      }
+    } else {
+      const int w = band_w(n, m, a.band_pct);
+      for (int i = 0; i < n; ++i) {
+        int lo, hi;
+        band_row(i, n, m, w, lo, hi);
+        if (hi >= lo) cells += hi - lo + 1;
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) cells += __shfl_xor_sync(0xffffffffu, cells, o);
+  if ((threadIdx.x & 31) == 0 && cells) atomicAdd(out, (unsigned long long)cells);
+}
+
 }  // namespace
+
+int band_cells(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
+               tsim_db* db, int64_t* cells_out) {
+  KArgs a{};
+  a.nq = nq;
+  a.C = db->count;
+  a.clen = db->len;
+  a.band_pct = p->band_pct;
+  a.delta = p->delta;
+  float4* qbox = arena_take<float4>(ctx, nq);
+  float4* qends = arena_take<float4>(ctx, nq);
+  int* qlen = arena_take<int>(ctx, nq);
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(ctx->dcounters) + 16;
+  TSIM_TRY(summarize(ctx, qpts, qoff, nq, qbox, qends, qlen));
+  a.qlen = qlen;
+  TSIM_CUDA(cudaMemsetAsync(acc, 0, sizeof(unsigned long long), ctx->stream));
+  const int meas = p->measure == TSIM_DTW ? M_DTW : (p->measure == TSIM_LCSS ? M_LCSS : M_FRECHET);
+  band_cells_kernel<<<dim3((a.C + 255) / 256, nq), 256, 0, ctx->stream>>>(a, meas, acc);
+  TSIM_CUDA(cudaGetLastError());
+  unsigned long long h = 0;
+  TSIM_CUDA(cudaMemcpyAsync(&h, acc, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+  *cells_out = (int64_t)h;
+  return TSIM_OK;
+}
 
 int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
         int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st) {
@@ -680,6 +848,7 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.nch = (C + kChunk - 1) / kChunk;
   a.T = std::min(kChunk, std::max(1, (2 * a.S + a.nch - 1) / a.nch));
   a.T = std::min(a.T, 64);
+  a.plain = (p->flags & TSIM_FLAG_PLAIN) ? 1 : 0;
   a.cost = p->cost;
   a.band_pct = p->band_pct;
   a.delta = p->delta;
@@ -701,7 +870,8 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
                 align256(sizeof(int) * 4) + align256(sizeof(int2) * nqC) +
                 align256(sizeof(float) * nqC) +
                 align256(sizeof(unsigned long long) * nq * (size_t)(a.S + C)) +
-                align256(sizeof(int2) * nq * a.RC) + align256(sizeof(double) * nq * a.RC);
+                align256(sizeof(int2) * nq * a.RC) + align256(sizeof(double) * nq * a.RC) +
+                align256(sizeof(int) * nqC) + align256(sizeof(int) * kNumShapes);
   TSIM_TRY(arena_reserve(ctx, need));
   float4* qbox = arena_take<float4>(ctx, nq);
   float4* qends = arena_take<float4>(ctx, nq);
@@ -727,9 +897,13 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.fkeys = arena_take<unsigned long long>(ctx, (size_t)nq * (a.S + C));
   a.rpairs = arena_take<int2>(ctx, (size_t)nq * a.RC);
   a.r64 = arena_take<double>(ctx, (size_t)nq * a.RC);
-  if (!a.r64) return fail(TSIM_ERR_OUT_OF_MEMORY, "knn scratch carve failed");
+  a.order = arena_take<int>(ctx, nqC);
+  a.shape_cnt = arena_take<int>(ctx, kNumShapes);
+  if (!a.shape_cnt) return fail(TSIM_ERR_OUT_OF_MEMORY, "knn scratch carve failed");
 
+  stage_begin(ctx, TSIM_STAGE_SUMMARY);
   TSIM_TRY(summarize(ctx, qpts, qoff, nq, qbox, qends, qlen));
+  stage_end(ctx);
   switch (p->measure) {
     case TSIM_DTW:
       return run_knn<M_DTW>(ctx, a, max_qlen, p->cost ? DP_DTW_EU : DP_DTW_SQ,
@@ -822,4 +996,15 @@ extern "C" int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
   memcpy(h_ids, hp + in_bytes, sizeof(int) * nq * p->k);
   memcpy(h_dists, hp + in_bytes + tsim::align256(sizeof(int) * nq * p->k), sizeof(float) * nq * p->k);
   return TSIM_OK;
+}
+
+extern "C" int tsim_band_cells(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
+                               const int64_t* d_qoff, int nq, tsim_db* db, int64_t* cells) {
+  TSIM_CHECK_ARG(ctx && p && db && d_qpts && d_qoff && cells && nq >= 1, "bad arguments");
+  TSIM_CHECK_ARG(p->measure == TSIM_DTW || p->measure == TSIM_LCSS || p->measure == TSIM_FRECHET,
+                 "band cells are defined for the DP measures");
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  TSIM_TRY(tsim::arena_reserve(ctx, tsim::align256(sizeof(float4) * nq) * 2 +
+                                        tsim::align256(sizeof(int) * nq) + 256));
+  return tsim::band_cells(ctx, p, (const float2*)d_qpts, d_qoff, nq, db, cells);
 }

@@ -57,6 +57,16 @@ struct tsim_ctx {
   void* pinned = nullptr;
   size_t pinned_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // instrumentation: kernels launched, and per-stage CUDA-event timing on
+  // the context stream when profiling is on
+  int64_t launches = 0;
+  bool profiling = false;
+  cudaEvent_t stage_ev[2 * 64] = {};
+  int stage_id[64] = {};
+  int nstage_ev = 0;
+  double stage_ms[TSIM_STAGE_COUNT] = {};
+  int64_t stage_calls[TSIM_STAGE_COUNT] = {};
+  unsigned long long* dcounters = nullptr;  // device: [0] DP cells computed
 };
 
 struct tsim_db {
@@ -89,6 +99,12 @@ T* arena_take(tsim_ctx* ctx, size_t count) {
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 int pinned_reserve(tsim_ctx* ctx, size_t bytes);
+
+// stage timing: bracket one stage's launches; no-ops unless profiling is on
+void stage_begin(tsim_ctx* ctx, int stage);
+void stage_end(tsim_ctx* ctx);
+int stage_collect(tsim_ctx* ctx);  // synchronises and accumulates pending stages
+inline void launched(tsim_ctx* ctx, int n = 1) { ctx->launches += n; }
 
 // ---------------------------------------------------------------------------
 // band geometry (host + device), identical to oracle/oracle.c orc_band_*
@@ -172,6 +188,8 @@ struct DpArgs {
   int delta;          // LCSS window, <0 none
   float eps;          // LCSS threshold
   int buf_len;        // shared-memory values per segment (>= max candidate length)
+  unsigned long long* cells;  // optional: band cells actually computed (atomic)
+  const int* order;   // optional: work item w is pair order[w] (shape-sorted schedule)
 };
 
 enum DpKind {
@@ -189,6 +207,8 @@ enum DpKind {
 
 int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
         int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st);
+int band_cells(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
+               tsim_db* db, int64_t* cells_out);
 int knn_pairwise(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff,
                  int nq, int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64,
                  tsim_stats* st);

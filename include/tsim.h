@@ -91,6 +91,19 @@ typedef struct tsim_stats {
   int32_t graph_replay;   /* 1 when the call replayed a captured graph */
 } tsim_stats;
 
+/* stages timed when profiling is on (tsim_ctx_set_profiling) */
+typedef enum tsim_stage {
+  TSIM_STAGE_SUMMARY = 0, /* query summaries */
+  TSIM_STAGE_LB1,         /* O(1) bounds of all pairs */
+  TSIM_STAGE_SEED,        /* seed selection + seed refinement */
+  TSIM_STAGE_FILTER,      /* threshold, compaction, O(length) bounds, scan */
+  TSIM_STAGE_DP,          /* exact FP32 DP / distance of the survivors */
+  TSIM_STAGE_SELECT,      /* k-th value and re-score set */
+  TSIM_STAGE_RESCORE,     /* FP64 re-score and final sort */
+  TSIM_STAGE_REF,         /* reference-semantics batch calls */
+  TSIM_STAGE_COUNT
+} tsim_stage;
+
 typedef struct tsim_ctx tsim_ctx; /* device, stream, scratch, tuning cache */
 typedef struct tsim_db tsim_db;   /* device-resident candidate set + summaries */
 
@@ -106,6 +119,16 @@ TSIM_API int tsim_ctx_set_stream(tsim_ctx* ctx, void* stream);
 TSIM_API int tsim_ctx_synchronize(tsim_ctx* ctx);
 /* bytes of device scratch the context currently holds */
 TSIM_API int64_t tsim_ctx_scratch_bytes(const tsim_ctx* ctx);
+/* Per-stage CUDA-event timing on the context stream (off by default). */
+TSIM_API int tsim_ctx_set_profiling(tsim_ctx* ctx, int on);
+/* Accumulated stage times (ms[TSIM_STAGE_COUNT], calls[TSIM_STAGE_COUNT]) and
+ * the number of kernels this context launched; synchronises the stream.
+ * reset != 0 clears the counters after reading. */
+TSIM_API int tsim_ctx_counters(tsim_ctx* ctx, double* ms, int64_t* calls, int64_t* launches,
+                               int64_t* dp_cells, int reset);
+/* Measured FP32 FMA throughput of this GPU in TFLOP/s (a short probe kernel,
+ * for roofline denominators). */
+TSIM_API int tsim_probe_fp32_tflops(tsim_ctx* ctx, double* tflops);
 
 /* ---- device-resident candidate database ---------------------------------- */
 /* Copies host points/offsets to the device and builds per-trajectory
@@ -120,6 +143,10 @@ TSIM_API int tsim_db_count(const tsim_db* db);
 TSIM_API int64_t tsim_db_device_bytes(const tsim_db* db);
 
 /* ---- exact kNN ------------------------------------------------------------ */
+/* Cells inside the DP band (DTW, LCSS window, Frechet: n*m) summed over all
+ * query x database pairs: the unpruned work, for "effective" cell rates. */
+TSIM_API int tsim_band_cells(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
+                             const int64_t* d_qoff, int nq, tsim_db* db, int64_t* cells);
 /* Device pointers; results d_ids[nq*k], d_dists[nq*k] (float, from the FP64
  * re-score), d_dists64 optional (may be NULL).  LCSS distances are the
  * integer match counts.  Asynchronous on the context stream unless stats is
