@@ -23,6 +23,7 @@ namespace {
 
 constexpr int kFilterThreads = 256;
 constexpr float kRefBig = 1e20f;  // the reference's infinity (dtw.cpp:23)
+constexpr size_t kRefSmemCap = 200 * 1024;
 
 __device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
@@ -123,33 +124,48 @@ __global__ void fixed_offsets_kernel(int64_t* off, int count, int len) {
 
 }  // namespace
 
-int ref_batch(tsim_ctx* ctx, int measure, const float2* d_t1, const float2* d_t2, int num_t, int n,
-              int m, float eps, float* d_out) {
+// Scratch of one reference-semantics batch call, carved from one block.
+size_t ref_scratch_bytes(int num_t, int m, bool* keys_in_smem) {
+  const int K = std::min(10, num_t);
+  const size_t env_bytes = (size_t)m * sizeof(float4);
+  const size_t key_bytes = (size_t)num_t * sizeof(unsigned long long);
+  const bool in_smem = env_bytes + key_bytes <= kRefSmemCap;
+  if (keys_in_smem) *keys_in_smem = in_smem;
+  return align256(sizeof(int2) * num_t * K) + align256(sizeof(float) * num_t * K) +
+         2 * align256(sizeof(int64_t) * (num_t + 1)) + (in_smem ? 0 : align256(key_bytes * num_t));
+}
+
+int ref_batch_core(tsim_ctx* ctx, int measure, const float2* d_t1, const float2* d_t2, int num_t,
+                   int n, int m, float eps, float* d_out, char* scratch) {
   const int K = std::min(10, num_t);
   // shared memory: m envelopes + keys when they fit, else keys in scratch
-  size_t env_bytes = (size_t)m * sizeof(float4);
-  size_t key_bytes = (size_t)num_t * sizeof(unsigned long long);
-  const size_t smem_cap = 200 * 1024;
-  bool keys_in_smem = env_bytes + key_bytes <= smem_cap;
-  TSIM_CHECK_ARG(env_bytes <= smem_cap, "candidate length too large for the envelope filter");
-  size_t need = align256(sizeof(int2) * num_t * K) + align256(sizeof(float) * num_t * K) +
-                2 * align256(sizeof(int64_t) * (num_t + 1)) +
-                (keys_in_smem ? 0 : align256(key_bytes * num_t));
-  TSIM_TRY(arena_reserve(ctx, need));
-  int2* pairs = arena_take<int2>(ctx, (size_t)num_t * K);
-  float* vals = arena_take<float>(ctx, (size_t)num_t * K);
-  int64_t* qoff = arena_take<int64_t>(ctx, num_t + 1);
-  int64_t* coff = arena_take<int64_t>(ctx, num_t + 1);
+  const size_t env_bytes = (size_t)m * sizeof(float4);
+  const size_t key_bytes = (size_t)num_t * sizeof(unsigned long long);
+  TSIM_CHECK_ARG(env_bytes <= kRefSmemCap, "candidate length too large for the envelope filter");
+  bool keys_in_smem = false;
+  ref_scratch_bytes(num_t, m, &keys_in_smem);
+  char* p = scratch;
+  auto take = [&p](size_t bytes) {
+    char* q = p;
+    p += align256(bytes);
+    return q;
+  };
+  int2* pairs = reinterpret_cast<int2*>(take(sizeof(int2) * num_t * K));
+  float* vals = reinterpret_cast<float*>(take(sizeof(float) * num_t * K));
+  int64_t* qoff = reinterpret_cast<int64_t*>(take(sizeof(int64_t) * (num_t + 1)));
+  int64_t* coff = reinterpret_cast<int64_t*>(take(sizeof(int64_t) * (num_t + 1)));
   unsigned long long* gkeys =
-      keys_in_smem ? nullptr : arena_take<unsigned long long>(ctx, (size_t)num_t * num_t);
+      keys_in_smem ? nullptr : reinterpret_cast<unsigned long long*>(take(key_bytes * num_t));
 
-  size_t smem = env_bytes + (keys_in_smem ? key_bytes : 0);
+  stage_begin(ctx, TSIM_STAGE_REF);
+  const size_t smem = env_bytes + (keys_in_smem ? key_bytes : 0);
   auto launch_filter = [&](auto kern) -> int {
     if (smem > 48 * 1024)
       TSIM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<num_t, kFilterThreads, smem, ctx->stream>>>(d_t1, d_t2, num_t, n, m, eps, K, gkeys,
                                                         pairs);
     TSIM_CUDA(cudaGetLastError());
+    launched(ctx);
     return TSIM_OK;
   };
   int kind;
@@ -166,6 +182,7 @@ int ref_batch(tsim_ctx* ctx, int measure, const float2* d_t1, const float2* d_t2
   fixed_offsets_kernel<<<(num_t + 256) / 256, 256, 0, ctx->stream>>>(qoff, num_t, n);
   fixed_offsets_kernel<<<(num_t + 256) / 256, 256, 0, ctx->stream>>>(coff, num_t, m);
   TSIM_CUDA(cudaGetLastError());
+  launched(ctx, 2);
 
   DpArgs a{};
   a.qpts = d_t1;
@@ -189,7 +206,16 @@ int ref_batch(tsim_ctx* ctx, int measure, const float2* d_t1, const float2* d_t2
   else
     ref_reduce_kernel<0><<<(num_t + tb - 1) / tb, tb, 0, ctx->stream>>>(vals, num_t, K, n, m, d_out);
   TSIM_CUDA(cudaGetLastError());
+  launched(ctx);
+  stage_end(ctx);
   return TSIM_OK;
+}
+
+int ref_batch(tsim_ctx* ctx, int measure, const float2* d_t1, const float2* d_t2, int num_t, int n,
+              int m, float eps, float* d_out) {
+  TSIM_TRY(arena_reserve(ctx, ref_scratch_bytes(num_t, m, nullptr)));
+  char* scratch = arena_take<char>(ctx, ref_scratch_bytes(num_t, m, nullptr));
+  return ref_batch_core(ctx, measure, d_t1, d_t2, num_t, n, m, eps, d_out, scratch);
 }
 
 }  // namespace tsim

@@ -207,6 +207,11 @@ enum DpKind {
 
 int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
         int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st);
+// reference-semantics batch: scratch size and the call on caller-given scratch
+size_t ref_scratch_bytes(int num_t, int m, bool* keys_in_smem);
+int ref_batch_core(tsim_ctx* ctx, int measure, const float2* d_t1, const float2* d_t2, int num_t,
+                   int n, int m, float eps, float* d_out, char* scratch);
+
 int band_cells(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
                tsim_db* db, int64_t* cells_out);
 int knn_pairwise(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff,

@@ -169,6 +169,28 @@ TSIM_API int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_point
 TSIM_API int tsim_ref_batch(tsim_ctx* ctx, int measure, const tsim_point* d_t1,
                             const tsim_point* d_t2, int num_t, int n, int m, float epsilon,
                             float* d_out);
+/* Bytes of device memory that the scratch array of tsim_ref_batch_static
+ * occupies on every GPU that loads libtsim.so, until the process exits. */
+#define TSIM_STATIC_SCRATCH_BYTES (4u << 20)
+/* No counterpart in the reference.  tsim_ref_batch for callers that may not
+ * allocate device memory -- e.g. a plugin inside a host application that owns
+ * the whole GPU memory pool, or a latency-critical loop that cannot take the
+ * implicit synchronisation of cudaMalloc/cudaFree.  Same inputs, outputs and
+ * results as tsim_ref_batch, on the caller's stream (NULL = legacy default
+ * stream), with no context and no cudaMalloc/cudaFree: scratch comes from a
+ * fixed array of TSIM_STATIC_SCRATCH_BYTES in the library's device memory.
+ * Limit: the call needs about 12*10*num_t + 16*(num_t+1) bytes of scratch and
+ * its candidate keys (8*num_t bytes) plus envelopes (16*m bytes) must fit in
+ * 200 KiB of shared memory; larger calls return TSIM_ERR_UNSUPPORTED.
+ * The first call on each device looks up the array's device address with that
+ * device current (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race, so the caller serialises them (one stream, or its own lock).  The
+ * array keeps the last call's contents; nothing in it needs clearing, as
+ * every entry read is written earlier in the same call. */
+TSIM_API int tsim_ref_batch_static(int measure, const tsim_point* d_t1, const tsim_point* d_t2,
+                                   int num_t, int n, int m, float epsilon, float* d_out,
+                                   void* stream);
 /* Min over the given candidates of the symmetric Hausdorff distance
  * (CudaRuntime1/hausdorff.cu:84-122). d_cand[num_t1*top_k]. */
 TSIM_API int tsim_hausdorff_cands(tsim_ctx* ctx, const tsim_point* d_t1, int num_t1, int n,
