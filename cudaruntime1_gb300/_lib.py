@@ -20,7 +20,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device mem
 
 DTW, LCSS, FRECHET, HAUSDORFF, EUCLIDEAN = range(5)
 COST_SQEUCLID, COST_EUCLID = 0, 1
-FLAG_NO_PRUNE, FLAG_PLAIN, FLAG_NO_GRAPH = 1, 2, 4
+FLAG_NO_PRUNE, FLAG_PLAIN, FLAG_NO_GRAPH, FLAG_FP64_RESCORE = 1, 2, 4, 8
 STAGES = ["summary", "lb1", "seed", "filter", "dp", "select", "rescore", "ref"]
 
 _vp = C.c_void_p
@@ -36,6 +36,7 @@ class TsimParams(C.Structure):
 class TsimStats(C.Structure):
     _fields_ = [("ms", C.c_double), ("pairs", C.c_int64), ("pairs_refined", C.c_int64),
                 ("cells", C.c_int64), ("cells_unpruned", C.c_int64), ("rescored", C.c_int64),
+                ("rescored_fp64", C.c_int64),
                 ("launches", C.c_int32), ("graph_replay", C.c_int32)]
 
     def as_dict(self):

@@ -16,8 +16,9 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import (COST_EUCLID, COST_SQEUCLID, DTW, EUCLIDEAN, FLAG_NO_GRAPH, FLAG_NO_PRUNE,
-                   FLAG_PLAIN, FRECHET, HAUSDORFF, LCSS, TsimParams, TsimStats, check)
+from ._lib import (COST_EUCLID, COST_SQEUCLID, DTW, EUCLIDEAN, FLAG_FP64_RESCORE,  # noqa: F401
+                   FLAG_NO_GRAPH, FLAG_NO_PRUNE, FLAG_PLAIN, FRECHET, HAUSDORFF, LCSS, TsimParams,
+                   TsimStats, check)
 
 MEASURES = {"dtw": DTW, "lcss": LCSS, "frechet": FRECHET, "hausdorff": HAUSDORFF,
             "euclidean": EUCLIDEAN}

@@ -2,6 +2,7 @@
 // reporting of the C ABI (include/tsim.h).
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 
 #include "tsim_internal.cuh"
@@ -275,10 +276,17 @@ int tsim_ctx_create(int device, void* stream, tsim_ctx** out) {
   return TSIM_OK;
 }
 
+static void db_free(tsim_db* db);
+
 int tsim_ctx_destroy(tsim_ctx* c) {
   if (!c) return TSIM_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  for (tsim_db* db : c->dbs) {  // detach: free device memory, keep the handle
+    db_free(db);
+    db->ctx = nullptr;
+  }
+  c->dbs.clear();
   if (c->arena) cudaFree(c->arena);
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -328,6 +336,10 @@ static void db_free(tsim_db* db) {
   cudaFree(db->box);
   cudaFree(db->ends);
   cudaFree(db->len);
+  db->pts = nullptr;
+  db->off = nullptr;
+  db->box = db->ends = nullptr;
+  db->len = nullptr;
 }
 
 int tsim_db_create(tsim_ctx* ctx, const tsim_point* h_pts, const int64_t* h_off, int count,
@@ -369,6 +381,7 @@ int tsim_db_create(tsim_ctx* ctx, const tsim_point* h_pts, const int64_t* h_off,
     delete db;
     return s;
   }
+  ctx->dbs.push_back(db);
   *out = db;
   return TSIM_OK;
 }
@@ -413,15 +426,20 @@ int tsim_db_wrap_device(tsim_ctx* ctx, const tsim_point* d_pts, const int64_t* d
     delete db;
     return s;
   }
+  ctx->dbs.push_back(db);
   *out = db;
   return TSIM_OK;
 }
 
 int tsim_db_destroy(tsim_db* db) {
   if (!db) return TSIM_OK;
-  cudaSetDevice(db->ctx->device);
-  cudaStreamSynchronize(db->ctx->stream);
-  db_free(db);
+  if (db->ctx) {  // still attached: release its memory and unregister it
+    cudaSetDevice(db->ctx->device);
+    cudaStreamSynchronize(db->ctx->stream);
+    db_free(db);
+    auto& v = db->ctx->dbs;
+    v.erase(std::remove(v.begin(), v.end(), db), v.end());
+  }
   delete db;
   return TSIM_OK;
 }

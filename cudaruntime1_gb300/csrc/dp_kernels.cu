@@ -19,6 +19,7 @@
 // lcss_refine_kernel_m_1 (lcss.cu:46-111), frechet_refine_kernel_m
 // (frechet.cu:44-117): one CTA per pair, one barrier per anti-diagonal, every
 // point re-read from global memory per cell.
+#include "dfloat.cuh"
 #include "tsim_internal.cuh"
 
 namespace tsim {
@@ -136,6 +137,44 @@ struct PolFrechetSq64 {
   }
 };
 
+// Compensated FP32 re-score policies: values are (hi, lo) pairs (dfloat.cuh).
+struct PolDtwSqC {
+  using V = df;
+  static constexpr bool kMin = true;
+  __device__ static V border() { return df_inf(); }
+  __device__ static V origin() { return df{0.0f, 0.0f}; }
+  __device__ static V masked(V) { return df_inf(); }
+  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
+    const df m = df_min(df_min(up, lf), dg);
+    if (!(m.hi < TSIM_INF)) return df_inf();
+    return df_add(df_sqdist(qx, qy, cx, cy), m);
+  }
+};
+
+struct PolDtwEuC {
+  using V = df;
+  static constexpr bool kMin = true;
+  __device__ static V border() { return df_inf(); }
+  __device__ static V origin() { return df{0.0f, 0.0f}; }
+  __device__ static V masked(V) { return df_inf(); }
+  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
+    const df m = df_min(df_min(up, lf), dg);
+    if (!(m.hi < TSIM_INF)) return df_inf();
+    return df_add(df_sqrt(df_sqdist(qx, qy, cx, cy)), m);
+  }
+};
+
+struct PolFrechetSqC {
+  using V = df;
+  static constexpr bool kMin = true;
+  __device__ static V border() { return df_inf(); }
+  __device__ static V origin() { return df{0.0f, 0.0f}; }
+  __device__ static V masked(V) { return df_inf(); }
+  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
+    return df_max(df_sqdist(qx, qy, cx, cy), df_min(df_min(up, lf), dg));
+  }
+};
+
 // LCSS: match iff |q.x-c.x| < eps and |q.y-c.y| < eps in FP32 (lcss.cpp:93-96).
 // Outside the index window a cell keeps its row's last in-window value (the
 // true LCSS value there); left of the window it stays 0.  The non-match case
@@ -181,10 +220,20 @@ __device__ void RowBand<PolLcss>::get(int i, int, int m, int, int delta, int& lo
 __device__ __forceinline__ void store_result(const DpArgs& a, int pid, float v) { a.out[pid] = v; }
 __device__ __forceinline__ void store_result(const DpArgs& a, int pid, int v) { a.out[pid] = (float)v; }
 __device__ __forceinline__ void store_result(const DpArgs& a, int pid, double v) { a.out64[pid] = v; }
+__device__ __forceinline__ void store_result(const DpArgs& a, int pid, df v) {
+  a.out64[pid] = v.hi < TSIM_INF ? df_to_double(v) : __longlong_as_double(0x7ff0000000000000ll);
+}
+__device__ __forceinline__ float vf(float v) { return v; }
+__device__ __forceinline__ float vf(int v) { return (float)v; }
+__device__ __forceinline__ float vf(double v) { return (float)v; }
+__device__ __forceinline__ float vf(df v) { return v.hi; }
 
 template <class V>
 __device__ __forceinline__ V shfl_up_seg(V v, int G) {
   return __shfl_up_sync(0xffffffffu, v, 1, G);
+}
+__device__ __forceinline__ df shfl_up_seg(df v, int G) {
+  return df{__shfl_up_sync(0xffffffffu, v.hi, 1, G), __shfl_up_sync(0xffffffffu, v.lo, 1, G)};
 }
 
 __device__ __forceinline__ float seg_max(float v, int G) {
@@ -319,7 +368,7 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
           }
           outv = u;
           if (sl == G - 1) buf[j] = outv;
-          if (P::kMin) bmin = fminf(bmin, (float)outv);
+          if (P::kMin) bmin = fminf(bmin, vf(outv));
         }
       }
       __syncwarp();
@@ -408,7 +457,7 @@ int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a_in, int max
   DpArgs a = a_in;
   a.buf_len = (max_m + 4) & ~3;
   // fewer segments per warp when the row buffers would not fit in shared memory
-  const size_t vbytes = (kind >= DP_DTW_SQ64) ? 8 : 4;
+  const size_t vbytes = (kind >= DP_DTW_SQ64) ? 8 : 4;  // FP64 and (hi, lo) kinds
   while (G < 32 && (size_t)(kDpThreads / 32) * (32 / G) * a.buf_len * vbytes > 200 * 1024) G *= 2;
   if ((size_t)(kDpThreads / 32) * (32 / G) * a.buf_len * vbytes > 200 * 1024)
     return fail(TSIM_ERR_UNSUPPORTED, "candidate trajectory too long for the shared-memory row buffer");
@@ -422,6 +471,9 @@ int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a_in, int max
     case DP_DTW_SQ64: return launch_g64<PolDtwSq64>(ctx, G, R, a);
     case DP_DTW_EU64: return launch_g64<PolDtwEu64>(ctx, G, R, a);
     case DP_FRECHET_SQ64: return launch_g64<PolFrechetSq64>(ctx, G, R, a);
+    case DP_DTW_SQC: return launch_g64<PolDtwSqC>(ctx, G, R, a);
+    case DP_DTW_EUC: return launch_g64<PolDtwEuC>(ctx, G, R, a);
+    case DP_FRECHET_SQC: return launch_g64<PolFrechetSqC>(ctx, G, R, a);
   }
   return fail(TSIM_ERR_INVALID_ARG, "unknown dp kind");
 }

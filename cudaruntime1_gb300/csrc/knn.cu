@@ -16,9 +16,12 @@
 //   D  DP              the survivors run the wavefront DP with early
 //                      abandon against the threshold;
 //   E  final           the k-th best FP32 value fixes the re-score set (all
-//                      pairs within the error bound of it), which is
-//                      re-computed in FP64 with the oracle's arithmetic and
-//                      sorted by (distance, candidate index).
+//                      pairs within the FP32 error bound of it); the set is
+//                      re-computed with compensated (hi, lo) FP32 arithmetic,
+//                      pairs whose compensated values are within that
+//                      tighter bound of a neighbour are re-computed in FP64
+//                      with the oracle's arithmetic, and the set is sorted by
+//                      (distance, candidate index).
 // LCSS counts are exact integers in FP32, so LCSS skips the re-score.
 //
 // The reference's GPU path (CudaRuntime1/dtw.cu:99-234) instead ranks every
@@ -77,7 +80,13 @@ struct KArgs {
   int* cnt1;                // [nq]
   int* list1;               // [nq*C]
   int* cnt2;                // [nq]
-  int* list2;               // [nq*C]
+  int* list2;               // [nq*C]  survivors of the O(length) bound
+  float* lb2v;              // [nq*C]  their bound values
+  int M;                    // round-1 pairs per query (best by O(length) bound)
+  int2* r1pairs;            // [nq*M]
+  float* r1vals;            // [nq*M]
+  float* thr2;              // [nq]  threshold after round 1
+  int* fcnt;                // [nq]  round-2 pairs per query (in list1)
   int* off2;                // [nq+1]
   int* npairs;              // [1]
   int2* flat;               // [nq*C]
@@ -86,9 +95,13 @@ struct KArgs {
   float* flat_vals;         // [nq*C]
   unsigned long long* fkeys;  // [nq*(S+C)]
   int RC;
-  int2* rpairs;             // [nq*RC]
-  double* r64;              // [nq*RC]
+  int2* rpairs;             // [nq*RC] re-score set
+  double* rdc;              // [nq*RC] compensated FP32 (hi+lo) values
+  int2* r64pairs;           // [nq*RC] members of ambiguous clusters (else y = -1)
+  double* r64;              // [nq*RC] FP64 values of those
   int* rcnt;                // [nq]
+  int* n64;                 // [1] pairs sent to FP64
+  int force64;              // re-score every pair in FP64 (bit-identical distances)
   // outputs
   int* ids;
   float* dists;
@@ -331,6 +344,7 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
     const float2* B = a.cpts + a.coff[c];
     const int m = a.clen[c];
     bool pass;
+    float lbv = MEAS == M_LCSS ? (float)min(n, m) : 0.0f;  // the bound (no bound: trivial)
     if (n <= 0 || m <= 0) {
       pass = false;
     } else if (MEAS != M_FRECHET && !use_table) {
@@ -390,6 +404,7 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
       for (int o = 16; o; o >>= 1) acc = __fadd_rd(acc, __shfl_xor_sync(0xffffffffu, acc, o));
       feasible = __all_sync(0xffffffffu, feasible);
       pass = feasible && acc <= t;
+      lbv = feasible ? acc : TSIM_INF;
     } else if (MEAS == M_FRECHET) {
       // every point of either trajectory is coupled to some point of the
       // other, so F^2 >= its squared distance to the other's box
@@ -405,6 +420,7 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
       }
       for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
       pass = mx <= t;
+      lbv = mx;
     } else {
       // LCSS: candidate points that can match some query point of their
       // window (rows [j-delta, j+delta]) inside the eps-inflated box
@@ -423,22 +439,100 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
           ++count;
       }
       for (int o = 16; o; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
-      pass = (float)min(count, min(n, m)) >= t;
+      lbv = (float)min(count, min(n, m));
+      pass = lbv >= t;
     }
     if (pass && lane == 0) {
       int pos = atomicAdd(a.cnt2 + q, 1);
       a.list2[(size_t)q * a.C + pos] = c;
+      a.lb2v[(size_t)q * a.C + pos] = lbv;
     }
   }
 }
 
-// exclusive scan of cnt2 -> off2, total -> npairs (one CTA)
+// Round 1: the M best survivors of each query by their O(length) bound
+// (most likely to hold the true neighbours) are refined first; their values
+// tighten the threshold for the rest.  Taken entries are consumed (-1).
+template <int MEAS>
+__global__ void __launch_bounds__(kSelThreads) r1_select_kernel(KArgs a) {
+  __shared__ unsigned long long red[33];
+  __shared__ unsigned long long sel[64];
+  const int q = blockIdx.x;
+  const int N = a.cnt2[q];
+  unsigned long long* keys = a.fkeys + (size_t)q * (a.S + a.C);
+  for (int i = threadIdx.x; i < N; i += kSelThreads) {
+    const float b = a.lb2v[(size_t)q * a.C + i];
+    keys[i] = pack_key(MEAS == M_LCSS ? -b : b, i);
+  }
+  __syncthreads();
+  block_select_k(keys, N, a.M, sel, red);
+  for (int i = threadIdx.x; i < a.M; i += kSelThreads) {
+    const int pos = key_index(sel[i]);
+    int c = -1;
+    if (pos >= 0) {
+      c = a.list2[(size_t)q * a.C + pos];
+      a.list2[(size_t)q * a.C + pos] = -1;
+    }
+    a.r1pairs[(size_t)q * a.M + i] = make_int2(q, c);
+  }
+}
+
+// k-th best of seeds and round 1 -> tightened threshold (never looser)
+template <int MEAS>
+__global__ void thresh2_kernel(KArgs a) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= a.nq) return;
+  float v[128];
+  int cnt = 0;
+  auto add = [&](float x) {
+    if (MEAS == M_LCSS) x = -x;
+    int p = cnt++;
+    while (p > 0 && v[p - 1] > x) {
+      v[p] = v[p - 1];
+      --p;
+    }
+    v[p] = x;
+  };
+  for (int i = 0; i < a.S; ++i)
+    if (a.seeds[(size_t)q * a.S + i].y >= 0) add(a.seed_vals[(size_t)q * a.S + i]);
+  for (int i = 0; i < a.M; ++i)
+    if (a.r1pairs[(size_t)q * a.M + i].y >= 0) add(a.r1vals[(size_t)q * a.M + i]);
+  float t = a.thr[q];
+  if (cnt >= a.k) {
+    if (MEAS == M_LCSS)
+      t = fmaxf(t, -v[a.k - 1]);
+    else
+      t = fminf(t, widen(v[a.k - 1], gamma_dp(MEAS, a.qlen[q], a.max_clen)));
+  }
+  a.thr2[q] = t;
+  a.fcnt[q] = 0;
+}
+
+// Round 2: the remaining survivors whose bound passes the tightened
+// threshold, into list1 (free after stage C).
+template <int MEAS>
+__global__ void refilter_kernel(KArgs a) {
+  const int q = blockIdx.y;
+  const int N = a.cnt2[q];
+  const float t = a.thr2[q];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+    const int c = a.list2[(size_t)q * a.C + e];
+    if (c < 0) continue;
+    const float b = a.lb2v[(size_t)q * a.C + e];
+    if (MEAS == M_LCSS ? (b >= t) : (b <= t)) {
+      const int pos = atomicAdd(a.fcnt + q, 1);
+      a.list1[(size_t)q * a.C + pos] = c;
+    }
+  }
+}
+
+// exclusive scan of fcnt -> off2, total -> npairs (one CTA)
 __global__ void __launch_bounds__(1024) scan_kernel(KArgs a) {
   __shared__ int part[1024];
   const int per = (a.nq + 1023) / 1024;
   const int b = threadIdx.x * per, e = min(a.nq, b + per);
   int s = 0;
-  for (int i = b; i < e; ++i) s += a.cnt2[i];
+  for (int i = b; i < e; ++i) s += a.fcnt[i];
   part[threadIdx.x] = s;
   __syncthreads();
   for (int o = 1; o < 1024; o <<= 1) {
@@ -450,7 +544,7 @@ __global__ void __launch_bounds__(1024) scan_kernel(KArgs a) {
   int run = part[threadIdx.x] - s;
   for (int i = b; i < e; ++i) {
     a.off2[i] = run;
-    run += a.cnt2[i];
+    run += a.fcnt[i];
   }
   if (threadIdx.x == 1023) {
     a.off2[a.nq] = part[1023];
@@ -460,9 +554,9 @@ __global__ void __launch_bounds__(1024) scan_kernel(KArgs a) {
 
 __global__ void flatten_kernel(KArgs a) {
   const int q = blockIdx.y;
-  const int cnt = a.cnt2[q], base = a.off2[q];
+  const int cnt = a.fcnt[q], base = a.off2[q];
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += gridDim.x * blockDim.x)
-    a.flat[base + e] = make_int2(q, a.list2[(size_t)q * a.C + e]);
+    a.flat[base + e] = make_int2(q, a.list1[(size_t)q * a.C + e]);
 }
 
 // Shape-sorted schedule of the survivor pairs: counting sort by (query
@@ -520,29 +614,34 @@ __global__ void shape_scatter_kernel(KArgs a) {
 // ---------------------------------------------------------------------------
 // stage E: final selection, FP64 re-score, sort
 // ---------------------------------------------------------------------------
+// entry i of a query's refined pairs: seeds, then round 1, then round 2
+__device__ __forceinline__ void entry(const KArgs& a, int q, int i, int base, int& c, float& v) {
+  if (i < a.S) {
+    c = a.seeds[(size_t)q * a.S + i].y;
+    v = a.seed_vals[(size_t)q * a.S + i];
+  } else if (i < a.S + a.M) {
+    c = a.r1pairs[(size_t)q * a.M + i - a.S].y;
+    v = a.r1vals[(size_t)q * a.M + i - a.S];
+  } else {
+    c = a.flat[base + i - a.S - a.M].y;
+    v = a.flat_vals[base + i - a.S - a.M];
+  }
+}
+
 template <int MEAS>
 __global__ void __launch_bounds__(kSelThreads) final_select_kernel(KArgs a) {
   __shared__ unsigned long long red[33];
   __shared__ unsigned long long sel[64];
   __shared__ int rc;
   const int q = blockIdx.x;
-  const int S = a.S, nf = a.cnt2[q], base = a.off2[q];
-  const int N = S + nf;
+  const int S = a.S, M = a.M, nf = a.fcnt[q], base = a.off2[q];
+  const int N = S + M + nf;
   unsigned long long* keys = a.fkeys + (size_t)q * (a.S + a.C);
   for (int i = threadIdx.x; i < N; i += kSelThreads) {
-    unsigned long long key = ~0ull;
-    if (i < S) {
-      int c = a.seeds[(size_t)q * S + i].y;
-      if (c >= 0) {
-        float v = a.seed_vals[(size_t)q * S + i];
-        key = pack_key(MEAS == M_LCSS ? -v : v, c);
-      }
-    } else {
-      float v = a.flat_vals[base + i - S];
-      int c = a.flat[base + i - S].y;
-      key = pack_key(MEAS == M_LCSS ? -v : v, c);
-    }
-    keys[i] = key;
+    int c;
+    float v;
+    entry(a, q, i, base, c, v);
+    keys[i] = c >= 0 ? pack_key(MEAS == M_LCSS ? -v : v, c) : ~0ull;
   }
   if (threadIdx.x == 0) rc = 0;
   __syncthreads();
@@ -566,13 +665,7 @@ __global__ void __launch_bounds__(kSelThreads) final_select_kernel(KArgs a) {
   for (int i = threadIdx.x; i < N; i += kSelThreads) {
     int c;
     float v;
-    if (i < S) {
-      c = a.seeds[(size_t)q * S + i].y;
-      v = a.seed_vals[(size_t)q * S + i];
-    } else {
-      c = a.flat[base + i - S].y;
-      v = a.flat_vals[base + i - S];
-    }
+    entry(a, q, i, base, c, v);
     if (c < 0) continue;
     bool take = finite ? (v <= tr) : (pack_key(v, c) <= kth);
     if (take) {
@@ -586,14 +679,73 @@ __global__ void __launch_bounds__(kSelThreads) final_select_kernel(KArgs a) {
   if (threadIdx.x == 0) a.rcnt[q] = min(rc, a.RC);
 }
 
-// sort the re-scored pairs by (FP64 distance, index); one thread per query
+// Bound on |compensated - FP64| relative to the value, for a path of P
+// cells: (4P + 32) u^2 from the (hi, lo) arithmetic plus (P + 8) 2^-53 from
+// FP64's own rounding, with 25% slack.
+__device__ __forceinline__ double gamma_c(int P) {
+  const double u2 = 1.0 / 281474976710656.0;  // 2^-48
+  const double e53 = 1.0 / 9007199254740992.0;
+  return ((4.0 * P + 32.0) * u2 + (P + 8.0) * e53) * 1.25;
+}
+
+// Sort the re-score set by compensated value; pairs whose values are within
+// the error bound of a neighbour in that order (chains of them) cannot be
+// ordered without FP64 and are sent to the FP64 re-score.  One thread/query.
+template <int MEAS>
+__global__ void cluster_kernel(KArgs a) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= a.nq) return;
+  const int cnt = a.rcnt[q];
+  const int2* rp = a.rpairs + (size_t)q * a.RC;
+  const double* rv = a.rdc + (size_t)q * a.RC;
+  int2* r64p = a.r64pairs + (size_t)q * a.RC;
+  const double g = gamma_c(a.qlen[q] + a.max_clen);
+  unsigned char ord[256];
+  int n = 0;
+  for (int i = 0; i < cnt && i < 256; ++i) {
+    int p = n++;
+    while (p > 0) {
+      const int j = ord[p - 1];
+      if (rv[j] < rv[i] || (rv[j] == rv[i] && rp[j].y < rp[i].y)) break;
+      ord[p] = ord[p - 1];
+      --p;
+    }
+    ord[p] = (unsigned char)i;
+  }
+  for (int i = 0; i < a.RC; ++i) r64p[i] = make_int2(q, -1);
+  int sent = 0;
+  for (int p = 0; p < n; ++p) {
+    const int i = ord[p];
+    const double v = rv[i];
+    if (!(v < __longlong_as_double(0x7ff0000000000000ll))) continue;  // infeasible: exact
+    bool amb = a.force64 != 0;
+    if (p > 0) {
+      const double u = rv[ord[p - 1]];
+      if (v - u <= g * (u + v)) amb = true;
+    }
+    if (p + 1 < n) {
+      const double w = rv[ord[p + 1]];
+      if (w < __longlong_as_double(0x7ff0000000000000ll) && w - v <= g * (v + w)) amb = true;
+    }
+    if (amb) {
+      r64p[i] = rp[i];
+      ++sent;
+    }
+  }
+  if (sent) atomicAdd(a.n64, sent);
+}
+
+// final order: FP64 value for cluster members, compensated value otherwise
+// (the two agree in order across clusters); ties by candidate index
 template <int MEAS>
 __global__ void final_sort_kernel(KArgs a) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= a.nq) return;
   const int cnt = a.rcnt[q];
   const int2* rp = a.rpairs + (size_t)q * a.RC;
-  const double* rv = a.r64 + (size_t)q * a.RC;
+  const double* rc = a.rdc + (size_t)q * a.RC;
+  const double* r64 = a.r64 + (size_t)q * a.RC;
+  const int2* r64p = a.r64pairs + (size_t)q * a.RC;
   double last_d = -1.0;
   int last_c = -1;
   for (int e = 0; e < a.k; ++e) {
@@ -602,7 +754,7 @@ __global__ void final_sort_kernel(KArgs a) {
     int bc = -1;
     bool found = false;
     for (int i = 0; i < cnt; ++i) {
-      double d = rv[i];
+      double d = r64p[i].y >= 0 ? r64[i] : rc[i];
       if (MEAS == M_FRECHET) d = __dsqrt_rn(d);
       const int c = rp[i].y;
       const bool after = d > last_d || (d == last_d && c > last_c);
@@ -635,10 +787,11 @@ __global__ void clear_u32_kernel(unsigned* p, size_t n) {
 }
 
 template <int MEAS>
-int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stats* st) {
+int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, tsim_stats* st) {
   cudaStream_t s = ctx->stream;
   const int nq = a.nq;
   dim3 g1(a.nch, nq);
+  TSIM_CUDA(cudaMemsetAsync(a.n64, 0, sizeof(int), s));
   stage_begin(ctx, TSIM_STAGE_LB1);
   clear_u32_kernel<<<std::min<size_t>(((size_t)nq * a.Cw + 255) / 256, 4096), 256, 0, s>>>(
       a.seedmap, (size_t)nq * a.Cw);
@@ -691,12 +844,43 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stat
   stage_begin(ctx, TSIM_STAGE_FILTER);
   thresh_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
   compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
+  launched(ctx, 2);
   const int ch = std::max(1, std::min(64, (2 * ctx->num_sms * 4 + nq - 1) / nq));
   size_t lb2_smem = MEAS == M_FRECHET ? 0 : qtable_bytes(max_qlen);
   if (lb2_smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(lb2_kernel<MEAS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)lb2_smem));
   lb2_kernel<MEAS><<<dim3(ch, nq), kLb2Warps * 32, lb2_smem, s>>>(a);
+  r1_select_kernel<MEAS><<<nq, kSelThreads, 0, s>>>(a);
+  TSIM_CUDA(cudaGetLastError());
+  launched(ctx, 4);
+  stage_end(ctx);
+
+  // round 1: the best survivors by bound, abandon against the seed threshold
+  stage_begin(ctx, TSIM_STAGE_DP);
+  {
+    DpArgs r1 = d;
+    r1.pairs = a.r1pairs;
+    r1.npairs = nq * a.M;
+    r1.out = a.r1vals;
+    r1.thr = a.thr;
+    if (a.plain) {
+      for (int i = 0; i < nq * a.M; ++i) {
+        DpArgs one = r1;
+        one.pairs = a.r1pairs + i;
+        one.npairs = 1;
+        one.out = a.r1vals + i;
+        TSIM_TRY(launch_dp(ctx, dp32, Gs, Rs, one, a.max_clen));
+      }
+    } else {
+      TSIM_TRY(launch_dp(ctx, dp32, Gs, Rs, r1, a.max_clen));
+    }
+  }
+  stage_end(ctx);
+
+  stage_begin(ctx, TSIM_STAGE_FILTER);
+  thresh2_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+  refilter_kernel<MEAS><<<dim3(ch, nq), 256, 0, s>>>(a);
   scan_kernel<<<1, 1024, 0, s>>>(a);
   flatten_kernel<<<dim3(ch, nq), 256, 0, s>>>(a);
   TSIM_CUDA(cudaMemsetAsync(a.shape_cnt, 0, sizeof(int) * kNumShapes, s));
@@ -705,7 +889,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stat
   shape_scan_kernel<<<1, 1024, 0, s>>>(a);
   shape_scatter_kernel<<<sb, 256, 0, s>>>(a);
   TSIM_CUDA(cudaGetLastError());
-  launched(ctx, 8);
+  launched(ctx, 7);
   stage_end(ctx);
 
   stage_begin(ctx, TSIM_STAGE_DP);
@@ -713,7 +897,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stat
   d.npairs = nq * a.C;
   d.npairs_dev = a.npairs;
   d.out = a.flat_vals;
-  d.thr = a.thr;
+  d.thr = a.thr2;
   d.order = a.order;
   if (a.plain) {
     int npairs = 0;
@@ -747,13 +931,19 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stat
     r.coff = a.coff;
     r.pairs = a.rpairs;
     r.npairs = nq * a.RC;
-    r.out64 = a.r64;
+    r.out64 = a.rdc;
     r.band_pct = d.band_pct;
     r.delta = -1;
+    // compensated FP32 re-score of the set, then FP64 only for the pairs it
+    // cannot order (near-ties within the compensated error bound)
+    TSIM_TRY(launch_dp(ctx, dpc, 32, 1, r, a.max_clen));
+    cluster_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+    r.pairs = a.r64pairs;
+    r.out64 = a.r64;
     TSIM_TRY(launch_dp(ctx, dp64, 32, 1, r, a.max_clen));
     final_sort_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
     TSIM_CUDA(cudaGetLastError());
-    launched(ctx);
+    launched(ctx, 2);
     stage_end(ctx);
   }
   if (st) {
@@ -763,10 +953,13 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dp64, tsim_stat
     std::vector<int> rc(nq);
     TSIM_CUDA(cudaMemcpyAsync(rc.data(), a.rcnt, sizeof(int) * nq, cudaMemcpyDeviceToHost, s));
     TSIM_CUDA(cudaStreamSynchronize(s));
-    st->pairs_refined = (int64_t)npairs + (int64_t)nq * a.S;
+    st->pairs_refined = (int64_t)npairs + (int64_t)nq * (a.S + a.M);
     int64_t r = 0;
     for (int v : rc) r += v;
     st->rescored = MEAS == M_LCSS ? 0 : r;
+    int n64 = 0;
+    TSIM_CUDA(cudaMemcpy(&n64, a.n64, sizeof(int), cudaMemcpyDeviceToHost));
+    st->rescored_fp64 = n64;
   }
   return TSIM_OK;
 }
@@ -845,6 +1038,7 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.max_qlen = max_qlen;
   a.k = k;
   a.S = std::min(C, std::min(64, std::max(2 * k, 16)));
+  a.M = std::min(64, std::max(2 * k, 32));
   a.nch = (C + kChunk - 1) / kChunk;
   a.T = std::min(kChunk, std::max(1, (2 * a.S + a.nch - 1) / a.nch));
   a.T = std::min(a.T, 64);
@@ -854,7 +1048,8 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.delta = p->delta;
   a.eps = p->epsilon;
   a.Cw = (C + 31) / 32;
-  a.RC = std::max(4 * k, 64);
+  a.RC = std::min(256, std::max(4 * k, 64));
+  a.force64 = (p->flags & TSIM_FLAG_FP64_RESCORE) ? 1 : 0;
   a.ids = ids;
   a.dists = dists;
   a.dists64 = dists64;
@@ -870,8 +1065,10 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
                 align256(sizeof(int) * 4) + align256(sizeof(int2) * nqC) +
                 align256(sizeof(float) * nqC) +
                 align256(sizeof(unsigned long long) * nq * (size_t)(a.S + C)) +
-                align256(sizeof(int2) * nq * a.RC) + align256(sizeof(double) * nq * a.RC) +
-                align256(sizeof(int) * nqC) + align256(sizeof(int) * kNumShapes);
+                2 * align256(sizeof(int2) * nq * a.RC) + 2 * align256(sizeof(double) * nq * a.RC) +
+                align256(sizeof(int) * nqC) + align256(sizeof(int) * kNumShapes) + 256 +
+                align256(sizeof(float) * nqC) + align256(sizeof(int2) * nq * a.M) +
+                align256(sizeof(float) * nq * a.M) + 2 * align256(sizeof(float) * (nq + 1));
   TSIM_TRY(arena_reserve(ctx, need));
   float4* qbox = arena_take<float4>(ctx, nq);
   float4* qends = arena_take<float4>(ctx, nq);
@@ -897,6 +1094,14 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.fkeys = arena_take<unsigned long long>(ctx, (size_t)nq * (a.S + C));
   a.rpairs = arena_take<int2>(ctx, (size_t)nq * a.RC);
   a.r64 = arena_take<double>(ctx, (size_t)nq * a.RC);
+  a.rdc = arena_take<double>(ctx, (size_t)nq * a.RC);
+  a.r64pairs = arena_take<int2>(ctx, (size_t)nq * a.RC);
+  a.n64 = arena_take<int>(ctx, 4);
+  a.lb2v = arena_take<float>(ctx, nqC);
+  a.r1pairs = arena_take<int2>(ctx, (size_t)nq * a.M);
+  a.r1vals = arena_take<float>(ctx, (size_t)nq * a.M);
+  a.thr2 = arena_take<float>(ctx, nq + 1);
+  a.fcnt = arena_take<int>(ctx, nq + 1);
   a.order = arena_take<int>(ctx, nqC);
   a.shape_cnt = arena_take<int>(ctx, kNumShapes);
   if (!a.shape_cnt) return fail(TSIM_ERR_OUT_OF_MEMORY, "knn scratch carve failed");
@@ -907,12 +1112,14 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   switch (p->measure) {
     case TSIM_DTW:
       return run_knn<M_DTW>(ctx, a, max_qlen, p->cost ? DP_DTW_EU : DP_DTW_SQ,
-                            p->cost ? DP_DTW_EU64 : DP_DTW_SQ64, st);
+                            p->cost ? DP_DTW_EUC : DP_DTW_SQC, p->cost ? DP_DTW_EU64 : DP_DTW_SQ64,
+                            st);
     case TSIM_LCSS:
-      return run_knn<M_LCSS>(ctx, a, max_qlen, DP_LCSS, DP_LCSS, st);
+      return run_knn<M_LCSS>(ctx, a, max_qlen, DP_LCSS, DP_LCSS, DP_LCSS, st);
     case TSIM_FRECHET:
       a.band_pct = -1;
-      return run_knn<M_FRECHET>(ctx, a, max_qlen, DP_FRECHET_SQ, DP_FRECHET_SQ64, st);
+      return run_knn<M_FRECHET>(ctx, a, max_qlen, DP_FRECHET_SQ, DP_FRECHET_SQC, DP_FRECHET_SQ64,
+                                st);
   }
   return fail(TSIM_ERR_UNSUPPORTED, "measure not supported by this path");
 }
@@ -928,7 +1135,7 @@ extern "C" int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d
   TSIM_CHECK_ARG(p->k >= 1 && p->k <= 64, "k must be in 1..64");
   TSIM_CHECK_ARG(p->measure >= TSIM_DTW && p->measure <= TSIM_EUCLIDEAN, "unknown measure");
   TSIM_CHECK_ARG(p->measure != TSIM_LCSS || p->epsilon >= 0.0f, "LCSS epsilon must be >= 0");
-  TSIM_CHECK_ARG(db->ctx == ctx, "database belongs to another context");
+  TSIM_CHECK_ARG(db->ctx == ctx, "database belongs to another (or a destroyed) context");
   TSIM_CUDA(cudaSetDevice(ctx->device));
   if (stats) {
     *stats = tsim_stats{};
@@ -957,6 +1164,7 @@ extern "C" int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
                              const int64_t* h_qoff, int nq, tsim_db* db, int* h_ids,
                              float* h_dists, tsim_stats* stats) {
   TSIM_CHECK_ARG(ctx && p && db && h_qpts && h_qoff && h_ids && h_dists, "NULL argument");
+  TSIM_CHECK_ARG(db->ctx == ctx, "database belongs to another (or a destroyed) context");
   TSIM_CHECK_ARG(nq >= 1 && p->k >= 1 && p->k <= 64, "bad nq or k");
   TSIM_CHECK_ARG(h_qoff[0] == 0, "query offsets must start at 0");
   int max_qlen = 0;
@@ -1001,6 +1209,7 @@ extern "C" int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
 extern "C" int tsim_band_cells(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
                                const int64_t* d_qoff, int nq, tsim_db* db, int64_t* cells) {
   TSIM_CHECK_ARG(ctx && p && db && d_qpts && d_qoff && cells && nq >= 1, "bad arguments");
+  TSIM_CHECK_ARG(db->ctx == ctx, "database belongs to another (or a destroyed) context");
   TSIM_CHECK_ARG(p->measure == TSIM_DTW || p->measure == TSIM_LCSS || p->measure == TSIM_FRECHET,
                  "band cells are defined for the DP measures");
   TSIM_CUDA(cudaSetDevice(ctx->device));

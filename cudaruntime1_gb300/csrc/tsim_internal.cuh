@@ -44,6 +44,7 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 // ---------------------------------------------------------------------------
 // context: device, stream and a grow-only scratch arena
 // ---------------------------------------------------------------------------
+struct tsim_db;
 struct tsim_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -67,6 +68,10 @@ struct tsim_ctx {
   double stage_ms[TSIM_STAGE_COUNT] = {};
   int64_t stage_calls[TSIM_STAGE_COUNT] = {};
   unsigned long long* dcounters = nullptr;  // device: [0] DP cells computed
+  // databases created on this context; destroying the context releases their
+  // device memory and detaches them (a later tsim_db_destroy only frees the
+  // handle), so destruction order cannot cause a use-after-free
+  std::vector<tsim_db*> dbs;
 };
 
 struct tsim_db {
@@ -202,6 +207,9 @@ enum DpKind {
   DP_DTW_SQ64,      // FP64 re-score kinds: the FP64 oracle's arithmetic
   DP_DTW_EU64,
   DP_FRECHET_SQ64,
+  DP_DTW_SQC,       // compensated FP32 (hi, lo) re-score kinds
+  DP_DTW_EUC,
+  DP_FRECHET_SQC,
   DP_NUM_KINDS
 };
 

@@ -19,8 +19,9 @@
  *    include/compat/ are thin wrappers over these;
  *  - exact kNN (tsim_knn*): rectangular query x database, variable lengths,
  *    top-k ids and distances, lower-bound pruning that never drops a true
- *    neighbour, FP64 re-score of the survivors; ids ranked by
- *    (distance, candidate index), LCSS by (count descending, index).
+ *    neighbour, a compensated (double-float) FP32 re-score of the survivors
+ *    with FP64 for pairs it cannot order; ids ranked by (FP64 distance,
+ *    candidate index), LCSS by (count descending, index).
  */
 #ifndef TSIM_H
 #define TSIM_H
@@ -69,6 +70,8 @@ typedef enum tsim_cost {
 #define TSIM_FLAG_NO_PRUNE 0x1u /* compute every pair (no lower bounds) */
 #define TSIM_FLAG_PLAIN 0x2u    /* "plain" form: one DP pair per kernel launch */
 #define TSIM_FLAG_NO_GRAPH 0x4u /* do not replay through a captured CUDA graph */
+#define TSIM_FLAG_FP64_RESCORE 0x8u /* re-score every top-k pair in FP64: distances
+                                       bit-identical to an FP64 evaluation */
 
 typedef struct tsim_params {
   int measure;    /* tsim_measure */
@@ -86,7 +89,8 @@ typedef struct tsim_stats {
   int64_t pairs_refined;  /* pairs that reached the exact DP / distance */
   int64_t cells;          /* DP cells (or point pairs) actually computed */
   int64_t cells_unpruned; /* DP cells (or point pairs) of all pairs, in band */
-  int64_t rescored;       /* pairs re-scored in FP64 */
+  int64_t rescored;       /* pairs re-scored with compensated FP32 */
+  int64_t rescored_fp64;  /* of those, pairs also re-scored in FP64 (near-ties) */
   int32_t launches;       /* kernels launched (graph replays count their nodes) */
   int32_t graph_replay;   /* 1 when the call replayed a captured graph */
 } tsim_stats;
@@ -99,7 +103,7 @@ typedef enum tsim_stage {
   TSIM_STAGE_FILTER,      /* threshold, compaction, O(length) bounds, scan */
   TSIM_STAGE_DP,          /* exact FP32 DP / distance of the survivors */
   TSIM_STAGE_SELECT,      /* k-th value and re-score set */
-  TSIM_STAGE_RESCORE,     /* FP64 re-score and final sort */
+  TSIM_STAGE_RESCORE,     /* compensated / FP64 re-score and final sort */
   TSIM_STAGE_REF,         /* reference-semantics batch calls */
   TSIM_STAGE_COUNT
 } tsim_stage;
@@ -147,10 +151,12 @@ TSIM_API int64_t tsim_db_device_bytes(const tsim_db* db);
  * query x database pairs: the unpruned work, for "effective" cell rates. */
 TSIM_API int tsim_band_cells(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
                              const int64_t* d_qoff, int nq, tsim_db* db, int64_t* cells);
-/* Device pointers; results d_ids[nq*k], d_dists[nq*k] (float, from the FP64
- * re-score), d_dists64 optional (may be NULL).  LCSS distances are the
- * integer match counts.  Asynchronous on the context stream unless stats is
- * non-NULL (then the call synchronises to fill it). */
+/* Device pointers; results d_ids[nq*k], d_dists[nq*k] (float), d_dists64
+ * optional (may be NULL): the compensated FP32 value (relative error below
+ * ~1e-10 of FP64), or the FP64 value for near-tied pairs and with
+ * TSIM_FLAG_FP64_RESCORE.  Ids are exact in every case.  LCSS distances are
+ * the integer match counts.  Asynchronous on the context stream unless stats
+ * is non-NULL (then the call synchronises to fill it). */
 TSIM_API int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
                       const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
                       float* d_dists, double* d_dists64, tsim_stats* stats);

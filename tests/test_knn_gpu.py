@@ -58,10 +58,19 @@ def test_knn_matches_fp64_oracle(tsim, cuda_ctx, oracle, measure, kw):
     if measure == "lcss":
         assert np.array_equal(d.astype(np.float64), want_d)
     else:
-        assert np.array_equal(d64, want_d)
         fin = np.isfinite(want_d)
+        assert np.array_equal(np.isfinite(d64), fin)
         rel = np.abs(d.astype(np.float64)[fin] - want_d[fin]) / np.maximum(want_d[fin], 1e-30)
         assert rel.max() <= REL_TOL
+        # compensated re-score: double-float accuracy against FP64
+        rel64 = np.abs(d64[fin] - want_d[fin]) / np.maximum(want_d[fin], 1e-30)
+        assert rel64.max() <= 1e-9, rel64.max()
+        # forced FP64 re-score: bit-identical to the FP64 oracle
+        ids2, _, d64b, st2 = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, k,
+                                         flags=tsim.api.FLAG_FP64_RESCORE, **kw)
+        assert np.array_equal(ids2, want_ids)
+        assert np.array_equal(d64b, want_d)
+        assert st2["rescored_fp64"] >= np.isfinite(want_d).sum()
     # the host-pointer entry point gives the same answer
     ids_h, d_h, _ = tsim.knn(cuda_ctx, db, qp, qo, measure, k, **kw)
     assert np.array_equal(ids_h, ids) and np.array_equal(d_h, d)
@@ -105,3 +114,20 @@ def test_knn_longer_queries_than_candidates(tsim, cuda_ctx, oracle):
         ids, d, d64, _ = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 5, **kw)
         assert np.array_equal(ids, want_ids), measure
     db.close()
+
+
+def test_context_destroyed_before_database(tsim):
+    """Destroying a context releases its databases' device memory and
+    detaches them; closing such a database afterwards is safe and using it is
+    an error, whatever order Python collects the objects in."""
+    ctx = tsim.Context(0)
+    cp, co = _db(50, 8, 20, 700)
+    db = tsim.Database(ctx, cp, co)
+    qp, qo = G.random_walks(1, 10, 701)
+    ids, _, _ = tsim.knn(ctx, db, qp, qo, "dtw", 3)
+    ctx2 = tsim.Context(0)
+    with pytest.raises(tsim._lib.TsimError):
+        tsim.knn(ctx2, db, qp, qo, "dtw", 3)  # wrong context
+    ctx.close()
+    db.close()
+    ctx2.close()
