@@ -43,7 +43,12 @@ constexpr int kSelThreads = 256;
 constexpr int kLb2Warps = 8;
 constexpr int kMaxTable = 512;  // sparse-table columns (query rows, downsampled beyond)
 
-enum Meas { M_DTW = 0, M_LCSS = 1, M_FRECHET = 2 };
+enum Meas { M_DTW = 0, M_LCSS = 1, M_FRECHET = 2, M_HAUSDORFF = 3, M_EUCLID = 4 };
+
+// measures refined by the wavefront DP (the others by pairwise kernels)
+constexpr bool is_dp(int meas) { return meas <= M_FRECHET; }
+// values carried in the squared domain (sqrt applied to the reported distance)
+constexpr bool is_squared(int meas) { return meas >= M_FRECHET; }
 
 struct KArgs {
   // queries
@@ -113,7 +118,8 @@ __device__ __forceinline__ double gamma_dp(int meas, int n, int m) {
   // every cost carries <= 4 roundings, a path of <= n+m-1 cells adds one
   // rounding per cell; Frechet values are single costs.
   const double u = 1.0 / 16777216.0;
-  if (meas == M_FRECHET) return 8.0 * u;
+  if (meas == M_FRECHET || meas == M_HAUSDORFF) return 8.0 * u;  // one FMA distance
+  if (meas == M_EUCLID) return 16.0 * u;  // compensated sum of FMA terms
   return (double)(n + m + 8) * u * 1.01 + 1e-12;
 }
 
@@ -137,10 +143,25 @@ __device__ __forceinline__ float bound1(const KArgs& a, float4 qb, float4 qe, in
               cb.w >= __fsub_rd(qb.y, e2) && cb.y <= __fadd_ru(qb.w, e2);
     return ov ? (float)min(n, m) : 0.0f;
   }
+  if (MEAS == M_HAUSDORFF) {
+    // the extreme point of either set along an axis is at least the
+    // difference of the two boxes' edges away from every point of the other
+    const float e = fmaxf(fmaxf(absdiff_rd(qb.x, cb.x), absdiff_rd(qb.z, cb.z)),
+                          fmaxf(absdiff_rd(qb.y, cb.y), absdiff_rd(qb.w, cb.w)));
+    return __fmul_rd(e, e);
+  }
   const float first = pd2_rd(qe.x, qe.y, ce.x, ce.y);
   const float last = pd2_rd(qe.z, qe.w, ce.z, ce.w);
   const float bb = box_box_d2_rd(qb, cb);
   if (MEAS == M_FRECHET) return fmaxf(fmaxf(first, last), bb);
+  if (MEAS == M_EUCLID) {
+    // point i of the candidate is paired with point i of the query; the
+    // query's full box contains its first-m-point prefix
+    if (n < m) return TSIM_INF;
+    if (m == 1) return first;
+    if (n == m) return __fadd_rd(__fadd_rd(first, last), __fmul_rd((float)(m - 2), bb));
+    return __fadd_rd(first, __fmul_rd((float)(m - 1), bb));
+  }
   // DTW: the path has >= max(n,m) cells; (0,0) and (n-1,m-1) are on it
   const int L = max(n, m);
   if (L < 2) return a.cost ? __fsqrt_rd(first) : first;
@@ -335,9 +356,10 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
   const float t = a.thr[q];
   // a query longer than the table was sized for passes every pair (the
   // bound is skipped, never guessed)
+  constexpr bool kTable = MEAS == M_DTW || MEAS == M_LCSS;
   const bool use_table = n <= a.max_qlen;
   QTable T;
-  if (MEAS != M_FRECHET && use_table) qtable_build(T, A, n, reinterpret_cast<float4*>(smem_raw));
+  if (kTable && use_table) qtable_build(T, A, n, reinterpret_cast<float4*>(smem_raw));
   const float e2 = __fmul_ru(a.eps, 1.0f + 1.0f / 1048576.0f);
   for (int e = blockIdx.x * kLb2Warps + warp; e < cnt; e += gridDim.x * kLb2Warps) {
     const int c = a.list1[(size_t)q * a.C + e];
@@ -347,7 +369,11 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
     float lbv = MEAS == M_LCSS ? (float)min(n, m) : 0.0f;  // the bound (no bound: trivial)
     if (n <= 0 || m <= 0) {
       pass = false;
-    } else if (MEAS != M_FRECHET && !use_table) {
+    } else if (MEAS == M_EUCLID) {
+      // no O(length) bound: the exact sum costs the same
+      lbv = a.lb1[(size_t)q * a.C + c];
+      pass = true;
+    } else if (kTable && !use_table) {
       pass = true;
     } else if (MEAS == M_DTW) {
       // banded LB_Keogh: column j costs at least the distance from c_j to the
@@ -405,9 +431,10 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
       feasible = __all_sync(0xffffffffu, feasible);
       pass = feasible && acc <= t;
       lbv = feasible ? acc : TSIM_INF;
-    } else if (MEAS == M_FRECHET) {
-      // every point of either trajectory is coupled to some point of the
-      // other, so F^2 >= its squared distance to the other's box
+    } else if (MEAS == M_FRECHET || MEAS == M_HAUSDORFF) {
+      // every point of either trajectory is coupled to (Frechet) or has a
+      // nearest point in (Hausdorff) the other, so the squared distance is
+      // at least its squared distance to the other's box
       const float4 cb = a.cbox[c];
       float mx = 0.0f;
       for (int j = lane; j < m; j += 32) {
@@ -670,7 +697,10 @@ __global__ void __launch_bounds__(kSelThreads) final_select_kernel(KArgs a) {
     bool take = finite ? (v <= tr) : (pack_key(v, c) <= kth);
     if (take) {
       int p = atomicAdd(&rc, 1);
-      if (p < a.RC) a.rpairs[(size_t)q * a.RC + p] = make_int2(q, c);
+      if (p < a.RC) {
+        a.rpairs[(size_t)q * a.RC + p] = make_int2(q, c);
+        a.rdc[(size_t)q * a.RC + p] = v;  // pairwise measures re-use their FP32 values
+      }
     }
   }
   __syncthreads();
@@ -699,7 +729,9 @@ __global__ void cluster_kernel(KArgs a) {
   const int2* rp = a.rpairs + (size_t)q * a.RC;
   const double* rv = a.rdc + (size_t)q * a.RC;
   int2* r64p = a.r64pairs + (size_t)q * a.RC;
-  const double g = gamma_c(a.qlen[q] + a.max_clen);
+  // compensated DP values: gamma_c; FP32 pairwise values: twice their bound
+  const double g = is_dp(MEAS) ? gamma_c(a.qlen[q] + a.max_clen)
+                               : 2.0 * gamma_dp(MEAS, a.qlen[q], a.max_clen);
   unsigned char ord[256];
   int n = 0;
   for (int i = 0; i < cnt && i < 256; ++i) {
@@ -755,7 +787,7 @@ __global__ void final_sort_kernel(KArgs a) {
     bool found = false;
     for (int i = 0; i < cnt; ++i) {
       double d = r64p[i].y >= 0 ? r64[i] : rc[i];
-      if (MEAS == M_FRECHET) d = __dsqrt_rn(d);
+      if (is_squared(MEAS)) d = __dsqrt_rn(d);
       const int c = rp[i].y;
       const bool after = d > last_d || (d == last_d && c > last_c);
       if (!after) continue;
@@ -784,6 +816,15 @@ __global__ void clear_u32_kernel(unsigned* p, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
     p[i] = 0;
+}
+
+// the FP32 refine of a pair list: wavefront DP or a pairwise kernel
+template <int MEAS>
+int refine32(tsim_ctx* ctx, int dp32, int G, int R, const DpArgs& d, int max_clen) {
+  if (is_dp(MEAS)) return launch_dp(ctx, dp32, G, R, d, max_clen);
+  PwArgs p{d.qpts, d.qoff, d.cpts, d.coff, d.pairs, d.npairs, d.npairs_dev, d.order, d.out,
+           nullptr, d.thr};
+  return launch_pairwise(ctx, MEAS == M_HAUSDORFF ? TSIM_HAUSDORFF : TSIM_EUCLIDEAN, p);
 }
 
 template <int MEAS>
@@ -834,10 +875,10 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
       one.pairs = a.seeds + i;
       one.npairs = 1;
       one.out = a.seed_vals + i;
-      TSIM_TRY(launch_dp(ctx, dp32, Gs, Rs, one, a.max_clen));
+      TSIM_TRY(refine32<MEAS>(ctx, dp32, Gs, Rs, one, a.max_clen));
     }
   } else {
-    TSIM_TRY(launch_dp(ctx, dp32, Gs, Rs, d, a.max_clen));
+    TSIM_TRY(refine32<MEAS>(ctx, dp32, Gs, Rs, d, a.max_clen));
   }
   stage_end(ctx);
 
@@ -846,7 +887,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
   launched(ctx, 2);
   const int ch = std::max(1, std::min(64, (2 * ctx->num_sms * 4 + nq - 1) / nq));
-  size_t lb2_smem = MEAS == M_FRECHET ? 0 : qtable_bytes(max_qlen);
+  size_t lb2_smem = (MEAS == M_DTW || MEAS == M_LCSS) ? qtable_bytes(max_qlen) : 0;
   if (lb2_smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(lb2_kernel<MEAS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)lb2_smem));
@@ -870,10 +911,10 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
         one.pairs = a.r1pairs + i;
         one.npairs = 1;
         one.out = a.r1vals + i;
-        TSIM_TRY(launch_dp(ctx, dp32, Gs, Rs, one, a.max_clen));
+        TSIM_TRY(refine32<MEAS>(ctx, dp32, Gs, Rs, one, a.max_clen));
       }
     } else {
-      TSIM_TRY(launch_dp(ctx, dp32, Gs, Rs, r1, a.max_clen));
+      TSIM_TRY(refine32<MEAS>(ctx, dp32, Gs, Rs, r1, a.max_clen));
     }
   }
   stage_end(ctx);
@@ -910,10 +951,10 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
       one.npairs_dev = nullptr;
       one.order = nullptr;
       one.out = a.flat_vals + i;
-      TSIM_TRY(launch_dp(ctx, dp32, Gs, Rs, one, a.max_clen));
+      TSIM_TRY(refine32<MEAS>(ctx, dp32, Gs, Rs, one, a.max_clen));
     }
   } else {
-    TSIM_TRY(launch_dp(ctx, dp32, G, R, d, a.max_clen));
+    TSIM_TRY(refine32<MEAS>(ctx, dp32, G, R, d, a.max_clen));
   }
   stage_end(ctx);
 
@@ -936,11 +977,17 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
     r.delta = -1;
     // compensated FP32 re-score of the set, then FP64 only for the pairs it
     // cannot order (near-ties within the compensated error bound)
-    TSIM_TRY(launch_dp(ctx, dpc, 32, 1, r, a.max_clen));
+    if (is_dp(MEAS)) TSIM_TRY(launch_dp(ctx, dpc, 32, 1, r, a.max_clen));
     cluster_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
     r.pairs = a.r64pairs;
     r.out64 = a.r64;
-    TSIM_TRY(launch_dp(ctx, dp64, 32, 1, r, a.max_clen));
+    if (is_dp(MEAS)) {
+      TSIM_TRY(launch_dp(ctx, dp64, 32, 1, r, a.max_clen));
+    } else {
+      PwArgs p{a.qpts, a.qoff, a.cpts, a.coff, a.r64pairs, nq * a.RC, nullptr, nullptr, nullptr,
+               a.r64, nullptr};
+      TSIM_TRY(launch_pairwise64(ctx, MEAS == M_HAUSDORFF ? TSIM_HAUSDORFF : TSIM_EUCLIDEAN, p));
+    }
     final_sort_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
     TSIM_CUDA(cudaGetLastError());
     launched(ctx, 2);
@@ -958,7 +1005,8 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
     for (int v : rc) r += v;
     st->rescored = MEAS == M_LCSS ? 0 : r;
     int n64 = 0;
-    TSIM_CUDA(cudaMemcpy(&n64, a.n64, sizeof(int), cudaMemcpyDeviceToHost));
+    TSIM_CUDA(cudaMemcpyAsync(&n64, a.n64, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TSIM_CUDA(cudaStreamSynchronize(s));
     st->rescored_fp64 = n64;
   }
   return TSIM_OK;
@@ -1120,6 +1168,12 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
       a.band_pct = -1;
       return run_knn<M_FRECHET>(ctx, a, max_qlen, DP_FRECHET_SQ, DP_FRECHET_SQC, DP_FRECHET_SQ64,
                                 st);
+    case TSIM_HAUSDORFF:
+      a.band_pct = -1;
+      return run_knn<M_HAUSDORFF>(ctx, a, max_qlen, 0, 0, 0, st);
+    case TSIM_EUCLIDEAN:
+      a.band_pct = -1;
+      return run_knn<M_EUCLID>(ctx, a, max_qlen, 0, 0, 0, st);
   }
   return fail(TSIM_ERR_UNSUPPORTED, "measure not supported by this path");
 }
@@ -1141,14 +1195,24 @@ extern "C" int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d
     *stats = tsim_stats{};
     TSIM_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
   }
-  int s;
-  if (p->measure == TSIM_HAUSDORFF || p->measure == TSIM_EUCLIDEAN)
-    s = tsim::knn_pairwise(ctx, p, reinterpret_cast<const float2*>(d_qpts), d_qoff, nq, max_qlen,
-                           db, d_ids, d_dists, d_dists64, stats);
-  else
-    s = tsim::knn(ctx, p, reinterpret_cast<const float2*>(d_qpts), d_qoff, nq, max_qlen, db, d_ids,
-                  d_dists, d_dists64, stats);
-  if (s != TSIM_OK) return s;
+  // queries in batches whose pair count keeps the scratch bounded (offsets
+  // stay absolute into d_qpts, so a batch is a slice of d_qoff)
+  const int64_t kMaxPairs = int64_t(1) << 24;
+  const int qb = (int)std::max<int64_t>(1, std::min<int64_t>(nq, kMaxPairs / std::max(db->count, 1)));
+  tsim_stats acc{};
+  for (int q0 = 0; q0 < nq; q0 += qb) {
+    const int nb = std::min(qb, nq - q0);
+    tsim_stats part{};
+    int s = tsim::knn(ctx, p, reinterpret_cast<const float2*>(d_qpts), d_qoff + q0, nb, max_qlen,
+                      db, d_ids + (size_t)q0 * p->k, d_dists + (size_t)q0 * p->k,
+                      d_dists64 ? d_dists64 + (size_t)q0 * p->k : nullptr,
+                      stats ? &part : nullptr);
+    if (s != TSIM_OK) return s;
+    acc.pairs_refined += part.pairs_refined;
+    acc.rescored += part.rescored;
+    acc.rescored_fp64 += part.rescored_fp64;
+  }
+  if (stats) *stats = acc;
   if (stats) {
     TSIM_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     TSIM_CUDA(cudaEventSynchronize(ctx->ev1));

@@ -222,9 +222,23 @@ int ref_batch_core(tsim_ctx* ctx, int measure, const float2* d_t1, const float2*
 
 int band_cells(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
                tsim_db* db, int64_t* cells_out);
-int knn_pairwise(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff,
-                 int nq, int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64,
-                 tsim_stats* st);
+
+// warp-per-pair refine kernels of Hausdorff and Euclidean (pairwise_knn.cu)
+struct PwArgs {
+  const float2* qpts;
+  const int64_t* qoff;
+  const float2* cpts;
+  const int64_t* coff;
+  const int2* pairs;
+  int npairs;
+  const int* npairs_dev;
+  const int* order;
+  float* out;       // FP32 pass: squared Hausdorff / squared Euclidean, +inf if abandoned
+  double* out64;    // FP64 pass
+  const float* thr; // per query abandon threshold or null
+};
+int launch_pairwise(tsim_ctx* ctx, int measure, const PwArgs& a);
+int launch_pairwise64(tsim_ctx* ctx, int measure, const PwArgs& a);
 
 // G lanes per pair (4, 8, 16 or 32), R rows per lane (1, 2, 4 or 8).
 int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a, int max_m);

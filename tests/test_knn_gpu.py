@@ -39,6 +39,7 @@ CASES = [
     ("lcss", dict(epsilon=0.5, delta=5)),
     ("lcss", dict(epsilon=0.25, delta=-1)),
     ("frechet", dict()),
+    ("hausdorff", dict()),
 ]
 
 
@@ -62,9 +63,10 @@ def test_knn_matches_fp64_oracle(tsim, cuda_ctx, oracle, measure, kw):
         assert np.array_equal(np.isfinite(d64), fin)
         rel = np.abs(d.astype(np.float64)[fin] - want_d[fin]) / np.maximum(want_d[fin], 1e-30)
         assert rel.max() <= REL_TOL
-        # compensated re-score: double-float accuracy against FP64
+        # compensated DP re-score: double-float accuracy against FP64;
+        # pairwise measures report their FP32 values (FP64 only for near-ties)
         rel64 = np.abs(d64[fin] - want_d[fin]) / np.maximum(want_d[fin], 1e-30)
-        assert rel64.max() <= 1e-9, rel64.max()
+        assert rel64.max() <= (1e-9 if measure in ("dtw", "frechet") else 1e-6), rel64.max()
         # forced FP64 re-score: bit-identical to the FP64 oracle
         ids2, _, d64b, st2 = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, k,
                                          flags=tsim.api.FLAG_FP64_RESCORE, **kw)
@@ -131,3 +133,43 @@ def test_context_destroyed_before_database(tsim):
     ctx.close()
     db.close()
     ctx2.close()
+
+
+def test_euclidean_knn_prefix_rule_and_long_pairs(tsim, cuda_ctx, oracle):
+    """Lock-step Euclidean: candidates of length 64 and a few of 1,100 points
+    (> 1024: the FP64 accumulation branch) against queries of 1,100 points;
+    a candidate is compared with the query's first m points."""
+    rng = np.random.default_rng(9)
+    lens = np.where(rng.random(600) < 0.02, 1100, 64)
+    lens[:3] = 1100
+    cp, co = G.random_walks(600, lens, 901, step="student_t")
+    qp, qo = G.random_walks(5, 1100, 902, step="student_t")
+    # plant near matches: candidate 1 = query 0 plus noise, candidate 7 = query 1 prefix
+    cp[co[1]:co[2]] = qp[qo[0]:qo[0] + 1100] + 0.01
+    cp[co[7]:co[8]] = qp[qo[1]:qo[1] + lens[7]] + 0.02
+    db = tsim.Database(cuda_ctx, cp, co)
+    want_ids, want_d = oracle.knn("euclidean", qp, qo, cp, co, 10)
+    ids, d, d64, st = _device_knn(tsim, cuda_ctx, db, qp, qo, "euclidean", 10)
+    assert np.array_equal(ids, want_ids)
+    assert ids[0][0] == 1 and ids[1][0] == 7
+    fin = np.isfinite(want_d)
+    assert np.max(np.abs(d[fin] - want_d[fin]) / want_d[fin]) <= REL_TOL
+    ids2, _, d64b, _ = _device_knn(tsim, cuda_ctx, db, qp, qo, "euclidean", 10,
+                                   flags=tsim.api.FLAG_FP64_RESCORE)
+    assert np.array_equal(ids2, want_ids) and np.array_equal(d64b, want_d)
+    db.close()
+
+
+def test_query_batches(tsim, cuda_ctx, oracle):
+    """More query x candidate pairs than one batch holds: the queries are
+    processed in slices with the same results."""
+    cp, co = _db(70000, 8, 24, 950)
+    qp, qo = G.random_walks(300, G.uniform_lengths(300, 8, 24, 951), 952)
+    db = tsim.Database(cuda_ctx, cp, co)
+    sel = [0, 137, 299]
+    ids, d, d64, _ = _device_knn(tsim, cuda_ctx, db, qp, qo, "frechet", 4)
+    for q in sel:
+        sub_o = np.array([0, qo[q + 1] - qo[q]])
+        wi, wd = oracle.knn("frechet", qp[qo[q]:qo[q + 1]], sub_o, cp, co, 4)
+        assert np.array_equal(ids[q], wi[0]), q
+    db.close()
