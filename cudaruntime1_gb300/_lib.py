@@ -34,7 +34,8 @@ class TsimParams(C.Structure):
 
 
 class TsimStats(C.Structure):
-    _fields_ = [("ms", C.c_double), ("pairs", C.c_int64), ("pairs_refined", C.c_int64),
+    _fields_ = [("ms", C.c_double), ("pairs", C.c_int64), ("pairs_lb1", C.c_int64),
+                ("pairs_lb2", C.c_int64), ("pairs_refined", C.c_int64),
                 ("cells", C.c_int64), ("cells_unpruned", C.c_int64), ("rescored", C.c_int64),
                 ("rescored_fp64", C.c_int64),
                 ("launches", C.c_int32), ("graph_replay", C.c_int32)]

@@ -92,6 +92,9 @@ struct KArgs {
   float* r1vals;            // [nq*M]
   float* thr2;              // [nq]  threshold after round 1
   int* fcnt;                // [nq]  round-2 pairs per query (in list1)
+  const float4* csegbox;    // [C*kSegs] candidate segment boxes
+  float4* qtab;             // [nq*tstride] query sparse tables (global memory)
+  int tstride;
   int* off2;                // [nq+1]
   int* npairs;              // [1]
   int2* flat;               // [nq*C]
@@ -261,28 +264,6 @@ __global__ void thresh_kernel(KArgs a) {
 // ---------------------------------------------------------------------------
 // stage C: compaction and O(length) bounds
 // ---------------------------------------------------------------------------
-template <int MEAS>
-__global__ void __launch_bounds__(kChunk) compact_kernel(KArgs a) {
-  const int q = blockIdx.y;
-  const int c = blockIdx.x * kChunk + threadIdx.x;
-  const float t = a.thr[q];
-  bool pass = false;
-  if (c < a.C) {
-    const bool seeded = (a.seedmap[(size_t)q * a.Cw + (c >> 5)] >> (c & 31)) & 1u;
-    const float b = a.lb1[(size_t)q * a.C + c];
-    pass = !seeded && (MEAS == M_LCSS ? (b >= t) : (b <= t));
-  }
-  const unsigned ball = __ballot_sync(0xffffffffu, pass);
-  if (ball) {
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(ball) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(a.cnt1 + q, __popc(ball));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (pass) a.list1[(size_t)q * a.C + base + __popc(ball & ((1u << lane) - 1))] = c;
-  }
-}
-
 // Sparse table of the query for O(1) range boxes: level l holds, for block b,
 // the box of blocks [b, b + 2^l).  Block = f consecutive rows (f = 1 for
 // queries up to kMaxTable rows, a power of two beyond, which widens boxes and
@@ -341,6 +322,134 @@ size_t qtable_bytes(int max_n) {
   int levels = 1;
   while ((1 << levels) <= nb) ++levels;
   return (size_t)levels * nb * sizeof(float4);
+}
+
+// view of a query table built by qtable_build for a query of n rows
+__device__ __forceinline__ QTable qtable_view(float4* t, int n) {
+  QTable T;
+  int f_log = 0;
+  while ((n + (1 << f_log) - 1) >> f_log > kMaxTable) ++f_log;
+  T.t = t;
+  T.f_log = f_log;
+  T.nb = (n + (1 << f_log) - 1) >> f_log;
+  int levels = 1;
+  while ((1 << levels) <= T.nb) ++levels;
+  T.levels = levels;
+  return T;
+}
+
+// one CTA per query: its sparse table in global memory (read by the
+// segment bound of every pair of the query)
+__global__ void qtable_global_kernel(KArgs a) {
+  const int q = blockIdx.x;
+  const int n = a.qlen[q];
+  if (n <= 0 || n > a.max_qlen) return;
+  QTable T;
+  qtable_build(T, a.qpts + a.qoff[q], n, a.qtab + (size_t)q * a.tstride);
+}
+
+// Segment bound of one pair: every column of candidate segment s lies in the
+// segment's box, and its band admits only the query rows between the band
+// rows of the segment's first and last column, so the column costs at least
+// the squared distance between the segment box and the box of those rows
+// (DTW: summed over the segment's columns; Frechet and Hausdorff: every
+// point is matched, so the maximum over segments; LCSS: a column can only
+// match when the boxes, eps-inflated, meet).  Columns 0 and m-1 are the
+// exact corner cells for DTW.
+template <int MEAS>
+__device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1) {
+  if (MEAS == M_EUCLID || n > a.max_qlen || n < 1 || m < 1) return lb1;
+  const float4* sb = a.csegbox + (size_t)c * kSegs;
+  const float4 qb = a.qbox[q];
+  if (MEAS == M_FRECHET || MEAS == M_HAUSDORFF) {
+    float mx = lb1;
+    for (int s = 0; s < kSegs; ++s) {
+      const float4 b = sb[s];
+      if (b.x > b.z) continue;  // empty segment
+      mx = fmaxf(mx, box_box_d2_rd(qb, b));
+    }
+    return mx;
+  }
+  const QTable T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
+  if (MEAS == M_LCSS) {
+    const float e2 = __fmul_ru(a.eps, 1.0f + 1.0f / 1048576.0f);
+    int count = 0;
+    for (int s = 0; s < kSegs; ++s) {
+      const int b0 = (int)((long long)s * m / kSegs), b1 = (int)((long long)(s + 1) * m / kSegs) - 1;
+      if (b1 < b0) continue;
+      int lo = 0, hi = n - 1;
+      if (a.delta >= 0) {
+        lo = max(0, b0 - a.delta);
+        hi = min(n - 1, b1 + a.delta);
+      }
+      if (lo > hi) continue;
+      const float4 qx = qtable_box(T, lo, hi), b = sb[s];
+      if (b.z >= __fsub_rd(qx.x, e2) && b.x <= __fadd_ru(qx.z, e2) && b.w >= __fsub_rd(qx.y, e2) &&
+          b.y <= __fadd_ru(qx.w, e2))
+        count += b1 - b0 + 1;
+    }
+    return fminf(lb1, (float)min(count, min(n, m)));
+  }
+  // DTW
+  const float4 qe = a.qends[q], ce = a.cends[c];
+  float acc;
+  if (m == 1) {
+    float d = pd2_rd(qe.x, qe.y, ce.x, ce.y);
+    acc = a.cost ? __fsqrt_rd(d) : d;
+    if (n > 1) {
+      float d2 = pd2_rd(qe.z, qe.w, ce.x, ce.y);
+      acc = __fadd_rd(acc, a.cost ? __fsqrt_rd(d2) : d2);
+    }
+    return fmaxf(acc, lb1);
+  }
+  {
+    float d0 = pd2_rd(qe.x, qe.y, ce.x, ce.y), d1 = pd2_rd(qe.z, qe.w, ce.z, ce.w);
+    acc = a.cost ? __fadd_rd(__fsqrt_rd(d0), __fsqrt_rd(d1)) : __fadd_rd(d0, d1);
+  }
+  const int w = band_w(n, m, a.band_pct);
+  const bool banded = w >= 0 && n > 1;
+  const long long W = banded ? (long long)w * (min(n, m) - 1) : 0;
+  for (int s = 0; s < kSegs; ++s) {
+    const int b0 = max(1, (int)((long long)s * m / kSegs));
+    const int b1 = min(m - 2, (int)((long long)(s + 1) * m / kSegs) - 1);
+    if (b1 < b0) continue;
+    int lo = 0, hi = n - 1;
+    if (banded) {
+      lo = (int)max(0ll, -floordiv_ll(-((long long)b0 * (n - 1) - W), m - 1));
+      hi = (int)min((long long)n - 1, floordiv_ll((long long)b1 * (n - 1) + W, m - 1));
+    }
+    if (lo > hi) return TSIM_INF;  // a column with no admissible row: infeasible
+    const float4 qx = qtable_box(T, lo, hi);
+    const float d = box_box_d2_rd(qx, sb[s]);
+    acc = __fadd_rd(acc, __fmul_rd((float)(b1 - b0 + 1), a.cost ? __fsqrt_rd(d) : d));
+  }
+  return fmaxf(acc, lb1);
+}
+
+template <int MEAS>
+__global__ void __launch_bounds__(kChunk) compact_kernel(KArgs a) {
+  const int q = blockIdx.y;
+  const int c = blockIdx.x * kChunk + threadIdx.x;
+  const float t = a.thr[q];
+  bool pass = false;
+  if (c < a.C) {
+    const bool seeded = (a.seedmap[(size_t)q * a.Cw + (c >> 5)] >> (c & 31)) & 1u;
+    const float b = a.lb1[(size_t)q * a.C + c];
+    pass = !seeded && (MEAS == M_LCSS ? (b >= t) : (b <= t));
+    if (pass) {  // the segment bound, only for pairs the O(1) bound keeps
+      const float sbnd = seg_bound<MEAS>(a, q, c, a.qlen[q], a.clen[c], b);
+      pass = MEAS == M_LCSS ? (sbnd >= t) : (sbnd <= t);
+    }
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, pass);
+  if (ball) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ball) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(a.cnt1 + q, __popc(ball));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pass) a.list1[(size_t)q * a.C + base + __popc(ball & ((1u << lane) - 1))] = c;
+  }
 }
 
 template <int MEAS>
@@ -884,6 +993,10 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
 
   stage_begin(ctx, TSIM_STAGE_FILTER);
   thresh_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+  if (MEAS == M_DTW || MEAS == M_LCSS) {
+    qtable_global_kernel<<<nq, 256, 0, s>>>(a);
+    launched(ctx);
+  }
   compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
   launched(ctx, 2);
   const int ch = std::max(1, std::min(64, (2 * ctx->num_sms * 4 + nq - 1) / nq));
@@ -997,9 +1110,15 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
     // counts for the caller (synchronises)
     int npairs = 0;
     TSIM_CUDA(cudaMemcpyAsync(&npairs, a.npairs, sizeof(int), cudaMemcpyDeviceToHost, s));
-    std::vector<int> rc(nq);
+    std::vector<int> rc(nq), c1(nq), c2(nq);
     TSIM_CUDA(cudaMemcpyAsync(rc.data(), a.rcnt, sizeof(int) * nq, cudaMemcpyDeviceToHost, s));
+    TSIM_CUDA(cudaMemcpyAsync(c1.data(), a.cnt1, sizeof(int) * nq, cudaMemcpyDeviceToHost, s));
+    TSIM_CUDA(cudaMemcpyAsync(c2.data(), a.cnt2, sizeof(int) * nq, cudaMemcpyDeviceToHost, s));
     TSIM_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < nq; ++i) {
+      st->pairs_lb1 += c1[i];
+      st->pairs_lb2 += c2[i];
+    }
     st->pairs_refined = (int64_t)npairs + (int64_t)nq * (a.S + a.M);
     int64_t r = 0;
     for (int v : rc) r += v;
@@ -1084,6 +1203,7 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.C = C;
   a.max_clen = db->max_len;
   a.max_qlen = max_qlen;
+  a.tstride = (int)(qtable_bytes(max_qlen) / sizeof(float4));
   a.k = k;
   a.S = std::min(C, std::min(64, std::max(2 * k, 16)));
   a.M = std::min(64, std::max(2 * k, 32));
@@ -1116,7 +1236,8 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
                 2 * align256(sizeof(int2) * nq * a.RC) + 2 * align256(sizeof(double) * nq * a.RC) +
                 align256(sizeof(int) * nqC) + align256(sizeof(int) * kNumShapes) + 256 +
                 align256(sizeof(float) * nqC) + align256(sizeof(int2) * nq * a.M) +
-                align256(sizeof(float) * nq * a.M) + 2 * align256(sizeof(float) * (nq + 1));
+                align256(sizeof(float) * nq * a.M) + 2 * align256(sizeof(float) * (nq + 1)) +
+                align256(sizeof(float4) * (size_t)nq * a.tstride);
   TSIM_TRY(arena_reserve(ctx, need));
   float4* qbox = arena_take<float4>(ctx, nq);
   float4* qends = arena_take<float4>(ctx, nq);
@@ -1150,6 +1271,8 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.r1vals = arena_take<float>(ctx, (size_t)nq * a.M);
   a.thr2 = arena_take<float>(ctx, nq + 1);
   a.fcnt = arena_take<int>(ctx, nq + 1);
+  a.qtab = arena_take<float4>(ctx, (size_t)nq * a.tstride);
+  a.csegbox = db->segbox;
   a.order = arena_take<int>(ctx, nqC);
   a.shape_cnt = arena_take<int>(ctx, kNumShapes);
   if (!a.shape_cnt) return fail(TSIM_ERR_OUT_OF_MEMORY, "knn scratch carve failed");
@@ -1209,6 +1332,8 @@ extern "C" int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d
                       stats ? &part : nullptr);
     if (s != TSIM_OK) return s;
     acc.pairs_refined += part.pairs_refined;
+    acc.pairs_lb1 += part.pairs_lb1;
+    acc.pairs_lb2 += part.pairs_lb2;
     acc.rescored += part.rescored;
     acc.rescored_fp64 += part.rescored_fp64;
   }

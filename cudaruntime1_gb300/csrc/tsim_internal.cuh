@@ -41,6 +41,10 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
     if (_s != TSIM_OK) return _s; \
   } while (0)
 
+// Candidate trajectories carry the bounding boxes of kSegs consecutive
+// column segments: segment s covers columns [s*m/kSegs, (s+1)*m/kSegs).
+constexpr int kSegs = 8;
+
 // ---------------------------------------------------------------------------
 // context: device, stream and a grow-only scratch arena
 // ---------------------------------------------------------------------------
@@ -85,6 +89,7 @@ struct tsim_db {
   float4* box = nullptr;      // device [count] (x0, y0, x1, y1)
   float4* ends = nullptr;     // device [count] (first.x, first.y, last.x, last.y)
   int* len = nullptr;         // device [count]
+  float4* segbox = nullptr;   // device [count * kSegs]: boxes of kSegs equal column segments
   std::vector<int64_t> h_off; // host copy of offsets (lengths for scheduling)
 };
 

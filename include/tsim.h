@@ -86,6 +86,8 @@ typedef struct tsim_params {
 typedef struct tsim_stats {
   double ms;              /* device time of the call (CUDA events) */
   int64_t pairs;          /* query x candidate pairs in the request */
+  int64_t pairs_lb1;      /* pairs passing the O(1) bound */
+  int64_t pairs_lb2;      /* pairs passing the O(length) bound */
   int64_t pairs_refined;  /* pairs that reached the exact DP / distance */
   int64_t cells;          /* DP cells (or point pairs) actually computed */
   int64_t cells_unpruned; /* DP cells (or point pairs) of all pairs, in band */
