@@ -267,3 +267,16 @@ def band_cells(ctx: Context, db: Database, qpts_ptr: int, qoff_ptr: int, nq: int
     check(ctx.L.tsim_band_cells(ctx.h, C.byref(p), C.c_void_p(qpts_ptr), C.c_void_p(qoff_ptr), nq,
                                 db.h, C.byref(v)))
     return v.value
+
+
+def dp_pairs(ctx: Context, measure: str, precision: int, kernel: int, qpts_ptr: int, qoff_ptr: int,
+             max_qlen: int, cpts_ptr: int, coff_ptr: int, max_clen: int, pairs_ptr: int,
+             npairs: int, out32_ptr: int = 0, out64_ptr: int = 0, **kw):
+    """DP values of explicit (query, candidate) pairs on the device
+    (tsim_dp_pairs): precision 0 FP32, 1 compensated, 2 FP64; kernel 0 auto,
+    1 round-striped, 2 anti-diagonal."""
+    p = make_params(measure, 1, **kw)
+    check(ctx.L.tsim_dp_pairs(ctx.h, C.byref(p), precision, kernel, C.c_void_p(qpts_ptr),
+                              C.c_void_p(qoff_ptr), max_qlen, C.c_void_p(cpts_ptr),
+                              C.c_void_p(coff_ptr), max_clen, C.c_void_p(pairs_ptr), npairs,
+                              C.c_void_p(out32_ptr), C.c_void_p(out64_ptr)))

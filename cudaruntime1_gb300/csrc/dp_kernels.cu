@@ -19,231 +19,11 @@
 // lcss_refine_kernel_m_1 (lcss.cu:46-111), frechet_refine_kernel_m
 // (frechet.cu:44-117): one CTA per pair, one barrier per anti-diagonal, every
 // point re-read from global memory per cell.
-#include "dfloat.cuh"
-#include "tsim_internal.cuh"
+#include "dp_policies.cuh"
 
 namespace tsim {
 namespace {
-
-// ---- cell policies ---------------------------------------------------------
-// V: value type; border(): value outside the matrix / band; origin(): D(-1,-1);
-// masked(left): value of a cell outside its row's band.
-
-struct PolDtwRef {  // CudaRuntime1/dtw.cpp:88-93 arithmetic, bit for bit
-  using V = float;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return TSIM_INF; }
-  __device__ static V origin() { return 0.0f; }
-  __device__ static V masked(V) { return TSIM_INF; }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    float dx = qx - cx, dy = qy - cy;
-    float c = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
-    return __fadd_rn(c, fminf(fminf(up, lf), dg));
-  }
-};
-
-struct PolFrechetRef {  // CudaRuntime1/frechet.cpp:72-76, 103-108
-  using V = float;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return TSIM_INF; }
-  __device__ static V origin() { return 0.0f; }
-  __device__ static V masked(V) { return TSIM_INF; }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    float dx = qx - cx, dy = qy - cy;
-    float d = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
-    return fmaxf(d, fminf(fminf(up, lf), dg));
-  }
-};
-
-struct PolDtwSq {  // squared cost; FMA allowed, error bounded by the caller
-  using V = float;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return TSIM_INF; }
-  __device__ static V origin() { return 0.0f; }
-  __device__ static V masked(V) { return TSIM_INF; }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    float dx = qx - cx, dy = qy - cy;
-    float c = fmaf(dy, dy, dx * dx);
-    return c + fminf(fminf(up, lf), dg);
-  }
-};
-
-struct PolDtwEu {
-  using V = float;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return TSIM_INF; }
-  __device__ static V origin() { return 0.0f; }
-  __device__ static V masked(V) { return TSIM_INF; }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    float dx = qx - cx, dy = qy - cy;
-    float c = sqrtf(fmaf(dy, dy, dx * dx));
-    return c + fminf(fminf(up, lf), dg);
-  }
-};
-
-struct PolFrechetSq {  // squared domain; sqrt is applied once at the end
-  using V = float;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return TSIM_INF; }
-  __device__ static V origin() { return 0.0f; }
-  __device__ static V masked(V) { return TSIM_INF; }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    float dx = qx - cx, dy = qy - cy;
-    float d2 = fmaf(dy, dy, dx * dx);
-    return fmaxf(d2, fminf(fminf(up, lf), dg));
-  }
-};
-
-// FP64 re-score policies: the arithmetic of the FP64 oracle
-// (oracle/oracle.c dtw64_core / orc_frechet64), so values are bit-identical
-// to it: dx = (double)a - (double)b, cost = dx*dx + dy*dy without FMA.
-__device__ __forceinline__ double d2_64(float qx, float qy, float cx, float cy) {
-  double dx = (double)qx - (double)cx, dy = (double)qy - (double)cy;
-  return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-}
-__device__ __forceinline__ double dmin(double a, double b) { return b < a ? b : a; }
-
-struct PolDtwSq64 {
-  using V = double;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return __longlong_as_double(0x7ff0000000000000ll); }
-  __device__ static V origin() { return 0.0; }
-  __device__ static V masked(V) { return border(); }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    return __dadd_rn(d2_64(qx, qy, cx, cy), dmin(dmin(up, lf), dg));
-  }
-};
-
-struct PolDtwEu64 {
-  using V = double;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return __longlong_as_double(0x7ff0000000000000ll); }
-  __device__ static V origin() { return 0.0; }
-  __device__ static V masked(V) { return border(); }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    return __dadd_rn(__dsqrt_rn(d2_64(qx, qy, cx, cy)), dmin(dmin(up, lf), dg));
-  }
-};
-
-struct PolFrechetSq64 {
-  using V = double;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return __longlong_as_double(0x7ff0000000000000ll); }
-  __device__ static V origin() { return 0.0; }
-  __device__ static V masked(V) { return border(); }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    double d = d2_64(qx, qy, cx, cy), mn = dmin(dmin(up, lf), dg);
-    return d > mn ? d : mn;
-  }
-};
-
-// Compensated FP32 re-score policies: values are (hi, lo) pairs (dfloat.cuh).
-struct PolDtwSqC {
-  using V = df;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return df_inf(); }
-  __device__ static V origin() { return df{0.0f, 0.0f}; }
-  __device__ static V masked(V) { return df_inf(); }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    const df m = df_min(df_min(up, lf), dg);
-    if (!(m.hi < TSIM_INF)) return df_inf();
-    return df_add(df_sqdist(qx, qy, cx, cy), m);
-  }
-};
-
-struct PolDtwEuC {
-  using V = df;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return df_inf(); }
-  __device__ static V origin() { return df{0.0f, 0.0f}; }
-  __device__ static V masked(V) { return df_inf(); }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    const df m = df_min(df_min(up, lf), dg);
-    if (!(m.hi < TSIM_INF)) return df_inf();
-    return df_add(df_sqrt(df_sqdist(qx, qy, cx, cy)), m);
-  }
-};
-
-struct PolFrechetSqC {
-  using V = df;
-  static constexpr bool kMin = true;
-  __device__ static V border() { return df_inf(); }
-  __device__ static V origin() { return df{0.0f, 0.0f}; }
-  __device__ static V masked(V) { return df_inf(); }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    return df_max(df_sqdist(qx, qy, cx, cy), df_min(df_min(up, lf), dg));
-  }
-};
-
-// LCSS: match iff |q.x-c.x| < eps and |q.y-c.y| < eps in FP32 (lcss.cpp:93-96).
-// Outside the index window a cell keeps its row's last in-window value (the
-// true LCSS value there); left of the window it stays 0.  The non-match case
-// takes max(up, left, diag), which equals max(up, left) inside the matrix and
-// is exact at the window edges where a neighbour lies outside.
-struct PolLcss {
-  using V = int;
-  static constexpr bool kMin = false;
-  __device__ static V border() { return 0; }
-  __device__ static V origin() { return 0; }
-  __device__ static V masked(V lf) { return lf; }
-  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float eps) {
-    bool match = (fabsf(qx - cx) < eps) && (fabsf(qy - cy) < eps);
-    return match ? dg + 1 : max(max(up, lf), dg);
-  }
-};
-
-// Row whose last in-band value is the pair's result: (n-1, m-1) for DTW and
-// Frechet.  For windowed LCSS with n-1 > m-1+delta the last row is empty and
-// L(n-1, m-1) = L(m-1+delta, m-1), which the row m-1+delta holds.
-template <class P>
-__device__ __forceinline__ int result_row(int n, int m, int delta) {
-  return n - 1;
-}
-template <>
-__device__ __forceinline__ int result_row<PolLcss>(int n, int m, int delta) {
-  return delta >= 0 ? min(n - 1, m - 1 + delta) : n - 1;
-}
-
-template <class P>
-struct RowBand {
-  __device__ static void get(int i, int n, int m, int w, int delta, int& lo, int& hi);
-};
-template <class P>
-__device__ void RowBand<P>::get(int i, int n, int m, int w, int, int& lo, int& hi) {
-  band_row(i, n, m, w, lo, hi);
-}
-template <>
-__device__ void RowBand<PolLcss>::get(int i, int, int m, int, int delta, int& lo, int& hi) {
-  window_row(i, m, delta, lo, hi);
-}
-
-__device__ __forceinline__ void store_result(const DpArgs& a, int pid, float v) { a.out[pid] = v; }
-__device__ __forceinline__ void store_result(const DpArgs& a, int pid, int v) { a.out[pid] = (float)v; }
-__device__ __forceinline__ void store_result(const DpArgs& a, int pid, double v) { a.out64[pid] = v; }
-__device__ __forceinline__ void store_result(const DpArgs& a, int pid, df v) {
-  a.out64[pid] = v.hi < TSIM_INF ? df_to_double(v) : __longlong_as_double(0x7ff0000000000000ll);
-}
-__device__ __forceinline__ float vf(float v) { return v; }
-__device__ __forceinline__ float vf(int v) { return (float)v; }
-__device__ __forceinline__ float vf(double v) { return (float)v; }
-__device__ __forceinline__ float vf(df v) { return v.hi; }
-
-template <class V>
-__device__ __forceinline__ V shfl_up_seg(V v, int G) {
-  return __shfl_up_sync(0xffffffffu, v, 1, G);
-}
-__device__ __forceinline__ df shfl_up_seg(df v, int G) {
-  return df{__shfl_up_sync(0xffffffffu, v.hi, 1, G), __shfl_up_sync(0xffffffffu, v.lo, 1, G)};
-}
-
-__device__ __forceinline__ float seg_max(float v, int G) {
-  for (int o = G >> 1; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o, G));
-  return v;
-}
-__device__ __forceinline__ int seg_max_i(int v, int G) {
-  for (int o = G >> 1; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o, G));
-  return v;
-}
+using namespace dp;
 
 constexpr int kDpThreads = 128;
 constexpr int kNoColumn = 1 << 30;

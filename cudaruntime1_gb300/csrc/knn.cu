@@ -93,6 +93,9 @@ struct KArgs {
   float* thr2;              // [nq]  threshold after round 1
   int* fcnt;                // [nq]  round-2 pairs per query (in list1)
   const float4* csegbox;    // [C*kSegs] candidate segment boxes
+  int* spill;               // pairs the anti-diagonal kernel leaves to the striped one
+  int* nspill;
+  int rdiag;                // rows per lane-group of the anti-diagonal kernel (0: off)
   float4* qtab;             // [nq*tstride] query sparse tables (global memory)
   int tstride;
   int* off2;                // [nq+1]
@@ -927,10 +930,25 @@ __global__ void clear_u32_kernel(unsigned* p, size_t n) {
     p[i] = 0;
 }
 
+// DP of a pair list: the anti-diagonal kernel for the pairs it can take,
+// the round-striped kernel (G lanes x R rows) for the rest
+int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& d) {
+  const bool diag_kind = kind == DP_DTW_SQ || kind == DP_DTW_EU || kind == DP_LCSS ||
+                         kind == DP_FRECHET_SQ || kind == DP_DTW_SQC || kind == DP_DTW_EUC ||
+                         kind == DP_FRECHET_SQC;
+  if (!diag_kind || a.rdiag == 0) return launch_dp(ctx, kind, G, R, d, a.max_clen);
+  TSIM_CUDA(cudaMemsetAsync(a.nspill, 0, sizeof(int), ctx->stream));
+  TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag, d, a.max_qlen, a.spill, a.nspill));
+  DpArgs sp = d;
+  sp.order = a.spill;
+  sp.npairs_dev = a.nspill;
+  return launch_dp(ctx, kind, G, R, sp, a.max_clen);
+}
+
 // the FP32 refine of a pair list: wavefront DP or a pairwise kernel
 template <int MEAS>
-int refine32(tsim_ctx* ctx, int dp32, int G, int R, const DpArgs& d, int max_clen) {
-  if (is_dp(MEAS)) return launch_dp(ctx, dp32, G, R, d, max_clen);
+int refine32(tsim_ctx* ctx, const KArgs& a, int dp32, int G, int R, const DpArgs& d) {
+  if (is_dp(MEAS)) return run_dp(ctx, a, dp32, G, R, d);
   PwArgs p{d.qpts, d.qoff, d.cpts, d.coff, d.pairs, d.npairs, d.npairs_dev, d.order, d.out,
            nullptr, d.thr};
   return launch_pairwise(ctx, MEAS == M_HAUSDORFF ? TSIM_HAUSDORFF : TSIM_EUCLIDEAN, p);
@@ -984,10 +1002,10 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
       one.pairs = a.seeds + i;
       one.npairs = 1;
       one.out = a.seed_vals + i;
-      TSIM_TRY(refine32<MEAS>(ctx, dp32, Gs, Rs, one, a.max_clen));
+      TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, one));
     }
   } else {
-    TSIM_TRY(refine32<MEAS>(ctx, dp32, Gs, Rs, d, a.max_clen));
+    TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, d));
   }
   stage_end(ctx);
 
@@ -1024,10 +1042,10 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
         one.pairs = a.r1pairs + i;
         one.npairs = 1;
         one.out = a.r1vals + i;
-        TSIM_TRY(refine32<MEAS>(ctx, dp32, Gs, Rs, one, a.max_clen));
+        TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, one));
       }
     } else {
-      TSIM_TRY(refine32<MEAS>(ctx, dp32, Gs, Rs, r1, a.max_clen));
+      TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, r1));
     }
   }
   stage_end(ctx);
@@ -1064,10 +1082,10 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
       one.npairs_dev = nullptr;
       one.order = nullptr;
       one.out = a.flat_vals + i;
-      TSIM_TRY(refine32<MEAS>(ctx, dp32, Gs, Rs, one, a.max_clen));
+      TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, one));
     }
   } else {
-    TSIM_TRY(refine32<MEAS>(ctx, dp32, G, R, d, a.max_clen));
+    TSIM_TRY(refine32<MEAS>(ctx, a, dp32, G, R, d));
   }
   stage_end(ctx);
 
@@ -1090,7 +1108,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
     r.delta = -1;
     // compensated FP32 re-score of the set, then FP64 only for the pairs it
     // cannot order (near-ties within the compensated error bound)
-    if (is_dp(MEAS)) TSIM_TRY(launch_dp(ctx, dpc, 32, 1, r, a.max_clen));
+    if (is_dp(MEAS)) TSIM_TRY(run_dp(ctx, a, dpc, 32, 1, r));
     cluster_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
     r.pairs = a.r64pairs;
     r.out64 = a.r64;
@@ -1211,6 +1229,20 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.T = std::min(kChunk, std::max(1, (2 * a.S + a.nch - 1) / a.nch));
   a.T = std::min(a.T, 64);
   a.plain = (p->flags & TSIM_FLAG_PLAIN) ? 1 : 0;
+  {
+    // rows per lane-group of the anti-diagonal kernel: the smallest R whose
+    // validity condition holds for the longest pair shape (n = m is the worst)
+    const int L = std::max(max_qlen, db->max_len);
+    const int wd = p->measure == TSIM_LCSS ? p->delta
+                                           : (p->measure == TSIM_DTW ? band_w(L, L, p->band_pct) : -1);
+    a.rdiag = 0;
+    for (int R : {1, 2, 4})
+      if (diag_ok(p->measure == TSIM_LCSS, L, L, wd, R)) {
+        a.rdiag = R;
+        break;
+      }
+    if (a.plain || (p->flags & TSIM_FLAG_NO_PRUNE)) a.rdiag = 0;
+  }
   a.cost = p->cost;
   a.band_pct = p->band_pct;
   a.delta = p->delta;
@@ -1237,7 +1269,8 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
                 align256(sizeof(int) * nqC) + align256(sizeof(int) * kNumShapes) + 256 +
                 align256(sizeof(float) * nqC) + align256(sizeof(int2) * nq * a.M) +
                 align256(sizeof(float) * nq * a.M) + 2 * align256(sizeof(float) * (nq + 1)) +
-                align256(sizeof(float4) * (size_t)nq * a.tstride);
+                align256(sizeof(float4) * (size_t)nq * a.tstride) +
+                align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 256;
   TSIM_TRY(arena_reserve(ctx, need));
   float4* qbox = arena_take<float4>(ctx, nq);
   float4* qends = arena_take<float4>(ctx, nq);
@@ -1272,6 +1305,8 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.thr2 = arena_take<float>(ctx, nq + 1);
   a.fcnt = arena_take<int>(ctx, nq + 1);
   a.qtab = arena_take<float4>(ctx, (size_t)nq * a.tstride);
+  a.spill = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
+  a.nspill = arena_take<int>(ctx, 4);
   a.csegbox = db->segbox;
   a.order = arena_take<int>(ctx, nqC);
   a.shape_cnt = arena_take<int>(ctx, kNumShapes);
@@ -1405,4 +1440,67 @@ extern "C" int tsim_band_cells(tsim_ctx* ctx, const tsim_params* p, const tsim_p
   TSIM_TRY(tsim::arena_reserve(ctx, tsim::align256(sizeof(float4) * nq) * 2 +
                                         tsim::align256(sizeof(int) * nq) + 256));
   return tsim::band_cells(ctx, p, (const float2*)d_qpts, d_qoff, nq, db, cells);
+}
+
+extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision, int kernel,
+                             const tsim_point* d_qpts, const int64_t* d_qoff, int max_qlen,
+                             const tsim_point* d_cpts, const int64_t* d_coff, int max_clen,
+                             const int* d_pairs, int npairs, float* d_out32, double* d_out64) {
+  using namespace tsim;
+  TSIM_CHECK_ARG(ctx && p && d_qpts && d_qoff && d_cpts && d_coff && d_pairs, "NULL argument");
+  TSIM_CHECK_ARG(npairs >= 0 && max_qlen >= 1 && max_clen >= 1, "bad sizes");
+  TSIM_CHECK_ARG(precision >= 0 && precision <= 2 && kernel >= 0 && kernel <= 2, "bad mode");
+  TSIM_CHECK_ARG(precision == 0 ? d_out32 != nullptr : d_out64 != nullptr, "NULL output");
+  int kinds[3];
+  if (p->measure == TSIM_DTW) {
+    kinds[0] = p->cost ? DP_DTW_EU : DP_DTW_SQ;
+    kinds[1] = p->cost ? DP_DTW_EUC : DP_DTW_SQC;
+    kinds[2] = p->cost ? DP_DTW_EU64 : DP_DTW_SQ64;
+  } else if (p->measure == TSIM_FRECHET) {
+    kinds[0] = DP_FRECHET_SQ;
+    kinds[1] = DP_FRECHET_SQC;
+    kinds[2] = DP_FRECHET_SQ64;
+  } else if (p->measure == TSIM_LCSS) {
+    TSIM_CHECK_ARG(precision == 0, "LCSS counts are exact: precision must be 0");
+    kinds[0] = kinds[1] = kinds[2] = DP_LCSS;
+  } else {
+    return fail(TSIM_ERR_INVALID_ARG, "tsim_dp_pairs: measure must be DTW, LCSS or Frechet");
+  }
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  if (npairs == 0) return TSIM_OK;
+  const int kind = kinds[precision];
+  DpArgs d{};
+  d.qpts = reinterpret_cast<const float2*>(d_qpts);
+  d.qoff = d_qoff;
+  d.cpts = reinterpret_cast<const float2*>(d_cpts);
+  d.coff = d_coff;
+  d.pairs = reinterpret_cast<const int2*>(d_pairs);
+  d.npairs = npairs;
+  d.out = d_out32;
+  d.out64 = d_out64;
+  d.band_pct = p->measure == TSIM_DTW ? p->band_pct : -1;
+  d.delta = p->delta;
+  d.eps = p->epsilon;
+  const int L = std::max(max_qlen, max_clen);
+  const int wd = p->measure == TSIM_LCSS ? p->delta : band_w(L, L, d.band_pct);
+  int Rd = 0;
+  for (int R : {1, 2, 4})
+    if (diag_ok(p->measure == TSIM_LCSS, L, L, wd, R)) {
+      Rd = R;
+      break;
+    }
+  int G, R;
+  dp_shape(kind, max_qlen, max_clen, wd, G, R);
+  const bool diag_kind = precision < 2;
+  if (kernel == 1 || (kernel == 0 && (!diag_kind || Rd == 0)) || !diag_kind)
+    return launch_dp(ctx, kind, G, R, d, max_clen);
+  if (Rd == 0) Rd = 4;  // forced: every pair spills to the striped kernel
+  TSIM_TRY(arena_reserve(ctx, align256(sizeof(int) * (size_t)npairs) + 256));
+  int* spill = arena_take<int>(ctx, npairs);
+  int* nspill = arena_take<int>(ctx, 4);
+  TSIM_CUDA(cudaMemsetAsync(nspill, 0, sizeof(int), ctx->stream));
+  TSIM_TRY(launch_dp_diag(ctx, kind, Rd, d, max_qlen, spill, nspill));
+  d.order = spill;
+  d.npairs_dev = nspill;
+  return launch_dp(ctx, kind, G, R, d, max_clen);
 }

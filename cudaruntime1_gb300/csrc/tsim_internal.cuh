@@ -247,6 +247,13 @@ int launch_pairwise64(tsim_ctx* ctx, int measure, const PwArgs& a);
 
 // G lanes per pair (4, 8, 16 or 32), R rows per lane (1, 2, 4 or 8).
 int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a, int max_m);
+// Anti-diagonal kernel (dp_diag.cu) for DTW/LCSS/Frechet FP32 and compensated
+// kinds, R rows per lane-group (1, 2 or 4); pairs it cannot take are appended
+// to spill[] (count in *nspill) for launch_dp.  max_n bounds the query length.
+int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_n, int* spill,
+                   int* nspill);
+bool diag_ok(bool lcss, int n, int m, int wd, int R);
+
 // choose (G, R) for pairs of shape n x m under band w
 void dp_shape(int kind, int n, int m, int band_w_or_delta, int& G, int& R);
 

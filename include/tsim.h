@@ -167,6 +167,17 @@ TSIM_API int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_point
                            const int64_t* h_qoff, int nq, tsim_db* db, int* h_ids,
                            float* h_dists, tsim_stats* stats);
 
+/* Values of given (query, candidate) pairs -- d_pairs[2*i] = query index,
+ * d_pairs[2*i+1] = candidate index -- for DTW, LCSS or Frechet under p's
+ * band / window / cost.  precision: 0 = FP32 (d_out32), 1 = compensated FP32
+ * (d_out64), 2 = FP64 (d_out64).  kernel: 0 = automatic, 1 = round-striped
+ * DP, 2 = anti-diagonal DP (pairs it cannot take fall back to 1).  Frechet
+ * values are squared distances; LCSS values are match counts. */
+TSIM_API int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision, int kernel,
+                           const tsim_point* d_qpts, const int64_t* d_qoff, int max_qlen,
+                           const tsim_point* d_cpts, const int64_t* d_coff, int max_clen,
+                           const int* d_pairs, int npairs, float* d_out32, double* d_out64);
+
 /* ---- reference-semantics batch calls (device pointers) -------------------- */
 /* DTW (Euclidean cell cost), LCSS (count/min(n,m)), Frechet: num_t queries of
  * length n against num_t candidates of length m, out[num_t].  The r=5
