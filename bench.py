@@ -64,7 +64,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "25"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -166,7 +166,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -242,7 +242,10 @@ def main():
                           "launches": launches}))
         return
 
-    # ---- per-stage device times (CUDA events on the launching stream)
+    # ---- per-stage device times (CUDA events on the launching stream); the
+    # chunks of a request overlap on child streams in the timed region, so
+    # per-kernel durations are taken with one stream
+    ctx.set_concurrency(1)
     ctx.set_profiling(True)
     prof_steps = 5
     for _ in range(prof_steps):
@@ -250,6 +253,7 @@ def main():
         step()
     prof = ctx.counters(reset=True)
     ctx.set_profiling(False)
+    ctx.set_concurrency(4)
     stage_ms = {s: v / prof_steps for s, v in prof["stage_ms"].items() if v > 0}
     dp_cells = prof["dp_cells"] / prof_steps
     dp_launch_ms = stage_ms.get("dp", 0.0) / max(1, prof["stage_calls"]["dp"] / prof_steps)

@@ -97,6 +97,7 @@ def load(build_if_missing: bool = False):
             "tsim_ctx_counters": ([_vp, C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int], C.c_int),
             "tsim_probe_fp32_tflops": ([_vp, C.POINTER(C.c_double)], C.c_int),
+            "tsim_ctx_set_concurrency": ([_vp, C.c_int], C.c_int),
             "tsim_band_cells": ([_vp, C.POINTER(TsimParams), _vp, _vp, C.c_int, _vp,
                                  C.POINTER(C.c_int64)], C.c_int),
             "tsim_dp_pairs": ([_vp, C.POINTER(TsimParams), C.c_int, C.c_int, _vp, _vp, C.c_int,

@@ -160,6 +160,10 @@ class Context:
                 "stage_calls": {s: calls[i] for i, s in enumerate(_lib.STAGES)},
                 "launches": launches.value, "dp_cells": cells.value}
 
+    def set_concurrency(self, streams: int):
+        """Streams one kNN request may use (chunks of queries overlap)."""
+        check(self.L.tsim_ctx_set_concurrency(self.h, streams))
+
     def probe_fp32_tflops(self) -> float:
         v = C.c_double()
         check(self.L.tsim_probe_fp32_tflops(self.h, C.byref(v)))

@@ -196,22 +196,77 @@ extern "C" int tsim_ctx_set_profiling(tsim_ctx* ctx, int on) {
   TSIM_CHECK_ARG(ctx != nullptr, "ctx is NULL");
   if (!on) TSIM_TRY(stage_collect(ctx));
   ctx->profiling = on != 0;
+  for (tsim_ctx* s : ctx->subs) {
+    if (!on) TSIM_TRY(stage_collect(s));
+    s->profiling = on != 0;
+  }
   return TSIM_OK;
 }
+
+extern "C" int tsim_ctx_set_concurrency(tsim_ctx* ctx, int streams) {
+  TSIM_CHECK_ARG(ctx != nullptr, "ctx is NULL");
+  TSIM_CHECK_ARG(streams >= 1 && streams <= 16, "streams must be in 1..16");
+  ctx->concurrency = streams;
+  return TSIM_OK;
+}
+
+namespace tsim {
+
+// child contexts for concurrent chunks (created on first use)
+int ensure_subs(tsim_ctx* ctx, int n) {
+  if (!ctx->fork_ev) TSIM_CUDA(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
+  while ((int)ctx->subs.size() < n) {
+    tsim_ctx* s = nullptr;
+    TSIM_TRY(tsim_ctx_create(ctx->device, nullptr, &s));
+    s->concurrency = 1;
+    s->profiling = ctx->profiling;
+    ctx->subs.push_back(s);
+    cudaEvent_t ev;
+    TSIM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    ctx->join_ev.push_back(ev);
+  }
+  return TSIM_OK;
+}
+
+}  // namespace tsim
 
 extern "C" int tsim_ctx_counters(tsim_ctx* ctx, double* ms, int64_t* calls, int64_t* launches,
                                  int64_t* dp_cells, int reset) {
   TSIM_CHECK_ARG(ctx != nullptr, "ctx is NULL");
-  TSIM_TRY(stage_collect(ctx));
-  TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
-  for (int s = 0; s < TSIM_STAGE_COUNT; ++s) {
-    if (ms) ms[s] = ctx->stage_ms[s];
-    if (calls) calls[s] = ctx->stage_calls[s];
+  double ms_acc[TSIM_STAGE_COUNT] = {};
+  int64_t calls_acc[TSIM_STAGE_COUNT] = {};
+  int64_t launches_acc = 0;
+  unsigned long long cells_acc = 0;
+  std::vector<tsim_ctx*> all{ctx};
+  all.insert(all.end(), ctx->subs.begin(), ctx->subs.end());
+  for (tsim_ctx* c : all) {  // the context and its child streams
+    TSIM_TRY(stage_collect(c));
+    TSIM_CUDA(cudaStreamSynchronize(c->stream));
+    for (int s = 0; s < TSIM_STAGE_COUNT; ++s) {
+      ms_acc[s] += c->stage_ms[s];
+      calls_acc[s] += c->stage_calls[s];
+    }
+    launches_acc += c->launches;
+    unsigned long long cells = 0;
+    TSIM_CUDA(cudaMemcpy(&cells, c->dcounters, sizeof(cells), cudaMemcpyDeviceToHost));
+    cells_acc += cells;
   }
-  if (launches) *launches = ctx->launches;
-  unsigned long long cells = 0;
-  TSIM_CUDA(cudaMemcpy(&cells, ctx->dcounters, sizeof(cells), cudaMemcpyDeviceToHost));
-  if (dp_cells) *dp_cells = (int64_t)cells;
+  for (int s = 0; s < TSIM_STAGE_COUNT; ++s) {
+    if (ms) ms[s] = ms_acc[s];
+    if (calls) calls[s] = calls_acc[s];
+  }
+  if (launches) *launches = launches_acc;
+  if (dp_cells) *dp_cells = (int64_t)cells_acc;
+  if (reset)
+    for (tsim_ctx* c : ctx->subs) {
+      for (int s = 0; s < TSIM_STAGE_COUNT; ++s) {
+        c->stage_ms[s] = 0.0;
+        c->stage_calls[s] = 0;
+      }
+      c->launches = 0;
+      TSIM_CUDA(cudaMemsetAsync(c->dcounters, 0, 64, c->stream));
+      TSIM_CUDA(cudaStreamSynchronize(c->stream));
+    }
   if (reset) {
     for (int s = 0; s < TSIM_STAGE_COUNT; ++s) {
       ctx->stage_ms[s] = 0.0;
@@ -306,6 +361,11 @@ int tsim_ctx_destroy(tsim_ctx* c) {
   if (!c) return TSIM_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  for (tsim_ctx* s : c->subs) tsim_ctx_destroy(s);
+  c->subs.clear();
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  for (auto ev : c->join_ev) cudaEventDestroy(ev);
+  c->join_ev.clear();
   for (tsim_db* db : c->dbs) {  // detach: free device memory, keep the handle
     db_free(db);
     db->ctx = nullptr;

@@ -3,10 +3,9 @@
 //
 // Error-free transformations: TwoSum (Knuth), Fast2Sum (Dekker, |a| >= |b|)
 // and the FMA product error.  A DP value carried as (hi, lo) accumulates its
-// rounding errors in lo, so a DTW path of P cells stays within about
-// (4P + 16) u^2 (u = 2^-24) of the exact value instead of P u: the re-score
-// reaches double-float accuracy on the FP32 pipes, which on this GPU issue
-// far faster than FP64.
+// rounding errors in lo, so the sum along a DTW path of P cells adds only
+// O(P u^2) (u = 2^-24) to the error of its terms instead of P u; the FP32
+// pipes issue these far faster than FP64 on this GPU.
 #pragma once
 #include "tsim_internal.cuh"
 
@@ -54,6 +53,13 @@ __device__ __forceinline__ df df_add(df a, df b) {
   float s, e;
   two_sum_f(a.hi, b.hi, s, e);
   return fast_two_sum_f(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+
+// c + b for a float c >= 0 and a normalised, finite, non-negative pair b
+__device__ __forceinline__ df df_add1(float c, df b) {
+  float s, e;
+  two_sum_f(c, b.hi, s, e);
+  return fast_two_sum_f(s, __fadd_rn(e, b.lo));
 }
 
 // sqrt of a normalised non-negative pair: one Newton correction of sqrtf(hi)

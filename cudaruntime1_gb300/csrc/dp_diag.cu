@@ -43,14 +43,16 @@ __host__ __device__ bool diag_ok(bool lcss, int n, int m, int wd, int R) {
 namespace {
 
 template <class P, int R>
-__global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row_cap, int* spill,
-                                                                int* nspill) {
+__global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row_cap, int col_cap,
+                                                                int* spill, int* nspill) {
   using V = typename P::V;
   extern __shared__ __align__(16) float4 diag_rows[];
   constexpr bool kLcss = !P::kMin;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float4* rt = diag_rows + (size_t)wib * row_cap;
+  // per warp: the row table, then the candidate's points
+  float4* rt = diag_rows + (size_t)wib * (row_cap + col_cap / 2);
+  float2* cs = reinterpret_cast<float2*>(rt + row_cap);
   const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
   const int nw = gridDim.x * (blockDim.x >> 5);
   const int npairs = a.npairs_dev ? min(*a.npairs_dev, a.npairs) : a.npairs;
@@ -67,7 +69,7 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
     const int w = band_w(n, m, a.band_pct);
     const int wd = kLcss ? a.delta : w;
     const int nr = (n + 32 * R - 1) / (32 * R) * (32 * R);  // rows incl. padding
-    if (!diag_ok(kLcss, n, m, wd, R) || nr > row_cap) {
+    if (!diag_ok(kLcss, n, m, wd, R) || nr > row_cap || m > col_cap) {
       if (lane == 0 && spill) spill[atomicAdd(nspill, 1)] = pid;
       continue;
     }
@@ -92,6 +94,7 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
       }
       rt[i] = e;
     }
+    for (int j = lane; j < m; j += 32) cs[j] = B[j];  // the candidate, read once
     __syncwarp();
 
     int i0 = R * lane;  // first row of the lane's current group
@@ -119,7 +122,7 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
     V prev_raw = P::border();  // the shuffled value of the previous step
     float2 cw[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) cw[r] = B[0];
+    for (int r = 0; r < R; ++r) cw[r] = cs[0];
     V result = P::border();
     bool holds = false;
     bool alive = true;
@@ -158,7 +161,7 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
 #pragma unroll
       for (int r = R - 1; r > 0; --r) cw[r] = cw[r - 1];
       const int j0 = t - i0;
-      cw[0] = __ldg(B + min(max(j0, 0), m - 1));
+      cw[0] = cs[min(max(j0, 0), m - 1)];
       float mstep = TSIM_INF;
       // row r computes column j0 - r: its up neighbour is row r-1 one step
       // ago and its diagonal neighbour row r-1 two steps ago, so rows are
@@ -219,12 +222,14 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
 }
 
 template <class P, int R>
-int launch_diag_one(tsim_ctx* ctx, const DpArgs& a, int max_n, int* spill, int* nspill) {
+int launch_diag_one(tsim_ctx* ctx, const DpArgs& a, int max_n, int max_m, int* spill,
+                    int* nspill) {
   if (a.npairs <= 0) return TSIM_OK;
   const int row_cap = (max_n + 32 * R - 1) / (32 * R) * (32 * R);
+  const int col_cap = (max_m + 1) & ~1;  // even: whole float4 slots
   const int warps = kDiagThreads / 32;
-  const size_t smem = (size_t)warps * row_cap * sizeof(float4);
-  if (smem > 200 * 1024) return fail(TSIM_ERR_UNSUPPORTED, "query too long for the row table");
+  const size_t smem = (size_t)warps * (row_cap + col_cap / 2) * sizeof(float4);
+  if (smem > 200 * 1024) return fail(TSIM_ERR_UNSUPPORTED, "pair too long for the row tables");
   auto kern = dp_diag_kernel<P, R>;
   if (smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -232,34 +237,35 @@ int launch_diag_one(tsim_ctx* ctx, const DpArgs& a, int max_n, int* spill, int* 
   TSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kDiagThreads, smem));
   long long blocks = std::min<long long>((a.npairs + warps - 1) / warps,
                                          (long long)std::max(per_sm, 1) * ctx->num_sms);
-  kern<<<(unsigned)std::max(blocks, 1ll), kDiagThreads, smem, ctx->stream>>>(a, row_cap, spill,
-                                                                            nspill);
+  kern<<<(unsigned)std::max(blocks, 1ll), kDiagThreads, smem, ctx->stream>>>(a, row_cap, col_cap,
+                                                                            spill, nspill);
   TSIM_CUDA(cudaGetLastError());
   launched(ctx);
   return TSIM_OK;
 }
 
 template <class P>
-int launch_diag_r(tsim_ctx* ctx, int R, const DpArgs& a, int max_n, int* spill, int* nspill) {
+int launch_diag_r(tsim_ctx* ctx, int R, const DpArgs& a, int max_n, int max_m, int* spill,
+                  int* nspill) {
   switch (R) {
-    case 1: return launch_diag_one<P, 1>(ctx, a, max_n, spill, nspill);
-    case 2: return launch_diag_one<P, 2>(ctx, a, max_n, spill, nspill);
-    default: return launch_diag_one<P, 4>(ctx, a, max_n, spill, nspill);
+    case 1: return launch_diag_one<P, 1>(ctx, a, max_n, max_m, spill, nspill);
+    case 2: return launch_diag_one<P, 2>(ctx, a, max_n, max_m, spill, nspill);
+    default: return launch_diag_one<P, 4>(ctx, a, max_n, max_m, spill, nspill);
   }
 }
 
 }  // namespace
 
-int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_n, int* spill,
-                   int* nspill) {
+int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_n, int max_m,
+                   int* spill, int* nspill) {
   switch (kind) {
-    case DP_DTW_SQ: return launch_diag_r<PolDtwSq>(ctx, R, a, max_n, spill, nspill);
-    case DP_DTW_EU: return launch_diag_r<PolDtwEu>(ctx, R, a, max_n, spill, nspill);
-    case DP_LCSS: return launch_diag_r<PolLcss>(ctx, R, a, max_n, spill, nspill);
-    case DP_FRECHET_SQ: return launch_diag_r<PolFrechetSq>(ctx, R, a, max_n, spill, nspill);
-    case DP_DTW_SQC: return launch_diag_r<PolDtwSqC>(ctx, R, a, max_n, spill, nspill);
-    case DP_DTW_EUC: return launch_diag_r<PolDtwEuC>(ctx, R, a, max_n, spill, nspill);
-    case DP_FRECHET_SQC: return launch_diag_r<PolFrechetSqC>(ctx, R, a, max_n, spill, nspill);
+    case DP_DTW_SQ: return launch_diag_r<PolDtwSq>(ctx, R, a, max_n, max_m, spill, nspill);
+    case DP_DTW_EU: return launch_diag_r<PolDtwEu>(ctx, R, a, max_n, max_m, spill, nspill);
+    case DP_LCSS: return launch_diag_r<PolLcss>(ctx, R, a, max_n, max_m, spill, nspill);
+    case DP_FRECHET_SQ: return launch_diag_r<PolFrechetSq>(ctx, R, a, max_n, max_m, spill, nspill);
+    case DP_DTW_SQC: return launch_diag_r<PolDtwSqC>(ctx, R, a, max_n, max_m, spill, nspill);
+    case DP_DTW_EUC: return launch_diag_r<PolDtwEuC>(ctx, R, a, max_n, max_m, spill, nspill);
+    case DP_FRECHET_SQC: return launch_diag_r<PolFrechetSqC>(ctx, R, a, max_n, max_m, spill, nspill);
   }
   return fail(TSIM_ERR_UNSUPPORTED, "no anti-diagonal kernel for this DP kind");
 }

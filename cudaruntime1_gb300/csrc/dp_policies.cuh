@@ -120,6 +120,9 @@ struct PolFrechetSq64 {
 };
 
 // Compensated FP32 re-score policies: values are (hi, lo) pairs (dfloat.cuh).
+// DTW: each cell cost in FP32 (<= 4u relative error, one FMA), the path sum
+// compensated; the value is then within 4u + O(P u^2) of exact -- a single
+// cost's rounding, not P of them.
 struct PolDtwSqC {
   using V = df;
   static constexpr bool kMin = true;
@@ -129,7 +132,8 @@ struct PolDtwSqC {
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     const df m = df_min(df_min(up, lf), dg);
     if (!(m.hi < TSIM_INF)) return df_inf();
-    return df_add(df_sqdist(qx, qy, cx, cy), m);
+    const float dx = qx - cx, dy = qy - cy;
+    return df_add1(fmaf(dy, dy, dx * dx), m);
   }
 };
 
@@ -142,7 +146,8 @@ struct PolDtwEuC {
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     const df m = df_min(df_min(up, lf), dg);
     if (!(m.hi < TSIM_INF)) return df_inf();
-    return df_add(df_sqrt(df_sqdist(qx, qy, cx, cy)), m);
+    const float dx = qx - cx, dy = qy - cy;
+    return df_add1(sqrtf(fmaf(dy, dy, dx * dx)), m);
   }
 };
 

@@ -69,7 +69,8 @@ struct KArgs {
   int max_qlen;  // shared-memory tables are sized for this query length
   // parameters
   int k, S, T, nch;
-  int plain;  // one DP pair per kernel launch (the unbatched comparison form)
+  int plain;    // one DP pair per kernel launch (the unbatched comparison form)
+  int noprune;  // thresholds stay open: every pair is refined
   int cost;  // DTW: 0 squared, 1 Euclidean
   int band_pct;
   int delta;
@@ -232,36 +233,64 @@ __global__ void __launch_bounds__(kSelThreads) seed_kernel(KArgs a) {
   }
 }
 
-// k-th best seed value -> threshold (DTW/Frechet: widened; LCSS: count)
+// k-th smallest of the keys a warp holds (SLOTS per lane, ~0 = empty; keys
+// unique); ~0 when there are fewer than k
+template <int SLOTS>
+__device__ unsigned long long warp_kth(unsigned long long (&key)[SLOTS], int k) {
+  unsigned long long kth = ~0ull;
+  for (int e = 0; e < k; ++e) {
+    unsigned long long mn = ~0ull;
+    int slot = 0;
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s)
+      if (key[s] < mn) {
+        mn = key[s];
+        slot = s;
+      }
+    const unsigned long long g = warp_min_u64(mn);
+    if (g == ~0ull) return ~0ull;
+    if (mn == g) {
+#pragma unroll
+      for (int s = 0; s < SLOTS; ++s)
+        if (s == slot) key[s] = ~0ull;
+    }
+    kth = g;
+  }
+  return kth;
+}
+
+// k-th best seed value -> threshold (DTW/Frechet: widened; LCSS: count).
+// One warp per query.
 template <int MEAS>
 __global__ void thresh_kernel(KArgs a) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (q >= a.nq) return;
-  float v[64];
-  int cnt = 0;
-  for (int i = 0; i < a.S; ++i) {
-    if (a.seeds[(size_t)q * a.S + i].y < 0) continue;
-    float x = a.seed_vals[(size_t)q * a.S + i];
-    if (MEAS == M_LCSS) x = -x;
-    int p = cnt++;
-    while (p > 0 && v[p - 1] > x) {
-      v[p] = v[p - 1];
-      --p;
+  unsigned long long key[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    const int i = s * 32 + lane;
+    key[s] = ~0ull;
+    if (i < a.S && a.seeds[(size_t)q * a.S + i].y >= 0) {
+      const float x = a.seed_vals[(size_t)q * a.S + i];
+      key[s] = pack_key(MEAS == M_LCSS ? -x : x, i);
     }
-    v[p] = x;
   }
-  float t;
-  if (cnt < a.k) {
-    t = MEAS == M_LCSS ? 0.0f : TSIM_INF;  // not enough seeds: keep everything
-  } else if (MEAS == M_LCSS) {
-    t = -v[a.k - 1];
-  } else {
-    t = widen(v[a.k - 1], gamma_dp(MEAS, a.qlen[q], a.max_clen));
+  const unsigned long long kth = warp_kth(key, a.k);
+  if (lane == 0) {
+    float t;
+    if (kth == ~0ull) {
+      t = MEAS == M_LCSS ? 0.0f : TSIM_INF;  // not enough seeds: keep everything
+    } else {
+      const float v = ord2f((unsigned)(kth >> 32));
+      t = MEAS == M_LCSS ? -v : widen(v, gamma_dp(MEAS, a.qlen[q], a.max_clen));
+    }
+    if (a.noprune) t = MEAS == M_LCSS ? -TSIM_INF : TSIM_INF;
+    a.thr[q] = t;
+    a.cnt1[q] = 0;
+    a.cnt2[q] = 0;
+    a.rcnt[q] = 0;
   }
-  a.thr[q] = t;
-  a.cnt1[q] = 0;
-  a.cnt2[q] = 0;
-  a.rcnt[q] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -616,35 +645,43 @@ __global__ void __launch_bounds__(kSelThreads) r1_select_kernel(KArgs a) {
   }
 }
 
-// k-th best of seeds and round 1 -> tightened threshold (never looser)
+// k-th best of seeds and round 1 -> tightened threshold (never looser).
+// One warp per query.
 template <int MEAS>
 __global__ void thresh2_kernel(KArgs a) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (q >= a.nq) return;
-  float v[128];
-  int cnt = 0;
-  auto add = [&](float x) {
-    if (MEAS == M_LCSS) x = -x;
-    int p = cnt++;
-    while (p > 0 && v[p - 1] > x) {
-      v[p] = v[p - 1];
-      --p;
+  unsigned long long key[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int i = s * 32 + lane;
+    key[s] = ~0ull;
+    if (i < a.S) {
+      if (a.seeds[(size_t)q * a.S + i].y >= 0) {
+        const float x = a.seed_vals[(size_t)q * a.S + i];
+        key[s] = pack_key(MEAS == M_LCSS ? -x : x, i);
+      }
+    } else if (i < a.S + a.M) {
+      if (a.r1pairs[(size_t)q * a.M + i - a.S].y >= 0) {
+        const float x = a.r1vals[(size_t)q * a.M + i - a.S];
+        key[s] = pack_key(MEAS == M_LCSS ? -x : x, i);
+      }
     }
-    v[p] = x;
-  };
-  for (int i = 0; i < a.S; ++i)
-    if (a.seeds[(size_t)q * a.S + i].y >= 0) add(a.seed_vals[(size_t)q * a.S + i]);
-  for (int i = 0; i < a.M; ++i)
-    if (a.r1pairs[(size_t)q * a.M + i].y >= 0) add(a.r1vals[(size_t)q * a.M + i]);
-  float t = a.thr[q];
-  if (cnt >= a.k) {
-    if (MEAS == M_LCSS)
-      t = fmaxf(t, -v[a.k - 1]);
-    else
-      t = fminf(t, widen(v[a.k - 1], gamma_dp(MEAS, a.qlen[q], a.max_clen)));
   }
-  a.thr2[q] = t;
-  a.fcnt[q] = 0;
+  const unsigned long long kth = warp_kth(key, a.k);
+  if (lane == 0) {
+    float t = a.thr[q];
+    if (kth != ~0ull && !a.noprune) {
+      const float v = ord2f((unsigned)(kth >> 32));
+      if (MEAS == M_LCSS)
+        t = fmaxf(t, -v);
+      else
+        t = fminf(t, widen(v, gamma_dp(MEAS, a.qlen[q], a.max_clen)));
+    }
+    a.thr2[q] = t;
+    a.fcnt[q] = 0;
+  }
 }
 
 // Round 2: the remaining survivors whose bound passes the tightened
@@ -822,12 +859,16 @@ __global__ void __launch_bounds__(kSelThreads) final_select_kernel(KArgs a) {
 }
 
 // Bound on |compensated - FP64| relative to the value, for a path of P
-// cells: (4P + 32) u^2 from the (hi, lo) arithmetic plus (P + 8) 2^-53 from
+// cells.  DTW: each FP32 cost within 4u (u = 2^-24) and the compensated path
+// sum within (4P + 32) u^2 of its terms' sum; Frechet: one cost computed
+// from exact differences, within (4P + 32) u^2.  Plus (P + 8) 2^-53 for
 // FP64's own rounding, with 25% slack.
-__device__ __forceinline__ double gamma_c(int P) {
-  const double u2 = 1.0 / 281474976710656.0;  // 2^-48
+__device__ __forceinline__ double gamma_c(int meas, int P) {
+  const double u = 1.0 / 16777216.0;
+  const double u2 = u * u;
   const double e53 = 1.0 / 9007199254740992.0;
-  return ((4.0 * P + 32.0) * u2 + (P + 8.0) * e53) * 1.25;
+  const double cost = meas == M_DTW ? 4.0 * u : 0.0;
+  return (cost + (4.0 * P + 32.0) * u2 + (P + 8.0) * e53) * 1.25;
 }
 
 // Sort the re-score set by compensated value; pairs whose values are within
@@ -842,7 +883,7 @@ __global__ void cluster_kernel(KArgs a) {
   const double* rv = a.rdc + (size_t)q * a.RC;
   int2* r64p = a.r64pairs + (size_t)q * a.RC;
   // compensated DP values: gamma_c; FP32 pairwise values: twice their bound
-  const double g = is_dp(MEAS) ? gamma_c(a.qlen[q] + a.max_clen)
+  const double g = is_dp(MEAS) ? gamma_c(MEAS, a.qlen[q] + a.max_clen)
                                : 2.0 * gamma_dp(MEAS, a.qlen[q], a.max_clen);
   unsigned char ord[256];
   int n = 0;
@@ -930,6 +971,32 @@ __global__ void clear_u32_kernel(unsigned* p, size_t n) {
     p[i] = 0;
 }
 
+// Per-request counters, accumulated on the device (no host sync per chunk):
+// counters[2..6] += pairs passing the O(1) bound, the O(length) bound,
+// refined pairs, re-scored pairs, FP64 re-scored pairs.
+__global__ void stats_kernel(KArgs a, unsigned long long* counters, int with_rescore) {
+  unsigned long long c1 = 0, c2 = 0, rc = 0;
+  for (int q = threadIdx.x; q < a.nq; q += blockDim.x) {
+    c1 += a.cnt1[q];
+    c2 += a.cnt2[q];
+    rc += with_rescore ? a.rcnt[q] : 0;
+  }
+  for (int o = 16; o; o >>= 1) {
+    c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+    c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+    rc += __shfl_xor_sync(0xffffffffu, rc, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(counters + 2, c1);
+    atomicAdd(counters + 3, c2);
+    atomicAdd(counters + 5, rc);
+  }
+  if (threadIdx.x == 0) {
+    atomicAdd(counters + 4, (unsigned long long)(*a.npairs) + (unsigned long long)a.nq * (a.S + a.M));
+    if (with_rescore) atomicAdd(counters + 6, (unsigned long long)(*a.n64));
+  }
+}
+
 // DP of a pair list: the anti-diagonal kernel for the pairs it can take,
 // the round-striped kernel (G lanes x R rows) for the rest
 int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& d) {
@@ -938,7 +1005,7 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
                          kind == DP_FRECHET_SQC;
   if (!diag_kind || a.rdiag == 0) return launch_dp(ctx, kind, G, R, d, a.max_clen);
   TSIM_CUDA(cudaMemsetAsync(a.nspill, 0, sizeof(int), ctx->stream));
-  TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag, d, a.max_qlen, a.spill, a.nspill));
+  TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag, d, a.max_qlen, a.max_clen, a.spill, a.nspill));
   DpArgs sp = d;
   sp.order = a.spill;
   sp.npairs_dev = a.nspill;
@@ -1010,7 +1077,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   stage_end(ctx);
 
   stage_begin(ctx, TSIM_STAGE_FILTER);
-  thresh_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+  thresh_kernel<MEAS><<<(nq + 3) / 4, 128, 0, s>>>(a);
   if (MEAS == M_DTW || MEAS == M_LCSS) {
     qtable_global_kernel<<<nq, 256, 0, s>>>(a);
     launched(ctx);
@@ -1051,7 +1118,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   stage_end(ctx);
 
   stage_begin(ctx, TSIM_STAGE_FILTER);
-  thresh2_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+  thresh2_kernel<MEAS><<<(nq + 3) / 4, 128, 0, s>>>(a);
   refilter_kernel<MEAS><<<dim3(ch, nq), 256, 0, s>>>(a);
   scan_kernel<<<1, 1024, 0, s>>>(a);
   flatten_kernel<<<dim3(ch, nq), 256, 0, s>>>(a);
@@ -1124,28 +1191,10 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
     launched(ctx, 2);
     stage_end(ctx);
   }
-  if (st) {
-    // counts for the caller (synchronises)
-    int npairs = 0;
-    TSIM_CUDA(cudaMemcpyAsync(&npairs, a.npairs, sizeof(int), cudaMemcpyDeviceToHost, s));
-    std::vector<int> rc(nq), c1(nq), c2(nq);
-    TSIM_CUDA(cudaMemcpyAsync(rc.data(), a.rcnt, sizeof(int) * nq, cudaMemcpyDeviceToHost, s));
-    TSIM_CUDA(cudaMemcpyAsync(c1.data(), a.cnt1, sizeof(int) * nq, cudaMemcpyDeviceToHost, s));
-    TSIM_CUDA(cudaMemcpyAsync(c2.data(), a.cnt2, sizeof(int) * nq, cudaMemcpyDeviceToHost, s));
-    TSIM_CUDA(cudaStreamSynchronize(s));
-    for (int i = 0; i < nq; ++i) {
-      st->pairs_lb1 += c1[i];
-      st->pairs_lb2 += c2[i];
-    }
-    st->pairs_refined = (int64_t)npairs + (int64_t)nq * (a.S + a.M);
-    int64_t r = 0;
-    for (int v : rc) r += v;
-    st->rescored = MEAS == M_LCSS ? 0 : r;
-    int n64 = 0;
-    TSIM_CUDA(cudaMemcpyAsync(&n64, a.n64, sizeof(int), cudaMemcpyDeviceToHost, s));
-    TSIM_CUDA(cudaStreamSynchronize(s));
-    st->rescored_fp64 = n64;
-  }
+  stats_kernel<<<1, 256, 0, s>>>(a, ctx->dcounters, MEAS != M_LCSS ? 1 : 0);
+  TSIM_CUDA(cudaGetLastError());
+  launched(ctx);
+  (void)st;
   return TSIM_OK;
 }
 
@@ -1229,6 +1278,7 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.T = std::min(kChunk, std::max(1, (2 * a.S + a.nch - 1) / a.nch));
   a.T = std::min(a.T, 64);
   a.plain = (p->flags & TSIM_FLAG_PLAIN) ? 1 : 0;
+  a.noprune = (p->flags & TSIM_FLAG_NO_PRUNE) ? 1 : 0;
   {
     // rows per lane-group of the anti-diagonal kernel: the smallest R whose
     // validity condition holds for the longest pair shape (n = m is the worst)
@@ -1353,27 +1403,56 @@ extern "C" int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d
     *stats = tsim_stats{};
     TSIM_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
   }
-  // queries in batches whose pair count keeps the scratch bounded (offsets
-  // stay absolute into d_qpts, so a batch is a slice of d_qoff)
+  // Queries in chunks: a chunk's pair count keeps the scratch bounded, and
+  // chunks run round-robin on up to ctx->concurrency child streams so the
+  // latency-bound stages of different chunks overlap (offsets stay absolute
+  // into d_qpts, so a chunk is a slice of d_qoff).
   const int64_t kMaxPairs = int64_t(1) << 24;
-  const int qb = (int)std::max<int64_t>(1, std::min<int64_t>(nq, kMaxPairs / std::max(db->count, 1)));
-  tsim_stats acc{};
-  for (int q0 = 0; q0 < nq; q0 += qb) {
-    const int nb = std::min(qb, nq - q0);
-    tsim_stats part{};
-    int s = tsim::knn(ctx, p, reinterpret_cast<const float2*>(d_qpts), d_qoff + q0, nb, max_qlen,
-                      db, d_ids + (size_t)q0 * p->k, d_dists + (size_t)q0 * p->k,
-                      d_dists64 ? d_dists64 + (size_t)q0 * p->k : nullptr,
-                      stats ? &part : nullptr);
-    if (s != TSIM_OK) return s;
-    acc.pairs_refined += part.pairs_refined;
-    acc.pairs_lb1 += part.pairs_lb1;
-    acc.pairs_lb2 += part.pairs_lb2;
-    acc.rescored += part.rescored;
-    acc.rescored_fp64 += part.rescored_fp64;
+  constexpr int kMinChunk = 8;
+  int qb = (int)std::max<int64_t>(1, std::min<int64_t>(nq, kMaxPairs / std::max(db->count, 1)));
+  int nstreams = std::min(ctx->concurrency, std::max(1, nq / kMinChunk));
+  if (p->flags & TSIM_FLAG_PLAIN) nstreams = 1;
+  if (nstreams > 1) qb = std::min(qb, (nq + nstreams - 1) / nstreams);
+  std::vector<tsim_ctx*> lanes{ctx};
+  if (nstreams > 1) {
+    TSIM_TRY(tsim::ensure_subs(ctx, nstreams));
+    TSIM_CUDA(cudaEventRecord(ctx->fork_ev, ctx->stream));
+    lanes.assign(ctx->subs.begin(), ctx->subs.begin() + nstreams);
+    for (tsim_ctx* s : lanes) {
+      s->profiling = ctx->profiling;
+      TSIM_CUDA(cudaStreamWaitEvent(s->stream, ctx->fork_ev, 0));
+    }
   }
-  if (stats) *stats = acc;
+  if (stats)
+    for (tsim_ctx* c : lanes)
+      TSIM_CUDA(cudaMemsetAsync(c->dcounters + 2, 0, 5 * sizeof(unsigned long long), c->stream));
+  tsim_stats acc{};
+  int chunk = 0;
+  for (int q0 = 0; q0 < nq; q0 += qb, ++chunk) {
+    const int nb = std::min(qb, nq - q0);
+    tsim_ctx* run = lanes[chunk % lanes.size()];
+    int s = tsim::knn(run, p, reinterpret_cast<const float2*>(d_qpts), d_qoff + q0, nb, max_qlen,
+                      db, d_ids + (size_t)q0 * p->k, d_dists + (size_t)q0 * p->k,
+                      d_dists64 ? d_dists64 + (size_t)q0 * p->k : nullptr, nullptr);
+    if (s != TSIM_OK) return s;
+  }
+  if (nstreams > 1)
+    for (int i = 0; i < nstreams; ++i) {
+      TSIM_CUDA(cudaEventRecord(ctx->join_ev[i], ctx->subs[i]->stream));
+      TSIM_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join_ev[i], 0));
+    }
   if (stats) {
+    TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (tsim_ctx* c : lanes) {
+      unsigned long long v[5];
+      TSIM_CUDA(cudaMemcpy(v, c->dcounters + 2, sizeof(v), cudaMemcpyDeviceToHost));
+      acc.pairs_lb1 += (int64_t)v[0];
+      acc.pairs_lb2 += (int64_t)v[1];
+      acc.pairs_refined += (int64_t)v[2];
+      acc.rescored += (int64_t)v[3];
+      acc.rescored_fp64 += (int64_t)v[4];
+    }
+    *stats = acc;
     TSIM_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     TSIM_CUDA(cudaEventSynchronize(ctx->ev1));
     float ms = 0.0f;
@@ -1499,7 +1578,7 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   int* spill = arena_take<int>(ctx, npairs);
   int* nspill = arena_take<int>(ctx, 4);
   TSIM_CUDA(cudaMemsetAsync(nspill, 0, sizeof(int), ctx->stream));
-  TSIM_TRY(launch_dp_diag(ctx, kind, Rd, d, max_qlen, spill, nspill));
+  TSIM_TRY(launch_dp_diag(ctx, kind, Rd, d, max_qlen, max_clen, spill, nspill));
   d.order = spill;
   d.npairs_dev = nspill;
   return launch_dp(ctx, kind, G, R, d, max_clen);

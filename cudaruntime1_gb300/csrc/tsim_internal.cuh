@@ -72,6 +72,14 @@ struct tsim_ctx {
   double stage_ms[TSIM_STAGE_COUNT] = {};
   int64_t stage_calls[TSIM_STAGE_COUNT] = {};
   unsigned long long* dcounters = nullptr;  // device: [0] DP cells computed
+  // concurrency: a request's queries are split into chunks that run on these
+  // child contexts (own stream and arena), forked from and joined back to
+  // `stream` with events, so that latency-bound stages of different chunks
+  // overlap on the GPU
+  int concurrency = 4;
+  std::vector<tsim_ctx*> subs;
+  cudaEvent_t fork_ev = nullptr;
+  std::vector<cudaEvent_t> join_ev;
   // databases created on this context; destroying the context releases their
   // device memory and detaches them (a later tsim_db_destroy only frees the
   // handle), so destruction order cannot cause a use-after-free
@@ -109,6 +117,7 @@ T* arena_take(tsim_ctx* ctx, size_t count) {
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 int pinned_reserve(tsim_ctx* ctx, size_t bytes);
+int ensure_subs(tsim_ctx* ctx, int n);
 
 // stage timing: bracket one stage's launches; no-ops unless profiling is on
 void stage_begin(tsim_ctx* ctx, int stage);
@@ -250,8 +259,8 @@ int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a, int max_m)
 // Anti-diagonal kernel (dp_diag.cu) for DTW/LCSS/Frechet FP32 and compensated
 // kinds, R rows per lane-group (1, 2 or 4); pairs it cannot take are appended
 // to spill[] (count in *nspill) for launch_dp.  max_n bounds the query length.
-int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_n, int* spill,
-                   int* nspill);
+int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_n, int max_m,
+                   int* spill, int* nspill);
 bool diag_ok(bool lcss, int n, int m, int wd, int R);
 
 // choose (G, R) for pairs of shape n x m under band w

@@ -132,6 +132,11 @@ TSIM_API int tsim_ctx_set_profiling(tsim_ctx* ctx, int on);
  * reset != 0 clears the counters after reading. */
 TSIM_API int tsim_ctx_counters(tsim_ctx* ctx, double* ms, int64_t* calls, int64_t* launches,
                                int64_t* dp_cells, int reset);
+/* Number of streams one kNN request may use (default 4): the queries are
+ * split into chunks run concurrently on internal child streams, forked from
+ * and joined back to the context stream, so that latency-bound stages of
+ * different chunks overlap.  1 runs everything on the context stream. */
+TSIM_API int tsim_ctx_set_concurrency(tsim_ctx* ctx, int streams);
 /* Measured FP32 FMA throughput of this GPU in TFLOP/s (a short probe kernel,
  * for roofline denominators). */
 TSIM_API int tsim_probe_fp32_tflops(tsim_ctx* ctx, double* tflops);

@@ -75,8 +75,9 @@ def test_dp_pairs_all_kernels(tsim, cuda_ctx, oracle, measure, kw, lo, hi):
             if precision == 2:
                 ok = np.array_equal(got[f], w[f]) if measure != "frechet" else rel.max() <= 1e-15
                 assert ok, (tag, rel.max())
-            elif precision == 1:
-                assert rel.max() <= 1e-9, (tag, rel.max(), np.argmax(rel), pairs[f][np.argmax(rel)])
+            elif precision == 1:  # DTW: 4u from the FP32 costs; Frechet: double-float
+                lim = 4.5 * 2.0 ** -24 if measure == "dtw" else 1e-9
+                assert rel.max() <= lim, (tag, rel.max(), np.argmax(rel), pairs[f][np.argmax(rel)])
             else:
                 bound = (n_[f] + m_[f] + 8) * 2.0 ** -24 * 1.01 + 1e-12
                 assert np.all(rel <= bound), (tag, rel.max(), np.argmax(rel / bound))

