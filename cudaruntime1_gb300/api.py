@@ -230,18 +230,21 @@ def make_params(measure: str, k: int = 10, *, cost: int = COST_SQEUCLID, band_pc
     return TsimParams(MEASURES[measure], k, cost, band_pct, epsilon, delta, flags)
 
 
-def knn(ctx: Context, db: Database, qpts, qoff, measure: str, k: int = 10, **kw):
-    """Exact kNN with host arrays end to end.  Returns (ids[nq,k], dists[nq,k], stats)."""
+def knn(ctx: Context, db: Database, qpts, qoff, measure: str, k: int = 10, stats: bool = True,
+        **kw):
+    """Exact kNN with host arrays end to end.  Returns (ids[nq,k], dists[nq,k],
+    stats dict or None).  Without stats, repeated requests of one shape replay a
+    captured CUDA graph."""
     qpts = _pts(qpts)
     qoff = np.ascontiguousarray(qoff, np.int64)
     nq = len(qoff) - 1
     ids = np.zeros(nq * k, np.int32)
     d = np.zeros(nq * k, np.float32)
-    st = TsimStats()
+    st = TsimStats() if stats else None
     p = make_params(measure, k, **kw)
     check(ctx.L.tsim_knn_host(ctx.h, C.byref(p), _ptr(qpts), _ptr(qoff), nq, db.h, _ptr(ids),
-                              _ptr(d), C.byref(st)))
-    return ids.reshape(nq, k), d.reshape(nq, k), st.as_dict()
+                              _ptr(d), C.byref(st) if st is not None else None))
+    return ids.reshape(nq, k), d.reshape(nq, k), (st.as_dict() if st is not None else None)
 
 
 def knn_device(ctx: Context, db: Database, qpts_ptr: int, qoff_ptr: int, nq: int, max_qlen: int,

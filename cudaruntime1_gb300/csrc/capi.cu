@@ -38,6 +38,7 @@ int arena_reserve(tsim_ctx* ctx, size_t bytes) {
   }
   TSIM_CUDA(cudaMalloc(&ctx->arena, cap));
   ctx->arena_cap = cap;
+  ctx->arena_gen++;  // graphs captured over the old arena are stale
   return TSIM_OK;
 }
 
@@ -361,6 +362,9 @@ int tsim_ctx_destroy(tsim_ctx* c) {
   if (!c) return TSIM_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  for (auto& g : c->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
   for (tsim_ctx* s : c->subs) tsim_ctx_destroy(s);
   c->subs.clear();
   if (c->fork_ev) cudaEventDestroy(c->fork_ev);
@@ -523,6 +527,9 @@ int tsim_db_destroy(tsim_db* db) {
   if (db->ctx) {  // still attached: release its memory and unregister it
     cudaSetDevice(db->ctx->device);
     cudaStreamSynchronize(db->ctx->stream);
+    for (auto& g : db->ctx->graphs)  // captured graphs may reference this database
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+    db->ctx->graphs.clear();
     db_free(db);
     auto& v = db->ctx->dbs;
     v.erase(std::remove(v.begin(), v.end(), db), v.end());

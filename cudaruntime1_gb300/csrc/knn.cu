@@ -27,6 +27,8 @@
 // The reference's GPU path (CudaRuntime1/dtw.cu:99-234) instead ranks every
 // candidate by a heuristic bound, refines a fixed 10 and returns one value:
 // not an exact kNN.  This path returns the exact top-k ids and distances.
+#include <cstring>
+
 #include "bounds.cuh"
 #include "topk.cuh"
 #include "tsim_internal.cuh"
@@ -1388,9 +1390,110 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
 
 }  // namespace tsim
 
+static int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
+                       const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
+                       float* d_dists, double* d_dists64, tsim_stats* stats);
+
+namespace {
+
+std::vector<uint64_t> graph_key(tsim_ctx* ctx, const tsim_params* p, const void* qpts,
+                                const void* qoff, int nq, int max_qlen, const tsim_db* db,
+                                const void* ids, const void* dists, const void* d64) {
+  uint32_t eps;
+  memcpy(&eps, &p->epsilon, 4);
+  return {(uint64_t)p->measure, (uint64_t)p->k, (uint64_t)p->cost, (uint64_t)(uint32_t)p->band_pct,
+          eps, (uint64_t)(uint32_t)p->delta, p->flags, (uint64_t)nq, (uint64_t)max_qlen,
+          (uint64_t)(uintptr_t)db, (uint64_t)db->count, (uint64_t)(uintptr_t)qpts,
+          (uint64_t)(uintptr_t)qoff, (uint64_t)(uintptr_t)ids, (uint64_t)(uintptr_t)dists,
+          (uint64_t)(uintptr_t)d64, (uint64_t)ctx->concurrency};
+}
+
+std::vector<uint64_t> arena_gens(tsim_ctx* ctx) {
+  std::vector<uint64_t> g{ctx->arena_gen};
+  for (tsim_ctx* s : ctx->subs) g.push_back(s->arena_gen);
+  return g;
+}
+
+}  // namespace
+
+// A request is replayed from a captured CUDA graph when the same shape,
+// parameters and buffers come again: the first call runs eagerly (sizing
+// every scratch arena), the second is captured -- the fork to child streams
+// and the join are captured as graph dependencies -- and later calls launch
+// the graph.  Graphs are dropped when an arena is reallocated or a database
+// is destroyed.  Stats, profiling, the plain form and TSIM_FLAG_NO_GRAPH
+// run eagerly.
 extern "C" int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
                         const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
                         float* d_dists, double* d_dists64, tsim_stats* stats) {
+  TSIM_CHECK_ARG(ctx && p && db, "NULL ctx, params or database");
+  const bool graphable = !stats && !ctx->profiling &&
+                         !(p->flags & (TSIM_FLAG_NO_GRAPH | TSIM_FLAG_PLAIN));
+  if (!graphable)
+    return knn_request(ctx, p, d_qpts, d_qoff, nq, max_qlen, db, d_ids, d_dists, d_dists64, stats);
+  TSIM_CHECK_ARG(db->ctx == ctx, "database belongs to another (or a destroyed) context");
+  const auto key = graph_key(ctx, p, d_qpts, d_qoff, nq, max_qlen, db, d_ids, d_dists, d_dists64);
+  tsim_ctx::GraphEntry* e = nullptr;
+  for (auto& g : ctx->graphs)
+    if (g.key == key) e = &g;
+  if (e && e->exec && e->gens != arena_gens(ctx)) {  // stale: scratch moved
+    cudaGraphExecDestroy(e->exec);
+    e->exec = nullptr;
+    e->seen = 0;
+  }
+  if (e && e->exec) {
+    TSIM_CUDA(cudaSetDevice(ctx->device));
+    TSIM_CUDA(cudaGraphLaunch(e->exec, ctx->stream));
+    ctx->launches += e->launches;
+    return TSIM_OK;
+  }
+  if (!e) {
+    if (ctx->graphs.size() >= 16) {  // bounded cache: drop the oldest
+      if (ctx->graphs.front().exec) cudaGraphExecDestroy(ctx->graphs.front().exec);
+      ctx->graphs.erase(ctx->graphs.begin());
+    }
+    ctx->graphs.push_back(tsim_ctx::GraphEntry{});
+    e = &ctx->graphs.back();
+    e->key = key;
+  }
+  if (e->seen++ == 0)  // first sighting: eager, sizes the arenas
+    return knn_request(ctx, p, d_qpts, d_qoff, nq, max_qlen, db, d_ids, d_dists, d_dists64, stats);
+  // capture
+  TSIM_CUDA(cudaSetDevice(ctx->device));
+  const int64_t before = ctx->launches;
+  for (tsim_ctx* s : ctx->subs) s->launches = 0;
+  TSIM_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int st = knn_request(ctx, p, d_qpts, d_qoff, nq, max_qlen, db, d_ids, d_dists, d_dists64, nullptr);
+  cudaGraph_t graph = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+  if (st != TSIM_OK || ce != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    e->seen = 0;  // fall back to eager execution of this request
+    return knn_request(ctx, p, d_qpts, d_qoff, nq, max_qlen, db, d_ids, d_dists, d_dists64, stats);
+  }
+  cudaGraphExec_t exec = nullptr;
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    e->seen = 0;
+    return knn_request(ctx, p, d_qpts, d_qoff, nq, max_qlen, db, d_ids, d_dists, d_dists64, stats);
+  }
+  int64_t captured = ctx->launches - before;
+  for (tsim_ctx* s : ctx->subs) captured += s->launches;
+  ctx->launches = before;
+  e->exec = exec;
+  e->launches = captured;
+  e->gens = arena_gens(ctx);
+  TSIM_CUDA(cudaGraphLaunch(exec, ctx->stream));
+  ctx->launches += captured;
+  return TSIM_OK;
+}
+
+static int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
+                       const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
+                       float* d_dists, double* d_dists64, tsim_stats* stats) {
   TSIM_CHECK_ARG(ctx && p && db, "NULL ctx, params or database");
   TSIM_CHECK_ARG(nq >= 1 && max_qlen >= 1, "nq and max_qlen must be >= 1");
   TSIM_CHECK_ARG(d_qpts && d_qoff && d_ids && d_dists, "NULL device pointer");

@@ -80,6 +80,16 @@ struct tsim_ctx {
   std::vector<tsim_ctx*> subs;
   cudaEvent_t fork_ev = nullptr;
   std::vector<cudaEvent_t> join_ev;
+  // captured request graphs (tsim_knn replays them for repeated requests)
+  struct GraphEntry {
+    std::vector<uint64_t> key;
+    std::vector<uint64_t> gens;  // arena generations of ctx and child contexts at capture
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;
+    int seen = 0;
+  };
+  std::vector<GraphEntry> graphs;
+  uint64_t arena_gen = 0;  // bumped whenever the arena is reallocated
   // databases created on this context; destroying the context releases their
   // device memory and detaches them (a later tsim_db_destroy only frees the
   // handle), so destruction order cannot cause a use-after-free

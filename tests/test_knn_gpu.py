@@ -189,3 +189,38 @@ def test_pruning_never_changes_the_answer(tsim, cuda_ctx, measure, kw):
     assert np.array_equal(ids, ids2) and np.array_equal(d, d2)
     assert st2["pairs_refined"] >= 6 * 1500 and st["pairs_refined"] < st2["pairs_refined"]
     db.close()
+
+
+def test_graph_replay_follows_inputs(tsim, cuda_ctx, oracle):
+    """Repeated requests of one shape replay a captured CUDA graph; the graph
+    re-reads its input buffers, so changed query points give the new answer."""
+    import torch
+    cp, co = _db(900, 20, 60, 1300)
+    qp, qo = G.random_walks(24, G.uniform_lengths(24, 20, 60, 1301), 1302)
+    db = tsim.Database(cuda_ctx, cp, co)
+    stream = torch.cuda.Stream()
+    cuda_ctx.set_stream(stream.cuda_stream)
+    qpt = torch.from_numpy(qp).cuda()
+    qot = torch.from_numpy(qo).cuda()
+    k = 5
+    ids = torch.empty(24 * k, dtype=torch.int32, device="cuda")
+    d = torch.empty(24 * k, dtype=torch.float32, device="cuda")
+    want, _ = oracle.knn("dtw", qp, qo, cp, co, k, band_pct=10)
+    cuda_ctx.counters(reset=True)
+    for it in range(4):  # eager, capture, replay, replay
+        tsim.knn_device(cuda_ctx, db, qpt.data_ptr(), qot.data_ptr(), 24, 60, ids.data_ptr(),
+                        d.data_ptr(), None, "dtw", k, band_pct=10)
+        stream.synchronize()
+        assert np.array_equal(ids.cpu().numpy().reshape(24, k), want), it
+    launches = cuda_ctx.counters(reset=True)["launches"]
+    assert launches > 0
+    qp2 = qp[::-1].copy()  # new query points in the same buffer
+    qpt.copy_(torch.from_numpy(qp2))
+    stream.synchronize()
+    tsim.knn_device(cuda_ctx, db, qpt.data_ptr(), qot.data_ptr(), 24, 60, ids.data_ptr(),
+                    d.data_ptr(), None, "dtw", k, band_pct=10)
+    stream.synchronize()
+    want2, _ = oracle.knn("dtw", qp2, qo, cp, co, k, band_pct=10)
+    assert np.array_equal(ids.cpu().numpy().reshape(24, k), want2)
+    cuda_ctx.set_stream(None)
+    db.close()
