@@ -163,6 +163,56 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+SERVING = dict(workload="serving_mixed_measures", db_trajectories=1_000_000, db_len_lo=50,
+               db_len_hi=500, query_len_lo=16, query_len_hi=2048, k=10, arrival="poisson",
+               offered_rps=2000, measures="dtw,lcss,frechet,hausdorff,euclidean (uniform)",
+               seed=77)
+
+
+def run_serving(args):
+    """Serving loop: a resident 1M-trajectory database, Poisson arrivals of
+    single-query kNN requests of uniformly drawn measures and lengths,
+    admitted by device-memory budget; p50/p99 latency and achieved rate."""
+    import torch
+
+    import cudaruntime1_gb300 as T
+    from cudaruntime1_gb300 import serving as S
+    T.build()
+    w = dict(SERVING)
+    w.update(slots=args.slots, hbm_budget_bytes=args.budget_gib << 30, seconds=args.serve_seconds)
+    dev = 0
+    torch.cuda.set_device(dev)
+    ctx = T.Context(dev)
+    t_gen = time.perf_counter()
+    pts, off, max_len = S.device_random_walks(w["db_trajectories"], w["db_len_lo"],
+                                              w["db_len_hi"], w["seed"])
+    torch.cuda.synchronize()
+    db = T.Database(ctx, device_pts=pts.data_ptr(), device_off=off.data_ptr(),
+                    count=w["db_trajectories"], max_len=max_len)
+    gen_s = time.perf_counter() - t_gen
+    n_open = int(w["offered_rps"] * w["seconds"])
+    reqs = S.make_requests(n_open, w["query_len_lo"], w["query_len_hi"], w["seed"] + 1)
+    warm = S.make_requests(max(3, args.warmup) * 5, w["query_len_lo"], w["query_len_hi"],
+                           w["seed"] + 2)
+    with T.Server(ctx, db, slots=w["slots"], hbm_budget_bytes=w["hbm_budget_bytes"]) as srv:
+        S.run_closed_loop(srv, warm, w["k"])
+        closed = S.run_closed_loop(srv, reqs[: max(200, n_open // 4)], w["k"])
+        with ClockSampler(dev) as clk:
+            opened = S.run_open_loop(srv, reqs, w["offered_rps"], w["k"], seed=w["seed"] + 3)
+        st = srv.stats()
+    line = {"metric": "kNN requests/s served at 2,000 req/s offered (mixed measures, exact top-10)",
+            "value": opened["achieved_rps"], "unit": "requests/s", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic", "config": w,
+            "latency_ms": {"p50": opened["p50_ms"], "p99": opened["p99_ms"],
+                           "mean": opened["mean_ms"]},
+            "open_loop": opened, "closed_loop_capacity": closed, "server": st,
+            "db_build_s": gen_s, "db_device_bytes": db.device_bytes(),
+            "clocks": clk.summary()}
+    print(json.dumps(line))
+    db.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -172,10 +222,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--kernels-only", action="store_true",
                     help="only the warm-up and timed steps (for profiler launch lists)")
+    ap.add_argument("--workload", default="dtw_knn_batched_uneven",
+                    choices=["dtw_knn_batched_uneven", "serving"])
+    ap.add_argument("--serve-seconds", type=float, default=5.0)
+    ap.add_argument("--slots", type=int, default=32)
+    ap.add_argument("--budget-gib", type=int, default=8)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "serving":
+        return run_serving(args)
 
     import torch
     import torch.distributed as dist

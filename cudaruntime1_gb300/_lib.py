@@ -16,7 +16,8 @@ _LOCK = threading.Lock()
 
 TSIM_OK = 0
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
-          4: "timeout", 5: "unsupported", 6: "over budget"}
+          4: "timeout", 5: "unsupported", 6: "over budget", 7: "pending", 8: "queue full"}
+TSIM_ERR_BUDGET, TSIM_PENDING, TSIM_ERR_BUSY = 6, 7, 8
 
 DTW, LCSS, FRECHET, HAUSDORFF, EUCLIDEAN = range(5)
 COST_SQEUCLID, COST_EUCLID = 0, 1
@@ -39,6 +40,29 @@ class TsimStats(C.Structure):
                 ("cells", C.c_int64), ("cells_unpruned", C.c_int64), ("rescored", C.c_int64),
                 ("rescored_fp64", C.c_int64),
                 ("launches", C.c_int32), ("graph_replay", C.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class TsimServerOpts(C.Structure):
+    _fields_ = [("slots", C.c_int), ("hbm_budget_bytes", C.c_int64), ("queue_cap", C.c_int)]
+
+
+class TsimRequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("nq", C.c_int), ("k", C.c_int), ("queue_ms", C.c_double),
+                ("latency_ms", C.c_double), ("device_ms", C.c_double),
+                ("scratch_bytes", C.c_int64), ("inflight_at_admit", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class TsimServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("rejected", C.c_int64), ("queued", C.c_int), ("in_flight", C.c_int),
+                ("peak_in_flight", C.c_int), ("slots", C.c_int), ("budget_bytes", C.c_int64),
+                ("scratch_in_use", C.c_int64), ("peak_scratch_bytes", C.c_int64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -100,6 +124,14 @@ def load(build_if_missing: bool = False):
             "tsim_ctx_set_concurrency": ([_vp, C.c_int], C.c_int),
             "tsim_band_cells": ([_vp, C.POINTER(TsimParams), _vp, _vp, C.c_int, _vp,
                                  C.POINTER(C.c_int64)], C.c_int),
+            "tsim_knn_scratch_bytes": ([C.POINTER(TsimParams), C.c_int, C.c_int, _vp], C.c_int64),
+            "tsim_server_create": ([_vp, _vp, C.POINTER(TsimServerOpts), C.POINTER(_vp)], C.c_int),
+            "tsim_server_submit": ([_vp, C.POINTER(TsimParams), _vp, _vp, C.c_int,
+                                    C.POINTER(C.c_uint64)], C.c_int),
+            "tsim_server_wait": ([_vp, C.c_uint64, C.c_int, _vp, _vp, C.POINTER(TsimRequestInfo)],
+                                 C.c_int),
+            "tsim_server_get_stats": ([_vp, C.POINTER(TsimServerStats)], C.c_int),
+            "tsim_server_destroy": ([_vp], C.c_int),
             "tsim_dp_pairs": ([_vp, C.POINTER(TsimParams), C.c_int, C.c_int, _vp, _vp, C.c_int,
                                _vp, _vp, C.c_int, _vp, C.c_int, _vp, _vp], C.c_int),
         }

@@ -7,7 +7,9 @@ Two layers, both calling the CUDA library through its C ABI:
   euclidean.cuh): host arrays in, one float per query out, plus the elapsed
   milliseconds the reference returns through ``float& gpu_time``;
 * the exact kNN engine: a context, a device-resident candidate database and
-  ``knn`` / ``knn_device`` returning top-k ids and distances.
+  ``knn`` / ``knn_device`` returning top-k ids and distances;
+* the serving loop (``Server``): continuous batching of requests of mixed
+  measures and lengths, admitted by device-memory budget.
 """
 from __future__ import annotations
 
@@ -17,7 +19,8 @@ import numpy as np
 
 from . import _lib
 from ._lib import (COST_EUCLID, COST_SQEUCLID, DTW, EUCLIDEAN, FLAG_FP64_RESCORE,  # noqa: F401
-                   FLAG_NO_GRAPH, FLAG_NO_PRUNE, FLAG_PLAIN, FRECHET, HAUSDORFF, LCSS, TsimParams,
+                   FLAG_NO_GRAPH, FLAG_NO_PRUNE, FLAG_PLAIN, FRECHET, HAUSDORFF, LCSS,
+                   TSIM_PENDING, TsimParams, TsimRequestInfo, TsimServerOpts, TsimServerStats,
                    TsimStats, check)
 
 MEASURES = {"dtw": DTW, "lcss": LCSS, "frechet": FRECHET, "hausdorff": HAUSDORFF,
@@ -287,3 +290,71 @@ def dp_pairs(ctx: Context, measure: str, precision: int, kernel: int, qpts_ptr: 
                               C.c_void_p(qoff_ptr), max_qlen, C.c_void_p(cpts_ptr),
                               C.c_void_p(coff_ptr), max_clen, C.c_void_p(pairs_ptr), npairs,
                               C.c_void_p(out32_ptr), C.c_void_p(out64_ptr)))
+
+
+class Server:
+    """Continuous-batching request loop over a resident database
+    (tsim_server_*): ``submit`` returns a ticket at once; the library's worker
+    thread admits requests into free stream slots while their scratch fits
+    the device pool, so requests of any measure and length overlap on the GPU."""
+
+    def __init__(self, ctx: Context, db: Database, slots: int = 16,
+                 hbm_budget_bytes: int = 1 << 30, queue_cap: int = 65536):
+        self.ctx, self.db, self.L = ctx, db, ctx.L
+        opts = TsimServerOpts(slots, hbm_budget_bytes, queue_cap)
+        h = C.c_void_p()
+        check(self.L.tsim_server_create(ctx.h, db.h, C.byref(opts), C.byref(h)))
+        self.h = h
+        self._k = {}
+
+    def submit(self, qpts, qoff, measure: str, k: int = 10, **kw) -> int:
+        qpts = _pts(qpts)
+        qoff = np.ascontiguousarray(qoff, np.int64)
+        p = make_params(measure, k, **kw)
+        t = C.c_uint64()
+        check(self.L.tsim_server_submit(self.h, C.byref(p), _ptr(qpts), _ptr(qoff), len(qoff) - 1,
+                                        C.byref(t)))
+        self._k[t.value] = (len(qoff) - 1, k)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """(ids[nq,k], dists[nq,k], info dict); None if still pending."""
+        nq, k = self._k[ticket]
+        ids = np.zeros(nq * k, np.int32)
+        d = np.zeros(nq * k, np.float32)
+        info = TsimRequestInfo()
+        st = self.L.tsim_server_wait(self.h, ticket, timeout_ms, _ptr(ids), _ptr(d),
+                                     C.byref(info))
+        if st == TSIM_PENDING:
+            return None
+        del self._k[ticket]
+        check(st)
+        return ids.reshape(nq, k), d.reshape(nq, k), info.as_dict()
+
+    def stats(self) -> dict:
+        st = TsimServerStats()
+        check(self.L.tsim_server_get_stats(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tsim_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def knn_scratch_bytes(db: Database, measure: str, nq: int, max_qlen: int, k: int = 10,
+                      **kw) -> int:
+    p = make_params(measure, k, **kw)
+    return int(db.L.tsim_knn_scratch_bytes(C.byref(p), nq, max_qlen, db.h))

@@ -29,6 +29,8 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
 int arena_reserve(tsim_ctx* ctx, size_t bytes) {
   ctx->arena_used = 0;
   if (bytes <= ctx->arena_cap) return TSIM_OK;
+  if (ctx->arena_external)  // a block lent by a server: it never grows
+    return fail(TSIM_ERR_BUDGET, "request needs more scratch than it was admitted with");
   size_t cap = std::max(bytes + bytes / 4, size_t(1) << 20);
   if (ctx->arena) {
     TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -309,6 +311,8 @@ const char* tsim_status_string(int s) {
     case TSIM_ERR_TIMEOUT: return "bounded wait timed out";
     case TSIM_ERR_UNSUPPORTED: return "unsupported";
     case TSIM_ERR_BUDGET: return "over admission budget";
+    case TSIM_PENDING: return "pending";
+    case TSIM_ERR_BUSY: return "admission queue full";
   }
   return "unknown status";
 }
@@ -375,7 +379,7 @@ int tsim_ctx_destroy(tsim_ctx* c) {
     db->ctx = nullptr;
   }
   c->dbs.clear();
-  if (c->arena) cudaFree(c->arena);
+  if (c->arena && !c->arena_external) cudaFree(c->arena);
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -505,7 +509,8 @@ int tsim_db_wrap_device(tsim_ctx* ctx, const tsim_point* d_pts, const int64_t* d
     }
     ml = std::max<int64_t>(ml, db->h_off[t + 1] - db->h_off[t]);
   }
-  db->max_len = max_len > 0 ? max_len : ml;
+  (void)max_len;  // the offsets, read here anyway, give the exact value
+  db->max_len = ml;
   int s = db_alloc(db);
   if (s == TSIM_OK) s = db_summarize(db);
   if (s == TSIM_OK) {

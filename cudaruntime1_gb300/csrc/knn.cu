@@ -1255,20 +1255,14 @@ int band_cells(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const in
   return TSIM_OK;
 }
 
-int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
-        int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st) {
+namespace {
+
+// Launch parameters of one knn call (everything but the pointers) and the
+// scratch it carves from the arena.
+size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, KArgs& a) {
   const int C = db->count;
-  TSIM_CHECK_ARG(C >= 1, "database is empty");
   const int k = p->k;
-  KArgs a{};
   a.nq = nq;
-  a.qpts = qpts;
-  a.qoff = qoff;
-  a.cpts = db->pts;
-  a.coff = db->off;
-  a.cbox = db->box;
-  a.cends = db->ends;
-  a.clen = db->len;
   a.C = C;
   a.max_clen = db->max_len;
   a.max_qlen = max_qlen;
@@ -1283,13 +1277,16 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.noprune = (p->flags & TSIM_FLAG_NO_PRUNE) ? 1 : 0;
   {
     // rows per lane-group of the anti-diagonal kernel: the smallest R whose
-    // validity condition holds for the longest pair shape (n = m is the worst)
-    const int L = std::max(max_qlen, db->max_len);
+    // validity condition holds for every pair shape.  2 w(max(n,m)) (min(n,m)-1)
+    // / (n+m-2) grows with both lengths, so the longest query against the
+    // longest candidate is the worst case (pairs that still fail are spilled
+    // to the striped kernel by the kernel itself).
+    const int n = max_qlen, m = db->max_len;
     const int wd = p->measure == TSIM_LCSS ? p->delta
-                                           : (p->measure == TSIM_DTW ? band_w(L, L, p->band_pct) : -1);
+                                           : (p->measure == TSIM_DTW ? band_w(n, m, p->band_pct) : -1);
     a.rdiag = 0;
     for (int R : {1, 2, 4})
-      if (diag_ok(p->measure == TSIM_LCSS, L, L, wd, R)) {
+      if (diag_ok(p->measure == TSIM_LCSS, n, m, wd, R)) {
         a.rdiag = R;
         break;
       }
@@ -1302,12 +1299,6 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.Cw = (C + 31) / 32;
   a.RC = std::min(256, std::max(4 * k, 64));
   a.force64 = (p->flags & TSIM_FLAG_FP64_RESCORE) ? 1 : 0;
-  a.ids = ids;
-  a.dists = dists;
-  a.dists64 = dists64;
-  TSIM_CHECK_ARG((size_t)a.nch * a.T * sizeof(unsigned long long) <= 200 * 1024,
-                 "database too large for one request (seed selection)");
-
   const size_t nqC = (size_t)nq * C;
   size_t need = align256(sizeof(float4) * nq) * 2 + align256(sizeof(int) * nq) +
                 align256(sizeof(float) * nqC) + align256(sizeof(int) * nq * a.nch * a.T) +
@@ -1323,7 +1314,36 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
                 align256(sizeof(float) * nq * a.M) + 2 * align256(sizeof(float) * (nq + 1)) +
                 align256(sizeof(float4) * (size_t)nq * a.tstride) +
                 align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 256;
+  return need;
+}
+
+}  // namespace
+
+size_t knn_scratch_bytes(const tsim_params* p, int nq, int max_qlen, const tsim_db* db) {
+  KArgs a{};
+  return knn_plan(p, nq, max_qlen, db, a);
+}
+
+int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
+        int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st) {
+  TSIM_CHECK_ARG(db->count >= 1, "database is empty");
+  KArgs a{};
+  const size_t need = knn_plan(p, nq, max_qlen, db, a);
+  TSIM_CHECK_ARG((size_t)a.nch * a.T * sizeof(unsigned long long) <= 200 * 1024,
+                 "database too large for one request (seed selection)");
+  a.qpts = qpts;
+  a.qoff = qoff;
+  a.cpts = db->pts;
+  a.coff = db->off;
+  a.cbox = db->box;
+  a.cends = db->ends;
+  a.clen = db->len;
+  a.ids = ids;
+  a.dists = dists;
+  a.dists64 = dists64;
   TSIM_TRY(arena_reserve(ctx, need));
+  const int C = a.C;
+  const size_t nqC = (size_t)nq * C;
   float4* qbox = arena_take<float4>(ctx, nq);
   float4* qends = arena_take<float4>(ctx, nq);
   int* qlen = arena_take<int>(ctx, nq);
@@ -1663,11 +1683,10 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   d.band_pct = p->measure == TSIM_DTW ? p->band_pct : -1;
   d.delta = p->delta;
   d.eps = p->epsilon;
-  const int L = std::max(max_qlen, max_clen);
-  const int wd = p->measure == TSIM_LCSS ? p->delta : band_w(L, L, d.band_pct);
+  const int wd = p->measure == TSIM_LCSS ? p->delta : band_w(max_qlen, max_clen, d.band_pct);
   int Rd = 0;
   for (int R : {1, 2, 4})
-    if (diag_ok(p->measure == TSIM_LCSS, L, L, wd, R)) {
+    if (diag_ok(p->measure == TSIM_LCSS, max_qlen, max_clen, wd, R)) {
       Rd = R;
       break;
     }

@@ -58,6 +58,7 @@ struct tsim_ctx {
   char* arena = nullptr;
   size_t arena_cap = 0;
   size_t arena_used = 0;
+  bool arena_external = false;  // arena lent by a server's pool (not freed or grown here)
   // pinned host staging for the host-pointer entry points
   void* pinned = nullptr;
   size_t pinned_cap = 0;
@@ -237,6 +238,8 @@ enum DpKind {
   DP_NUM_KINDS
 };
 
+// scratch bytes one knn() call carves from the arena
+size_t knn_scratch_bytes(const tsim_params* p, int nq, int max_qlen, const tsim_db* db);
 int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
         int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st);
 // reference-semantics batch: scratch size and the call on caller-given scratch

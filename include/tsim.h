@@ -50,7 +50,9 @@ typedef enum tsim_status {
   TSIM_ERR_OUT_OF_MEMORY = 3,
   TSIM_ERR_TIMEOUT = 4, /* a bounded device-side wait ran out */
   TSIM_ERR_UNSUPPORTED = 5,
-  TSIM_ERR_BUDGET = 6 /* request exceeds the admission budget */
+  TSIM_ERR_BUDGET = 6, /* request exceeds the admission budget */
+  TSIM_PENDING = 7,    /* a served request has not finished yet */
+  TSIM_ERR_BUSY = 8    /* the server's admission queue is full */
 } tsim_status;
 
 typedef enum tsim_measure {
@@ -146,7 +148,8 @@ TSIM_API int tsim_probe_fp32_tflops(tsim_ctx* ctx, double* tflops);
  * summaries (bounding box, first/last point). */
 TSIM_API int tsim_db_create(tsim_ctx* ctx, const tsim_point* host_pts, const int64_t* host_off,
                             int count, tsim_db** out);
-/* Wraps device-resident points/offsets (not copied, caller keeps them alive). */
+/* Wraps device-resident points/offsets (not copied, caller keeps them alive).
+ * max_len is advisory: the longest trajectory is taken from the offsets. */
 TSIM_API int tsim_db_wrap_device(tsim_ctx* ctx, const tsim_point* dev_pts,
                                  const int64_t* dev_off, int count, int max_len, tsim_db** out);
 TSIM_API int tsim_db_destroy(tsim_db* db);
@@ -171,6 +174,57 @@ TSIM_API int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_q
 TSIM_API int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_point* h_qpts,
                            const int64_t* h_qoff, int nq, tsim_db* db, int* h_ids,
                            float* h_dists, tsim_stats* stats);
+
+/* Device scratch one tsim_knn call of this shape takes (per query chunk;
+ * the server admits requests against it). */
+TSIM_API int64_t tsim_knn_scratch_bytes(const tsim_params* p, int nq, int max_qlen,
+                                        const tsim_db* db);
+
+/* ---- Serving loop: continuous batching of kNN requests -----------------
+ * A server owns `slots` device streams and one device pool of
+ * `hbm_budget_bytes`.  Submitted requests (any measure, any query lengths)
+ * wait in a FIFO queue; a worker thread admits the head request as soon as a
+ * slot is free and its scratch (tsim_knn_scratch_bytes + staging) fits in the
+ * pool, so requests that arrive while others run start at once and their
+ * kernels overlap on the GPU.  The database stays resident.  A request's
+ * results do not depend on what else is in flight. */
+typedef struct tsim_server tsim_server;
+typedef struct tsim_server_opts {
+  int slots;                /* requests in flight at once (0: 16) */
+  int64_t hbm_budget_bytes; /* device pool for requests in flight (0: 1 GiB) */
+  int queue_cap;            /* requests waiting for admission (0: 65536) */
+} tsim_server_opts;
+typedef struct tsim_request_info {
+  int status;             /* tsim_status of the request */
+  int nq, k;
+  double queue_ms;        /* submit -> admission (host clock) */
+  double latency_ms;      /* submit -> results ready on the host (host clock) */
+  double device_ms;       /* CUDA-event time of the request on its stream */
+  int64_t scratch_bytes;  /* device memory it was admitted with */
+  int inflight_at_admit;  /* other requests on the device when it was admitted */
+} tsim_request_info;
+typedef struct tsim_server_stats {
+  int64_t submitted, completed, failed, rejected;
+  int queued, in_flight, peak_in_flight, slots;
+  int64_t budget_bytes, scratch_in_use, peak_scratch_bytes;
+} tsim_server_stats;
+
+TSIM_API int tsim_server_create(tsim_ctx* ctx, tsim_db* db, const tsim_server_opts* opts,
+                                tsim_server** out);
+/* Copies the query (host CSR, h_qoff[0] == 0) and returns at once with a
+ * ticket; TSIM_ERR_BUSY when the queue is full, TSIM_ERR_BUDGET when the
+ * request could never fit the pool. */
+TSIM_API int tsim_server_submit(tsim_server* s, const tsim_params* p, const tsim_point* h_qpts,
+                                const int64_t* h_qoff, int nq, uint64_t* ticket);
+/* Waits up to timeout_ms (< 0: forever) for a request; on completion copies
+ * h_ids[nq*k], h_dists[nq*k] (either may be NULL), fills info (may be NULL),
+ * forgets the ticket and returns the request's status.  TSIM_PENDING if it
+ * is still running. */
+TSIM_API int tsim_server_wait(tsim_server* s, uint64_t ticket, int timeout_ms, int* h_ids,
+                              float* h_dists, tsim_request_info* info);
+TSIM_API int tsim_server_get_stats(tsim_server* s, tsim_server_stats* st);
+/* Finishes the requests in flight, fails the queued ones, frees the pool. */
+TSIM_API int tsim_server_destroy(tsim_server* s);
 
 /* Values of given (query, candidate) pairs -- d_pairs[2*i] = query index,
  * d_pairs[2*i+1] = candidate index -- for DTW, LCSS or Frechet under p's
