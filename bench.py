@@ -163,6 +163,165 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# the other measured workloads: every measure, each over one device-resident
+# database; the CPU leg (the oracle's brute-force exact kNN on a bounded
+# sample of the queries, all host threads) also gives the parity answers
+KNN_WORKLOADS = {
+    "plain_small": dict(
+        workload="plain_small_five_measures", queries=8, candidates=1024, len_lo=128, len_hi=128,
+        lengths="fixed 128", step="normal", k=10, seed=11, cpu_queries=8, plain=True,
+        runs=[("dtw", dict(band_pct=-1, cost=0), 0), ("lcss", dict(epsilon=0.5, delta=-1), 0),
+              ("frechet", dict(), 0), ("hausdorff", dict(), 0), ("euclidean", dict(), 0)]),
+    "lcss_frechet": dict(
+        workload="lcss_frechet_256x65536", queries=256, candidates=65536,
+        lengths="lognormal(ln 200, 0.6) clipped to [32, 1024]", step="normal", k=10, seed=23,
+        cpu_queries=1, plain=False,
+        runs=[("lcss", dict(epsilon=0.25, delta=20), 0), ("frechet", dict(), 8)]),
+    "hausdorff_euclid": dict(
+        workload="hausdorff_euclid_1024x262144", queries=1024, candidates=262144,
+        lengths="Hausdorff: U[32, 256]; Euclidean: 256, 1% of candidates 2048, queries 2048",
+        step="student_t(3)", k=10, seed=37, cpu_queries=1, plain=False,
+        runs=[("hausdorff", dict(), 0), ("euclidean", dict(), 0)]),
+}
+
+
+def knn_workload_data(name, w, measure):
+    from cudaruntime1_gb300 import datagen as G
+    s, nq, nc = w["seed"], w["queries"], w["candidates"]
+    step = "student_t" if w["step"].startswith("student") else "normal"
+    if name == "plain_small":
+        ql, cl = np.full(nq, 128), np.full(nc, 128)
+    elif name == "lcss_frechet":
+        ql = G.lognormal_lengths(nq, np.log(200.0), 0.6, 32, 1024, s)
+        cl = G.lognormal_lengths(nc, np.log(200.0), 0.6, 32, 1024, s + 1)
+    elif measure == "hausdorff":
+        ql, cl = G.uniform_lengths(nq, 32, 256, s), G.uniform_lengths(nc, 32, 256, s + 1)
+    else:  # lock-step Euclidean: 256 points, 1% of the candidates 2048; queries 2048
+        rng = np.random.default_rng(s + 2)
+        cl = np.where(rng.random(nc) < 0.01, 2048, 256)
+        ql = np.full(nq, 2048)
+    cp, co = G.random_walks(nc, cl, s + 3, step=step)
+    qp, qo = G.random_walks(nq, ql, s + 4, step=step)
+    return qp, qo, cp, co
+
+
+def run_knn_workload(args, name):
+    import torch
+
+    import cudaruntime1_gb300 as T
+    from cudaruntime1_gb300 import api
+    w = KNN_WORKLOADS[name]
+    T.build()
+    dev = 0
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    ctx = T.Context(dev, stream.cuda_stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    k = w["k"]
+    per = {}
+    cache = {}
+    total_launches = 0
+    with ClockSampler(dev) as clk:
+        for measure, kw, flags in w["runs"]:
+            key = measure if name == "hausdorff_euclid" else "all"  # one dataset per shape
+            if key not in cache:
+                cache = {key: knn_workload_data(name, w, measure)}
+            qp, qo, cp, co = cache[key]
+            nq = len(qo) - 1
+            db = T.Database(ctx, cp, co)
+            qpt = torch.from_numpy(qp).cuda()
+            qot = torch.from_numpy(qo).cuda()
+            ids = torch.empty(nq * k, dtype=torch.int32, device="cuda")
+            dd = torch.empty(nq * k, dtype=torch.float32, device="cuda")
+            d64 = torch.empty(nq * k, dtype=torch.float64, device="cuda")
+            maxq = int(np.max(np.diff(qo)))
+            tune = ctx.autotune(db, qpt.data_ptr(), qot.data_ptr(), nq, maxq, measure, k, reps=3,
+                                flags=flags, **kw)
+
+            def step():
+                api.knn_device(ctx, db, qpt.data_ptr(), qot.data_ptr(), nq, maxq, ids.data_ptr(),
+                               dd.data_ptr(), d64.data_ptr(), measure, k, flags=flags, **kw)
+
+            for _ in range(args.warmup):
+                step()
+            torch.cuda.synchronize()
+            ctx.counters(reset=True)
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(args.steps)]
+            for a, b in evs:
+                flush.zero_()
+                a.record(stream)
+                step()
+                b.record(stream)
+            torch.cuda.synchronize()
+            ms = sum(a.elapsed_time(b) for a, b in evs)
+            cnt = ctx.counters(reset=True)
+            total_launches += cnt["launches"]
+            r_ids = ids.cpu().numpy().reshape(nq, k)
+            r_d = dd.cpu().numpy().reshape(nq, k).astype(np.float64)
+            r_d64 = d64.cpu().numpy().reshape(nq, k)
+            _, _, st = T.knn(ctx, db, qp, qo, measure, k, stats=True, flags=flags, **kw)
+            res = {"queries_per_s": nq * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                   "dp_cells_per_step": cnt["dp_cells"] / args.steps,
+                   "gcups": cnt["dp_cells"] / (ms * 1e6) if cnt["dp_cells"] else None,
+                   "funnel": {x: st[x] for x in ("pairs", "pairs_lb1", "pairs_lb2",
+                                                 "pairs_refined", "rescored", "rescored_fp64")},
+                   "autotune": tune, "params": dict(kw, flags=flags)}
+            if w["plain"]:
+                T.knn(ctx, db, qp, qo, measure, k, flags=api.FLAG_PLAIN, **kw)
+                t0 = time.perf_counter()
+                p_ids, _, _ = T.knn(ctx, db, qp, qo, measure, k, flags=api.FLAG_PLAIN, **kw)
+                res["plain_queries_per_s"] = nq / (time.perf_counter() - t0)
+                res["batched_vs_plain"] = res["queries_per_s"] / res["plain_queries_per_s"]
+                res["plain_ids_match"] = bool(np.array_equal(p_ids, r_ids))
+            if not args.no_cpu:
+                res["cpu_baseline"], res["parity"] = knn_cpu_leg(
+                    measure, kw, qp, qo, cp, co, k, w["cpu_queries"], r_ids, r_d, r_d64)
+            per[measure] = res
+            db.close()
+    first = w["runs"][0][0]
+    line = {"metric": f"exact kNN queries/s per measure ({w['workload']})",
+            "value": per[first]["queries_per_s"], "unit": "queries/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {x: w[x] for x in w if x not in ("runs", "plain", "cpu_queries")},
+            "value_measure": first, "per_measure": per, "gpu_launches": total_launches,
+            "l2": "flushed before every timed step (512 MiB write)", "clocks": clk.summary()}
+    print(json.dumps(line))
+    ctx.close()
+
+
+def knn_cpu_leg(measure, kw, qp, qo, cp, co, k, nsample, r_ids, r_d, r_d64):
+    """The oracle's brute-force exact kNN on the first ``nsample`` queries
+    (FP64, all host threads): CPU queries/s and the parity of those queries."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build(ref=False)
+    okw = dict(kw)
+    if "epsilon" in okw:
+        okw["eps"] = okw.pop("epsilon")
+    qo_s = np.asarray(qo[:nsample + 1], np.int64)
+    qp_s = qp[:qo_s[-1]]
+    t0 = time.perf_counter()
+    oids, od = O.knn(measure, qp_s, qo_s, cp, co, k, **okw)
+    el = time.perf_counter() - t0
+    base = {"value": nsample / el, "unit": "queries/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"{nsample} queries x {len(co) - 1} candidates, oracle brute-force exact kNN "
+                      f"(FP64, OpenMP), {el:.1f} s"}
+    fin = np.isfinite(od)
+    par = {"queries_checked": nsample,
+           "ids_bit_exact": bool(np.array_equal(oids, r_ids[:nsample]))}
+    if measure == "lcss":
+        par["counts_exact"] = bool(np.array_equal(od, r_d[:nsample]))
+    elif fin.any():
+        denom = np.maximum(od[fin], 1e-300)
+        par["max_rel_err_f32"] = float(np.max(np.abs(r_d[:nsample][fin] - od[fin]) / denom))
+        par["max_rel_err_f64_output"] = float(np.max(np.abs(r_d64[:nsample][fin] - od[fin]) / denom))
+    return base, par
+
+
 SERVING = dict(workload="serving_mixed_measures", db_trajectories=1_000_000, db_len_lo=50,
                db_len_hi=500, query_len_lo=16, query_len_hi=2048, k=10, arrival="poisson",
                offered_rps=2000, measures="dtw,lcss,frechet,hausdorff,euclidean (uniform)",
@@ -223,7 +382,7 @@ def main():
     ap.add_argument("--kernels-only", action="store_true",
                     help="only the warm-up and timed steps (for profiler launch lists)")
     ap.add_argument("--workload", default="dtw_knn_batched_uneven",
-                    choices=["dtw_knn_batched_uneven", "serving"])
+                    choices=["dtw_knn_batched_uneven", "serving"] + list(KNN_WORKLOADS))
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--slots", type=int, default=32)
     ap.add_argument("--budget-gib", type=int, default=8)
@@ -233,6 +392,8 @@ def main():
         return run_reference(args)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload in KNN_WORKLOADS:
+        return run_knn_workload(args, args.workload)
 
     import torch
     import torch.distributed as dist
@@ -265,6 +426,9 @@ def main():
         api.knn_device(ctx, db, qpt.data_ptr(), qot.data_ptr(), nq, maxq, ids.data_ptr(),
                        dd.data_ptr(), d64.data_ptr(), "dtw", k, **kw)
 
+    # launch choices (rows per lane-group, concurrent query chunks) picked by
+    # the autotuner on this request before anything is timed
+    tune = ctx.autotune(db, qpt.data_ptr(), qot.data_ptr(), nq, maxq, "dtw", k, reps=5, **kw)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -302,18 +466,28 @@ def main():
     # ---- per-stage device times (CUDA events on the launching stream); the
     # chunks of a request overlap on child streams in the timed region, so
     # per-kernel durations are taken with one stream
+    import tempfile
+    tune_file = os.path.join(tempfile.mkdtemp(), "tuning.txt")
+    ctx.save_tuning(tune_file)
+    ctx.clear_tuning()
     ctx.set_concurrency(1)
     ctx.set_profiling(True)
     prof_steps = 5
     for _ in range(prof_steps):
         flush.zero_()
         step()
+    surv_cells = ctx.survivor_cells() / prof_steps
     prof = ctx.counters(reset=True)
     ctx.set_profiling(False)
     ctx.set_concurrency(4)
+    ctx.load_tuning(tune_file)
     stage_ms = {s: v / prof_steps for s, v in prof["stage_ms"].items() if v > 0}
     dp_cells = prof["dp_cells"] / prof_steps
-    dp_launch_ms = stage_ms.get("dp", 0.0) / max(1, prof["stage_calls"]["dp"] / prof_steps)
+    # the dominant kernel: the survivor round's DP launch (one per step here)
+    surv_calls = max(1.0, prof["stage_calls"]["dp_survivors"] / prof_steps)
+    surv_ms = stage_ms.get("dp_survivors", 0.0) / surv_calls
+    surv_cells_launch = surv_cells / surv_calls
+    _, _, funnel = T.knn(ctx, db, qp, qo, "dtw", k, stats=True, **kw)
     band_cells = api.band_cells(ctx, db, qpt.data_ptr(), qot.data_ptr(), nq, "dtw",
                                 band_pct=w["band_pct"])
     fp32_peak = ctx.probe_fp32_tflops()
@@ -362,7 +536,8 @@ def main():
         peaks = measured_peaks()
         step_s = total_ms / args.steps / 1e3
         dominant = max(stage_ms, key=stage_ms.get) if stage_ms else "dp"
-        achieved = dp_cells * DP_FLOPS_PER_CELL / (dp_launch_ms * 1e-3) / 1e12 if dp_launch_ms else 0
+        achieved = (surv_cells_launch * DP_FLOPS_PER_CELL / (surv_ms * 1e-3) / 1e12
+                    if surv_ms else 0.0)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -374,17 +549,22 @@ def main():
             "dp_cells_per_step": dp_cells, "band_cells_per_step": band_cells,
             "survivor_cell_frac": dp_cells / band_cells if band_cells else None,
             "stage_ms": stage_ms, "dominant_stage": dominant,
+            "funnel": {x: funnel[x] for x in ("pairs", "pairs_lb1", "pairs_lb2", "pairs_refined",
+                                              "rescored", "rescored_fp64")},
+            "autotune": tune,
             "plain": {"value": plain_qps, "unit": UNIT, "sample_queries": nplain,
                       "ids_match_batched": plain_ok},
             "batched_vs_plain": value / plain_qps if plain_qps else None,
             "parity": {"ids_bit_exact_vs_fp64_oracle": ids_match, "max_rel_err": max_rel},
             "roofline": {
-                "kernel": "dp_pairs_kernel (FP32 wavefront DTW of the surviving pairs)",
+                "kernel": "dp_diag_kernel<PolDtwSq,R>, survivor round (FP32 anti-diagonal DTW)",
                 "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
                 "peak_source": "measured FP32 FMA probe kernel on this GPU (tsim_probe_fp32_tflops)",
-                "flops_per_cell": DP_FLOPS_PER_CELL,
-                "dp_launch_ms": dp_launch_ms},
+                "flops_per_cell": DP_FLOPS_PER_CELL, "cells_per_launch": surv_cells_launch,
+                "launch_ms": surv_ms,
+                "timing": "CUDA events around the launch on its stream, single-stream "
+                          "profiling pass of the same workload after the timed region"},
             "cpu_baseline": base,
             "e2e": {"value": e2e_qps, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ids_match_device_path": e2e_ok},

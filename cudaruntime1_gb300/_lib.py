@@ -22,7 +22,7 @@ TSIM_ERR_BUDGET, TSIM_PENDING, TSIM_ERR_BUSY = 6, 7, 8
 DTW, LCSS, FRECHET, HAUSDORFF, EUCLIDEAN = range(5)
 COST_SQEUCLID, COST_EUCLID = 0, 1
 FLAG_NO_PRUNE, FLAG_PLAIN, FLAG_NO_GRAPH, FLAG_FP64_RESCORE = 1, 2, 4, 8
-STAGES = ["summary", "lb1", "seed", "filter", "dp", "select", "rescore", "ref"]
+STAGES = ["summary", "lb1", "seed", "filter", "dp", "select", "rescore", "ref", "dp_survivors"]
 
 _vp = C.c_void_p
 _ip = C.POINTER(C.c_int)
@@ -63,6 +63,14 @@ class TsimServerStats(C.Structure):
                 ("rejected", C.c_int64), ("queued", C.c_int), ("in_flight", C.c_int),
                 ("peak_in_flight", C.c_int), ("slots", C.c_int), ("budget_bytes", C.c_int64),
                 ("scratch_in_use", C.c_int64), ("peak_scratch_bytes", C.c_int64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class TsimTuneResult(C.Structure):
+    _fields_ = [("rdiag", C.c_int), ("streams", C.c_int), ("best_ms", C.c_double),
+                ("default_ms", C.c_double), ("tried", C.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -122,8 +130,15 @@ def load(build_if_missing: bool = False):
                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int], C.c_int),
             "tsim_probe_fp32_tflops": ([_vp, C.POINTER(C.c_double)], C.c_int),
             "tsim_ctx_set_concurrency": ([_vp, C.c_int], C.c_int),
+            "tsim_ctx_survivor_cells": ([_vp, C.POINTER(C.c_int64)], C.c_int),
             "tsim_band_cells": ([_vp, C.POINTER(TsimParams), _vp, _vp, C.c_int, _vp,
                                  C.POINTER(C.c_int64)], C.c_int),
+            "tsim_autotune": ([_vp, C.POINTER(TsimParams), _vp, _vp, C.c_int, C.c_int, _vp, C.c_int,
+                               C.POINTER(TsimTuneResult)], C.c_int),
+            "tsim_tuning_save": ([_vp, C.c_char_p], C.c_int),
+            "tsim_tuning_load": ([_vp, C.c_char_p], C.c_int),
+            "tsim_tuning_clear": ([_vp], C.c_int),
+            "tsim_tuning_count": ([_vp], C.c_int),
             "tsim_knn_scratch_bytes": ([C.POINTER(TsimParams), C.c_int, C.c_int, _vp], C.c_int64),
             "tsim_server_create": ([_vp, _vp, C.POINTER(TsimServerOpts), C.POINTER(_vp)], C.c_int),
             "tsim_server_submit": ([_vp, C.POINTER(TsimParams), _vp, _vp, C.c_int,

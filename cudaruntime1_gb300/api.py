@@ -167,6 +167,34 @@ class Context:
         """Streams one kNN request may use (chunks of queries overlap)."""
         check(self.L.tsim_ctx_set_concurrency(self.h, streams))
 
+    def autotune(self, db, qpts_ptr: int, qoff_ptr: int, nq: int, max_qlen: int, measure: str,
+                 k: int = 10, reps: int = 5, **kw) -> dict:
+        """Time the launch choices on this request (device pointers) and keep
+        the fastest for its shape class (tsim_autotune)."""
+        p = make_params(measure, k, **kw)
+        r = _lib.TsimTuneResult()
+        check(self.L.tsim_autotune(self.h, C.byref(p), C.c_void_p(qpts_ptr), C.c_void_p(qoff_ptr),
+                                   nq, max_qlen, db.h, reps, C.byref(r)))
+        return r.as_dict()
+
+    def save_tuning(self, path: str):
+        check(self.L.tsim_tuning_save(self.h, str(path).encode()))
+
+    def load_tuning(self, path: str):
+        check(self.L.tsim_tuning_load(self.h, str(path).encode()))
+
+    def clear_tuning(self):
+        check(self.L.tsim_tuning_clear(self.h))
+
+    def tuning_count(self) -> int:
+        return self.L.tsim_tuning_count(self.h)
+
+    def survivor_cells(self) -> int:
+        """DP cells of the survivor round since the last counter reset."""
+        v = C.c_int64()
+        check(self.L.tsim_ctx_survivor_cells(self.h, C.byref(v)))
+        return v.value
+
     def probe_fp32_tflops(self) -> float:
         v = C.c_double()
         check(self.L.tsim_probe_fp32_tflops(self.h, C.byref(v)))

@@ -250,9 +250,9 @@ extern "C" int tsim_ctx_counters(tsim_ctx* ctx, double* ms, int64_t* calls, int6
       calls_acc[s] += c->stage_calls[s];
     }
     launches_acc += c->launches;
-    unsigned long long cells = 0;
-    TSIM_CUDA(cudaMemcpy(&cells, c->dcounters, sizeof(cells), cudaMemcpyDeviceToHost));
-    cells_acc += cells;
+    unsigned long long cells[2] = {0, 0};  // [0] all DP cells but [1] those of the survivor round
+    TSIM_CUDA(cudaMemcpy(cells, c->dcounters, sizeof(cells), cudaMemcpyDeviceToHost));
+    cells_acc += cells[0] + cells[1];
   }
   for (int s = 0; s < TSIM_STAGE_COUNT; ++s) {
     if (ms) ms[s] = ms_acc[s];
@@ -279,6 +279,21 @@ extern "C" int tsim_ctx_counters(tsim_ctx* ctx, double* ms, int64_t* calls, int6
     TSIM_CUDA(cudaMemsetAsync(ctx->dcounters, 0, 64, ctx->stream));
     TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
   }
+  return TSIM_OK;
+}
+
+extern "C" int tsim_ctx_survivor_cells(tsim_ctx* ctx, int64_t* cells) {
+  TSIM_CHECK_ARG(ctx && cells, "NULL argument");
+  unsigned long long acc = 0;
+  std::vector<tsim_ctx*> all{ctx};
+  all.insert(all.end(), ctx->subs.begin(), ctx->subs.end());
+  for (tsim_ctx* c : all) {
+    TSIM_CUDA(cudaStreamSynchronize(c->stream));
+    unsigned long long v = 0;
+    TSIM_CUDA(cudaMemcpy(&v, c->dcounters + 1, sizeof(v), cudaMemcpyDeviceToHost));
+    acc += v;
+  }
+  *cells = (int64_t)acc;
   return TSIM_OK;
 }
 

@@ -15,12 +15,19 @@
 // |i(m-1) - j(n-1)| <= W (W = w (min(n,m)-1)) that holds whenever
 // 2W < 31 R (n + m - 2); for a full row (no band) when m <= 31 R + 1; for
 // an LCSS window |i - j| <= delta when delta <= 31 R.  Pairs that fail the
-// condition (or whose query exceeds the row table) are listed for the
-// round-striped kernel instead (dp_kernels.cu).
+// condition are listed for the round-striped kernel instead (dp_kernels.cu).
+//
+// No shared memory: a lane's band columns come from integer ramps stepped
+// by additions, the query points of its next group are prefetched into
+// registers one group ahead, and the candidate point of the next step is
+// loaded (through L1) one step ahead.  Occupancy is set by registers alone.
 //
 // Early abandon: every warping path crosses one of any two consecutive
 // anti-diagonals and DP values never decrease along a path, so the minimum
 // over the last two anti-diagonals bounds the final value from below.
+#include <type_traits>
+#include <vector>
+
 #include "dp_policies.cuh"
 
 namespace tsim {
@@ -28,6 +35,7 @@ namespace {
 using namespace dp;
 
 constexpr int kDiagThreads = 128;
+constexpr int kMaxStagedCols = 768;  // candidate points staged per warp (6 KiB)
 constexpr int kNone = 1 << 30;
 
 }  // namespace
@@ -42,20 +50,77 @@ __host__ __device__ bool diag_ok(bool lcss, int n, int m, int wd, int R) {
 
 namespace {
 
+// Row band [lo(i), hi(i)] as exact integer ramps,
+//   lo(i) = max(0, ceil((a i - Wl) / d)),  hi(i) = min(m - 1, floor((a i + Wh) / d)):
+// band: a = m-1, d = n-1, Wl = Wh = w (min(n,m)-1); LCSS window: a = d = 1,
+// Wl = Wh = delta; full rows: a = 0, d = 1, Wl = 0, Wh = m-1.  A numerator is
+// kept as quotient and remainder by d, so stepping rows costs additions; the
+// lo numerator is shifted by K d (K d > Wl) to stay non-negative.
+struct Ramp {
+  int q, r;
+};
+
+struct Ramps {
+  int d, K, m, n;
+  long long a, Wl, Wh;
+  __device__ __forceinline__ Ramp lo_at(long long i) const {
+    const long long x = a * i - Wl + (d - 1) + (long long)K * d;
+    return Ramp{(int)(x / d), (int)(x % d)};
+  }
+  __device__ __forceinline__ Ramp hi_at(long long i) const {
+    const long long x = a * i + Wh;
+    return Ramp{(int)(x / d), (int)(x % d)};
+  }
+  __device__ __forceinline__ void step(Ramp& x, int dq, int dr) const {
+    x.q += dq;
+    x.r += dr;
+    if (x.r >= d) {
+      x.r -= d;
+      x.q += 1;
+    }
+  }
+  __device__ __forceinline__ int lo(const Ramp& x) const { return max(0, x.q - K); }
+  __device__ __forceinline__ int hi(const Ramp& x) const { return min(m - 1, x.q); }
+};
+
+// wd: band width w (DTW/Frechet), window delta (LCSS), < 0 for full rows
+__device__ __forceinline__ Ramps make_ramps(int n, int m, int wd, bool lcss) {
+  Ramps rp;
+  rp.m = m;
+  rp.n = n;
+  if (wd < 0) {
+    rp.a = 0, rp.d = 1, rp.Wl = 0, rp.Wh = m - 1;
+  } else if (lcss) {
+    rp.a = 1, rp.d = 1, rp.Wl = rp.Wh = wd;
+  } else {
+    rp.a = m - 1, rp.d = n - 1, rp.Wl = rp.Wh = (long long)wd * (min(n, m) - 1);
+  }
+  rp.K = (int)(rp.Wl / rp.d) + 1;
+  return rp;
+}
+
+// resident CTAs per SM asked of the register allocator: 8 (32 warps) where
+// the FP32 policies fit 64 registers without spilling, fewer for the
+// compensated (two-float) values and for R = 4
 template <class P, int R>
-__global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row_cap, int col_cap,
-                                                                int* spill, int* nspill) {
+constexpr int diag_min_blocks() {
+  return sizeof(typename P::V) > 4        ? (R == 1 ? 8 : (R == 2 ? 6 : 4))
+         : std::is_same<P, PolDtwEu>::value ? (R == 1 ? 8 : (R == 2 ? 6 : 4))
+                                            : (R <= 2 ? 8 : 5);
+}
+
+template <class P, int R>
+__global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
+    dp_diag_kernel(DpArgs a, int col_cap, int* spill, int* nspill) {
   using V = typename P::V;
-  extern __shared__ __align__(16) float4 diag_rows[];
+  extern __shared__ __align__(16) float2 diag_cand[];
   constexpr bool kLcss = !P::kMin;
+  constexpr int kRound = 32 * R;  // rows between two groups of one lane
   const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  // per warp: the row table, then the candidate's points
-  float4* rt = diag_rows + (size_t)wib * (row_cap + col_cap / 2);
-  float2* cs = reinterpret_cast<float2*>(rt + row_cap);
-  const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
-  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
   const int npairs = a.npairs_dev ? min(*a.npairs_dev, a.npairs) : a.npairs;
+  float2* cs = diag_cand + (size_t)(threadIdx.x >> 5) * col_cap;  // this warp's candidate
 
   for (int wk = gw; wk < npairs; wk += nw) {
     const int pid = a.order ? a.order[wk] : wk;
@@ -66,10 +131,12 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
     const int n = (int)(a.qoff[q + 1] - qo), m = (int)(a.coff[pr.y + 1] - co);
     const float2* A = a.qpts + qo;
     const float2* B = a.cpts + co;
+    // the candidate's points, read once into shared memory when they fit
+    // (longer candidates are read through L1 step by step)
+    const bool staged = m <= col_cap;
     const int w = band_w(n, m, a.band_pct);
     const int wd = kLcss ? a.delta : w;
-    const int nr = (n + 32 * R - 1) / (32 * R) * (32 * R);  // rows incl. padding
-    if (!diag_ok(kLcss, n, m, wd, R) || nr > row_cap || m > col_cap) {
+    if (!diag_ok(kLcss, n, m, wd, R)) {
       if (lane == 0 && spill) spill[atomicAdd(nspill, 1)] = pid;
       continue;
     }
@@ -77,52 +144,69 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
     const int rrow = result_row<P>(n, m, a.delta);
     if (lane == 0) store_result(a, pid, P::border());
 
-    // row table: query point and band of every row (empty rows: kNone)
-    long long cells_all = 0;
-    for (int i = lane; i < nr; i += 32) {
-      float4 e = make_float4(0.f, 0.f, __int_as_float(kNone), __int_as_float(kNone));
-      if (i < n) {
-        int lo, hi;
-        RowBand<P>::get(i, n, m, w, a.delta, lo, hi);
-        const float2 p = A[i];
-        if (hi >= lo) {
-          e = make_float4(p.x, p.y, __int_as_float(lo), __int_as_float(hi));
-          cells_all += hi - lo + 1;
-        } else {
-          e = make_float4(p.x, p.y, __int_as_float(kNone), __int_as_float(kNone));
-        }
-      }
-      rt[i] = e;
-    }
-    for (int j = lane; j < m; j += 32) cs[j] = B[j];  // the candidate, read once
-    __syncwarp();
+    const Ramps rp = make_ramps(n, m, wd, kLcss);
+    const int row_q = (int)(rp.a / rp.d), row_r = (int)(rp.a % rp.d);
+    const int rnd_q = (int)(kRound * rp.a / rp.d), rnd_r = (int)(kRound * rp.a % rp.d);
 
-    int i0 = R * lane;  // first row of the lane's current group
-    float qx[R], qy[R];
-    int jlo[R], jhi[R];
-    V left[R], left2[R];  // each row's values one and two columns back
+    // the lane's next group (first row i1, its band ramps, prefetched points)
+    int i1 = R * lane;
+    Ramp L1 = rp.lo_at(i1), H1 = rp.hi_at(i1);
+    float nqx[R], nqy[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const float4 e = rt[i0 + r];
-      qx[r] = e.x;
-      qy[r] = e.y;
-      jlo[r] = __float_as_int(e.z);
-      jhi[r] = __float_as_int(e.w);
-      left[r] = left2[r] = P::border();
+      const float2 p = i1 + r < n ? __ldg(A + i1 + r) : make_float2(0.f, 0.f);
+      nqx[r] = p.x;
+      nqy[r] = p.y;
     }
-    // step at which the next group's first row starts (never, if none)
-    auto next_start = [&](int base) -> int {
-      const int i1 = base + 32 * R;
-      if (i1 >= n) return 0x7fffffff;
-      const int lo = __float_as_int(rt[i1].z);
-      return lo == kNone ? 0x7fffffff : i1 + lo;
+    int i0 = 0;
+    float qx[R], qy[R];
+    int base[R];      // step at which row r's band starts: t - base = column - lo
+    unsigned wdt[R];  // band width - 1 (empty rows: never in band)
+    V left[R], left2[R];  // each row's values one and two columns back
+    // switch to the next group: rows from the ramps, points from the prefetch
+    auto take_next = [&]() -> int {
+      i0 = i1;
+      Ramp L = L1, H = H1;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int lo = rp.lo(L), hi = rp.hi(H);
+        const bool ok = i0 + r < n && hi >= lo;
+        base[r] = ok ? i0 + r + lo : 0x3fffffff;
+        wdt[r] = ok ? (unsigned)(hi - lo) : 0u;
+        qx[r] = nqx[r];
+        qy[r] = nqy[r];
+        left[r] = left2[r] = P::border();
+        if (r + 1 < R) {
+          rp.step(L, row_q, row_r);
+          rp.step(H, row_q, row_r);
+        }
+      }
+      i1 += kRound;
+      rp.step(L1, rnd_q, rnd_r);
+      rp.step(H1, rnd_q, rnd_r);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float2 p = i1 + r < n ? __ldg(A + i1 + r) : make_float2(0.f, 0.f);
+        nqx[r] = p.x;
+        nqy[r] = p.y;
+      }
+      if (i1 >= n) return 0x7fffffff;  // step at which the following group starts
+      const int lo = rp.lo(L1), hi = rp.hi(H1);
+      return hi >= lo ? i1 + lo : 0x7fffffff;
     };
-    int ns = next_start(i0);
+    int ns = take_next();
+    __syncwarp();
+    if (staged)
+      for (int j = lane; j < m; j += 32) cs[j] = __ldg(B + j);
+    __syncwarp();
+    const float2* C = staged ? cs : B;
     V out = P::border();
     V prev_raw = P::border();  // the shuffled value of the previous step
     float2 cw[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) cw[r] = cs[0];
+    for (int r = 0; r < R; ++r) cw[r] = make_float2(0.f, 0.f);
+    // candidate point of the next step, loaded one step ahead
+    float2 cnext = C[min(max(-i0, 0), m - 1)];
     V result = P::border();
     bool holds = false;
     bool alive = true;
@@ -138,17 +222,7 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
             result = left[r];
             holds = true;
           }
-        i0 += 32 * R;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const float4 e = rt[i0 + r];
-          qx[r] = e.x;
-          qy[r] = e.y;
-          jlo[r] = __float_as_int(e.z);
-          jhi[r] = __float_as_int(e.w);
-          left[r] = left2[r] = P::border();
-        }
-        ns = next_start(i0);
+        ns = take_next();
       }
       // the last row of the previous lane's group, one column back: the row
       // above this lane's first row (lane 0's first group reads the virtual
@@ -160,22 +234,24 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
       prev_raw = raw;
 #pragma unroll
       for (int r = R - 1; r > 0; --r) cw[r] = cw[r - 1];
-      const int j0 = t - i0;
-      cw[0] = cs[min(max(j0, 0), m - 1)];
+      cw[0] = cnext;
+      {
+        const int inext = t + 1 == ns ? i1 : i0;
+        cnext = C[min(max(t + 1 - inext, 0), m - 1)];
+      }
       float mstep = TSIM_INF;
-      // row r computes column j0 - r: its up neighbour is row r-1 one step
+      // row r computes column t - i0 - r: its up neighbour is row r-1 one step
       // ago and its diagonal neighbour row r-1 two steps ago, so rows are
       // visited last to first before row r-1 is overwritten
 #pragma unroll
       for (int r = R - 1; r >= 0; --r) {
-        const int j = j0 - r;
         const V lf = left[r];
         const V up = r > 0 ? left[r > 0 ? r - 1 : 0] : up_in;
         const V dg = r > 0 ? left2[r > 0 ? r - 1 : 0] : dg_in;
         V v = P::cell(qx[r], qy[r], cw[r].x, cw[r].y, up, lf, dg, a.eps);
-        const bool in = (unsigned)(j - jlo[r]) <= (unsigned)(jhi[r] - jlo[r]);
+        const bool in = (unsigned)(t - base[r]) <= wdt[r];
         v = in ? v : P::masked(lf);
-        if (P::kMin) mstep = fminf(mstep, in ? vf(v) : TSIM_INF);
+        if (P::kMin) mstep = fminf(mstep, vf(v));  // masked cells are +inf
         left2[r] = lf;
         left[r] = v;
       }
@@ -199,17 +275,16 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
         result = left[r];
         holds = true;
       }
-    if (a.cells) {
-      long long cells = cells_all;
-      if (!alive) {  // cells of the anti-diagonals computed before abandoning
-        cells = 0;
-        for (int i = lane; i < n; i += 32) {
-          const float4 e = rt[i];
-          const int lo = __float_as_int(e.z), hi = __float_as_int(e.w);
-          if (lo == kNone) continue;
-          const int h = min(hi, t_ab - i);
-          if (h >= lo) cells += h - lo + 1;
-        }
+    if (a.cells) {  // cells of the anti-diagonals 0 .. t_ab inside the band
+      const Ramps rp = make_ramps(n, m, kLcss ? a.delta : band_w(n, m, a.band_pct), kLcss);
+      long long cells = 0;
+      const int q32 = (int)(32 * rp.a / rp.d), r32 = (int)(32 * rp.a % rp.d);
+      Ramp L = rp.lo_at(lane), H = rp.hi_at(lane);
+      for (int i = lane; i < n; i += 32) {
+        const int lo = rp.lo(L), hi = min(rp.hi(H), t_ab - i);
+        if (hi >= lo) cells += hi - lo + 1;
+        rp.step(L, q32, r32);
+        rp.step(H, q32, r32);
       }
       for (int o = 16; o; o >>= 1) cells += __shfl_xor_sync(0xffffffffu, cells, o);
       if (lane == 0) atomicAdd(a.cells, (unsigned long long)cells);
@@ -222,14 +297,11 @@ __global__ void __launch_bounds__(kDiagThreads) dp_diag_kernel(DpArgs a, int row
 }
 
 template <class P, int R>
-int launch_diag_one(tsim_ctx* ctx, const DpArgs& a, int max_n, int max_m, int* spill,
-                    int* nspill) {
+int launch_diag_one(tsim_ctx* ctx, const DpArgs& a, int max_m, int* spill, int* nspill) {
   if (a.npairs <= 0) return TSIM_OK;
-  const int row_cap = (max_n + 32 * R - 1) / (32 * R) * (32 * R);
-  const int col_cap = (max_m + 1) & ~1;  // even: whole float4 slots
   const int warps = kDiagThreads / 32;
-  const size_t smem = (size_t)warps * (row_cap + col_cap / 2) * sizeof(float4);
-  if (smem > 200 * 1024) return fail(TSIM_ERR_UNSUPPORTED, "pair too long for the row tables");
+  const int col_cap = (std::min(max_m, kMaxStagedCols) + 1) & ~1;
+  const size_t smem = (size_t)warps * col_cap * sizeof(float2);
   auto kern = dp_diag_kernel<P, R>;
   if (smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -237,35 +309,57 @@ int launch_diag_one(tsim_ctx* ctx, const DpArgs& a, int max_n, int max_m, int* s
   TSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kDiagThreads, smem));
   long long blocks = std::min<long long>((a.npairs + warps - 1) / warps,
                                          (long long)std::max(per_sm, 1) * ctx->num_sms);
-  kern<<<(unsigned)std::max(blocks, 1ll), kDiagThreads, smem, ctx->stream>>>(a, row_cap, col_cap,
-                                                                            spill, nspill);
+  kern<<<(unsigned)std::max(blocks, 1ll), kDiagThreads, smem, ctx->stream>>>(a, col_cap, spill,
+                                                                            nspill);
   TSIM_CUDA(cudaGetLastError());
   launched(ctx);
   return TSIM_OK;
 }
 
 template <class P>
-int launch_diag_r(tsim_ctx* ctx, int R, const DpArgs& a, int max_n, int max_m, int* spill,
-                  int* nspill) {
+int launch_diag_r(tsim_ctx* ctx, int R, const DpArgs& a, int max_m, int* spill, int* nspill) {
   switch (R) {
-    case 1: return launch_diag_one<P, 1>(ctx, a, max_n, max_m, spill, nspill);
-    case 2: return launch_diag_one<P, 2>(ctx, a, max_n, max_m, spill, nspill);
-    default: return launch_diag_one<P, 4>(ctx, a, max_n, max_m, spill, nspill);
+    case 1: return launch_diag_one<P, 1>(ctx, a, max_m, spill, nspill);
+    case 2: return launch_diag_one<P, 2>(ctx, a, max_m, spill, nspill);
+    default: return launch_diag_one<P, 4>(ctx, a, max_m, spill, nspill);
   }
+}
+
+template <class P>
+int launch_chain(tsim_ctx* ctx, int R0, const DpArgs& a, int max_m, int* spill, int* nspill,
+                 int* tmp, int* ntmp) {
+  // R0, 2 R0, .., 4: each pass takes the pairs the previous one spilled, so
+  // every pair runs with the fewest rows per lane-group its shape admits
+  // (fewer rows in flight, fewer masked cells); the last pass writes `spill`
+  std::vector<int> rs;
+  for (int R = std::max(1, R0); R <= 4; R *= 2) rs.push_back(R);
+  const int np = (int)rs.size();
+  DpArgs in = a;
+  for (int p = 0; p < np; ++p) {
+    const bool to_spill = ((np - 1 - p) & 1) == 0;
+    int* out = to_spill ? spill : tmp;
+    int* nout = to_spill ? nspill : ntmp;
+    TSIM_CUDA(cudaMemsetAsync(nout, 0, sizeof(int), ctx->stream));
+    TSIM_TRY(launch_diag_r<P>(ctx, rs[p], in, max_m, out, nout));
+    in.order = out;
+    in.npairs_dev = nout;
+  }
+  return TSIM_OK;
 }
 
 }  // namespace
 
-int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_n, int max_m,
-                   int* spill, int* nspill) {
+int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, int* spill,
+                   int* nspill, int* tmp, int* ntmp) {
   switch (kind) {
-    case DP_DTW_SQ: return launch_diag_r<PolDtwSq>(ctx, R, a, max_n, max_m, spill, nspill);
-    case DP_DTW_EU: return launch_diag_r<PolDtwEu>(ctx, R, a, max_n, max_m, spill, nspill);
-    case DP_LCSS: return launch_diag_r<PolLcss>(ctx, R, a, max_n, max_m, spill, nspill);
-    case DP_FRECHET_SQ: return launch_diag_r<PolFrechetSq>(ctx, R, a, max_n, max_m, spill, nspill);
-    case DP_DTW_SQC: return launch_diag_r<PolDtwSqC>(ctx, R, a, max_n, max_m, spill, nspill);
-    case DP_DTW_EUC: return launch_diag_r<PolDtwEuC>(ctx, R, a, max_n, max_m, spill, nspill);
-    case DP_FRECHET_SQC: return launch_diag_r<PolFrechetSqC>(ctx, R, a, max_n, max_m, spill, nspill);
+    case DP_DTW_SQ: return launch_chain<PolDtwSq>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_EU: return launch_chain<PolDtwEu>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_LCSS: return launch_chain<PolLcss>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_FRECHET_SQ: return launch_chain<PolFrechetSq>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_SQC: return launch_chain<PolDtwSqC>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_EUC: return launch_chain<PolDtwEuC>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_FRECHET_SQC:
+      return launch_chain<PolFrechetSqC>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
   }
   return fail(TSIM_ERR_UNSUPPORTED, "no anti-diagonal kernel for this DP kind");
 }

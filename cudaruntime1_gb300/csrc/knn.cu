@@ -42,6 +42,7 @@ namespace {
 
 constexpr int kChunk = 256;     // candidates per stage-A CTA
 constexpr int kSelThreads = 256;
+constexpr int kSeg = 2048;       // list entries per CTA of the two-level selections
 constexpr int kLb2Warps = 8;
 constexpr int kMaxTable = 512;  // sparse-table columns (query rows, downsampled beyond)
 
@@ -98,6 +99,8 @@ struct KArgs {
   const float4* csegbox;    // [C*kSegs] candidate segment boxes
   int* spill;               // pairs the anti-diagonal kernel leaves to the striped one
   int* nspill;
+  int* spill2;              // the list between passes of the anti-diagonal kernel
+  int* nspill2;
   int rdiag;                // rows per lane-group of the anti-diagonal kernel (0: off)
   float4* qtab;             // [nq*tstride] query sparse tables (global memory)
   int tstride;
@@ -107,7 +110,10 @@ struct KArgs {
   int* order;               // [nq*C] shape-sorted schedule of flat
   int* shape_cnt;           // [kNumShapes]
   float* flat_vals;         // [nq*C]
-  unsigned long long* fkeys;  // [nq*(S+C)]
+  int nseg;                 // segments of kSeg entries per query (two-level selection)
+  unsigned long long* segkeys;  // [nq*nseg*64] best keys of every segment
+  unsigned long long* kthkey;   // [nq] key of the k-th best refined pair
+  int* rraw;                    // [nq] pairs within the re-score bound (before the cap)
   int RC;
   int2* rpairs;             // [nq*RC] re-score set
   double* rdc;              // [nq*RC] compensated FP32 (hi+lo) values
@@ -390,21 +396,65 @@ __global__ void qtable_global_kernel(KArgs a) {
 // point is matched, so the maximum over segments; LCSS: a column can only
 // match when the boxes, eps-inflated, meet).  Columns 0 and m-1 are the
 // exact corner cells for DTW.
+// columns of candidate segment s: [seg_first(s), seg_first(s + 1))
+__device__ __forceinline__ int seg_first(int s, int m) { return (int)(((long long)s * m) / kSegs); }
+
+// Row side of the segment bounds: the query's rows in kRowSegs segments;
+// the rows of a segment admit only columns [clo, chi], so each costs at
+// least the distance between the segment's box and the nearest candidate
+// segment box meeting those columns.
+constexpr int kRowSegs = 32;
+
+__device__ __forceinline__ float row_seg_min(const QTable& T, const float4* sb, int m, int r0,
+                                             int r1, int clo, int chi, int& sf) {
+  const float4 qx = qtable_box(T, r0, r1);
+  while (sf < kSegs - 1 && seg_first(sf + 1, m) <= clo) ++sf;
+  float mn = TSIM_INF;
+  for (int s = sf; s < kSegs && seg_first(s, m) <= chi; ++s) {
+    const float4 b = sb[s];
+    if (b.x > b.z) continue;  // empty segment (m < kSegs)
+    mn = fminf(mn, box_box_d2_rd(qx, b));
+  }
+  return mn;
+}
+
+// t: the pair's pruning threshold; once a partial bound exceeds it the pair
+// is pruned and the rest is not evaluated
 template <int MEAS>
-__device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1) {
-  if (MEAS == M_EUCLID || n > a.max_qlen || n < 1 || m < 1) return lb1;
+__device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1, float t) {
+  if (n > a.max_qlen || n < 1 || m < 1) return lb1;
   const float4* sb = a.csegbox + (size_t)c * kSegs;
   const float4 qb = a.qbox[q];
+  const QTable T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
+  if (MEAS == M_EUCLID) {
+    // lock-step: column j meets row j only, so segment s of the candidate
+    // costs at least its box's distance to the box of the same query rows
+    if (n < m) return TSIM_INF;
+    float acc = 0.0f;
+    for (int s = 0; s < kSegs; ++s) {
+      const int b0 = seg_first(s, m), b1 = seg_first(s + 1, m) - 1;
+      if (b1 < b0) continue;
+      const float d = box_box_d2_rd(qtable_box(T, b0, b1), sb[s]);
+      acc = __fadd_rd(acc, __fmul_rd((float)(b1 - b0 + 1), d));
+    }
+    return fmaxf(acc, lb1);
+  }
   if (MEAS == M_FRECHET || MEAS == M_HAUSDORFF) {
+    // every point of either set is matched to some point of the other
     float mx = lb1;
     for (int s = 0; s < kSegs; ++s) {
       const float4 b = sb[s];
       if (b.x > b.z) continue;  // empty segment
       mx = fmaxf(mx, box_box_d2_rd(qb, b));
     }
+    const int L = (n + kRowSegs - 1) / kRowSegs;
+    int sf = 0;
+    for (int r0 = 0; r0 < n && mx <= t; r0 += L) {
+      sf = 0;
+      mx = fmaxf(mx, row_seg_min(T, sb, m, r0, min(n - 1, r0 + L - 1), 0, m - 1, sf));
+    }
     return mx;
   }
-  const QTable T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
   if (MEAS == M_LCSS) {
     const float e2 = __fmul_ru(a.eps, 1.0f + 1.0f / 1048576.0f);
     int count = 0;
@@ -457,7 +507,44 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
     const float d = box_box_d2_rd(qx, sb[s]);
     acc = __fadd_rd(acc, __fmul_rd((float)(b1 - b0 + 1), a.cost ? __fsqrt_rd(d) : d));
   }
-  return fmaxf(acc, lb1);
+  // rows 1 .. n-2, each with at least one path cell inside its band columns
+  // (the corner cells of rows 0 and n-1 are already counted); a segment of
+  // rows r0..r1 admits columns [lo(r0), hi(r0 + L - 1)], from integer ramps
+  if (fmaxf(acc, lb1) > t) return fmaxf(acc, lb1);
+  float accr;
+  {
+    const float d0 = pd2_rd(qe.x, qe.y, ce.x, ce.y), d1 = pd2_rd(qe.z, qe.w, ce.z, ce.w);
+    accr = a.cost ? __fadd_rd(__fsqrt_rd(d0), __fsqrt_rd(d1)) : __fadd_rd(d0, d1);
+  }
+  if (n > 2) {
+    const int L = (n - 2 + kRowSegs - 1) / kRowSegs;
+    const long long d = n - 1, sl = (long long)L * (m - 1);
+    const long long K = W / d + 1;
+    long long xl = (long long)(m - 1) - W + (d - 1) + K * d;  // lo numerator at row 1
+    long long xh = (long long)L * (m - 1) + W;                // hi numerator at row L
+    int ql = (int)(xl / d), rl = (int)(xl % d), qh = (int)(xh / d), rh = (int)(xh % d);
+    const int sq = (int)(sl / d), sr = (int)(sl % d);
+    int sf = 0;
+    for (int r0 = 1; r0 <= n - 2; r0 += L) {
+      const int r1 = min(n - 2, r0 + L - 1);
+      int clo = 0, chi = m - 1;
+      if (banded) {
+        clo = max(0, ql - (int)K);
+        chi = min(m - 1, qh);
+        ql += sq;
+        rl += sr;
+        if (rl >= d) rl -= (int)d, ++ql;
+        qh += sq;
+        rh += sr;
+        if (rh >= d) rh -= (int)d, ++qh;
+      }
+      if (chi < clo) return TSIM_INF;  // rows with no admissible column: infeasible
+      const float mn = row_seg_min(T, sb, m, r0, r1, clo, chi, sf);
+      accr = __fadd_rd(accr, __fmul_rd((float)(r1 - r0 + 1), a.cost ? __fsqrt_rd(mn) : mn));
+      if (accr > t) break;
+    }
+  }
+  return fmaxf(fmaxf(acc, accr), lb1);
 }
 
 template <int MEAS>
@@ -471,7 +558,7 @@ __global__ void __launch_bounds__(kChunk) compact_kernel(KArgs a) {
     const float b = a.lb1[(size_t)q * a.C + c];
     pass = !seeded && (MEAS == M_LCSS ? (b >= t) : (b <= t));
     if (pass) {  // the segment bound, only for pairs the O(1) bound keeps
-      const float sbnd = seg_bound<MEAS>(a, q, c, a.qlen[q], a.clen[c], b);
+      const float sbnd = seg_bound<MEAS>(a, q, c, a.qlen[q], a.clen[c], b, t);
       pass = MEAS == M_LCSS ? (sbnd >= t) : (sbnd <= t);
     }
   }
@@ -628,14 +715,9 @@ __global__ void __launch_bounds__(kSelThreads) r1_select_kernel(KArgs a) {
   __shared__ unsigned long long red[33];
   __shared__ unsigned long long sel[64];
   const int q = blockIdx.x;
-  const int N = a.cnt2[q];
-  unsigned long long* keys = a.fkeys + (size_t)q * (a.S + a.C);
-  for (int i = threadIdx.x; i < N; i += kSelThreads) {
-    const float b = a.lb2v[(size_t)q * a.C + i];
-    keys[i] = pack_key(MEAS == M_LCSS ? -b : b, i);
-  }
-  __syncthreads();
-  block_select_k(keys, N, a.M, sel, red);
+  const int ns = (a.cnt2[q] + kSeg - 1) / kSeg;
+  // the segments' M best (seg_select_kernel) hold the query's M best
+  block_select_k(a.segkeys + (size_t)q * a.nseg * 64, ns * a.M, a.M, sel, red);
   for (int i = threadIdx.x; i < a.M; i += kSelThreads) {
     const int pos = key_index(sel[i]);
     int c = -1;
@@ -806,24 +888,48 @@ __device__ __forceinline__ void entry(const KArgs& a, int q, int i, int base, in
   }
 }
 
+// K best keys of one kSeg-entry segment of each query's list, selected in
+// shared memory: MODE 0 the O(length) bounds of the survivors (key index =
+// position in list2), MODE 1 the refined values (key index = candidate).
+// The per-query selections then run over nseg * K keys instead of the list.
+template <int MEAS, int MODE>
+__global__ void __launch_bounds__(kSelThreads) seg_select_kernel(KArgs a, int K) {
+  __shared__ unsigned long long keys[kSeg];
+  __shared__ unsigned long long red[33];
+  __shared__ unsigned long long sel[64];
+  const int q = blockIdx.y, seg = blockIdx.x;
+  const int N = MODE == 0 ? a.cnt2[q] : a.S + a.M + a.fcnt[q];
+  const int lo = seg * kSeg;
+  if (lo >= N) return;
+  const int cnt = min(kSeg, N - lo);
+  const int base = MODE == 1 ? a.off2[q] : 0;
+  for (int t = threadIdx.x; t < cnt; t += kSelThreads) {
+    const int i = lo + t;
+    unsigned long long key;
+    if (MODE == 0) {
+      const float b = a.lb2v[(size_t)q * a.C + i];
+      key = pack_key(MEAS == M_LCSS ? -b : b, i);
+    } else {
+      int c;
+      float v;
+      entry(a, q, i, base, c, v);
+      key = c >= 0 ? pack_key(MEAS == M_LCSS ? -v : v, c) : ~0ull;
+    }
+    keys[t] = key;
+  }
+  __syncthreads();
+  block_select_k(keys, cnt, K, sel, red);
+  unsigned long long* out = a.segkeys + (size_t)q * a.nseg * 64 + (size_t)seg * K;
+  for (int t = threadIdx.x; t < K; t += kSelThreads) out[t] = sel[t];
+}
+
 template <int MEAS>
 __global__ void __launch_bounds__(kSelThreads) final_select_kernel(KArgs a) {
   __shared__ unsigned long long red[33];
   __shared__ unsigned long long sel[64];
-  __shared__ int rc;
   const int q = blockIdx.x;
-  const int S = a.S, M = a.M, nf = a.fcnt[q], base = a.off2[q];
-  const int N = S + M + nf;
-  unsigned long long* keys = a.fkeys + (size_t)q * (a.S + a.C);
-  for (int i = threadIdx.x; i < N; i += kSelThreads) {
-    int c;
-    float v;
-    entry(a, q, i, base, c, v);
-    keys[i] = c >= 0 ? pack_key(MEAS == M_LCSS ? -v : v, c) : ~0ull;
-  }
-  if (threadIdx.x == 0) rc = 0;
-  __syncthreads();
-  block_select_k(keys, N, a.k, sel, red);
+  const int ns = (a.S + a.M + a.fcnt[q] + kSeg - 1) / kSeg;
+  block_select_k(a.segkeys + (size_t)q * a.nseg * 64, ns * a.k, a.k, sel, red);
   if (MEAS == M_LCSS) {
     for (int i = threadIdx.x; i < a.k; i += kSelThreads) {
       int c = key_index(sel[i]);
@@ -834,30 +940,49 @@ __global__ void __launch_bounds__(kSelThreads) final_select_kernel(KArgs a) {
     }
     return;
   }
-  // the k-th best FP32 value fixes the re-score set
-  const unsigned long long kth = sel[a.k - 1];
+  // the k-th best FP32 value fixes the re-score set (collected by
+  // rescore_collect_kernel)
+  if (threadIdx.x == 0) {
+    a.kthkey[q] = sel[a.k - 1];
+    a.rraw[q] = 0;
+  }
+}
+
+// The re-score set: every refined pair within the FP32 error bound of the
+// k-th value (or, when that is infinite, the k best keys).  Segments of the
+// list in parallel; members are appended in any order (later stages sort).
+template <int MEAS>
+__global__ void rescore_collect_kernel(KArgs a) {
+  const int q = blockIdx.y;
+  const int N = a.S + a.M + a.fcnt[q], base = a.off2[q];
+  const unsigned long long kth = a.kthkey[q];
   const float tk = kth == ~0ull ? TSIM_INF : ord2f((unsigned)(kth >> 32));
   const bool finite = tk < TSIM_INF;
   const float tr = widen(tk, gamma_dp(MEAS, a.qlen[q], a.max_clen));
-  // keys were consumed by the selection: rebuild membership from values
-  for (int i = threadIdx.x; i < N; i += kSelThreads) {
+  const int hi = min(N, (blockIdx.x + 1) * kSeg);
+  for (int i = blockIdx.x * kSeg + threadIdx.x; i < hi; i += blockDim.x) {
     int c;
     float v;
     entry(a, q, i, base, c, v);
     if (c < 0) continue;
-    bool take = finite ? (v <= tr) : (pack_key(v, c) <= kth);
+    const bool take = finite ? (v <= tr) : (pack_key(v, c) <= kth);
     if (take) {
-      int p = atomicAdd(&rc, 1);
+      const int p = atomicAdd(a.rraw + q, 1);
       if (p < a.RC) {
         a.rpairs[(size_t)q * a.RC + p] = make_int2(q, c);
         a.rdc[(size_t)q * a.RC + p] = v;  // pairwise measures re-use their FP32 values
       }
     }
   }
-  __syncthreads();
-  for (int p = rc + threadIdx.x; p < a.RC; p += kSelThreads)
-    a.rpairs[(size_t)q * a.RC + p] = make_int2(q, -1);
-  if (threadIdx.x == 0) a.rcnt[q] = min(rc, a.RC);
+}
+
+// pad the re-score set to RC entries, count its members (one thread/query)
+__global__ void rescore_pad_kernel(KArgs a) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= a.nq) return;
+  const int rc = min(a.rraw[q], a.RC);
+  for (int p = rc; p < a.RC; ++p) a.rpairs[(size_t)q * a.RC + p] = make_int2(q, -1);
+  a.rcnt[q] = rc;
 }
 
 // Bound on |compensated - FP64| relative to the value, for a path of P
@@ -1006,8 +1131,8 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
                          kind == DP_FRECHET_SQ || kind == DP_DTW_SQC || kind == DP_DTW_EUC ||
                          kind == DP_FRECHET_SQC;
   if (!diag_kind || a.rdiag == 0) return launch_dp(ctx, kind, G, R, d, a.max_clen);
-  TSIM_CUDA(cudaMemsetAsync(a.nspill, 0, sizeof(int), ctx->stream));
-  TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag, d, a.max_qlen, a.max_clen, a.spill, a.nspill));
+  TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag, d, a.max_clen, a.spill, a.nspill, a.spill2,
+                          a.nspill2));
   DpArgs sp = d;
   sp.order = a.spill;
   sp.npairs_dev = a.nspill;
@@ -1080,21 +1205,22 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
 
   stage_begin(ctx, TSIM_STAGE_FILTER);
   thresh_kernel<MEAS><<<(nq + 3) / 4, 128, 0, s>>>(a);
-  if (MEAS == M_DTW || MEAS == M_LCSS) {
-    qtable_global_kernel<<<nq, 256, 0, s>>>(a);
-    launched(ctx);
-  }
+  qtable_global_kernel<<<nq, 256, 0, s>>>(a);  // segment bounds of every measure
+  launched(ctx);
   compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
   launched(ctx, 2);
-  const int ch = std::max(1, std::min(64, (2 * ctx->num_sms * 4 + nq - 1) / nq));
+  // CTAs per query of the grid-stride filter kernels: about 8 per SM over the
+  // whole request, so a single query against a large database fills the GPU
+  const int ch = std::max(1, std::min(65535, (8 * ctx->num_sms + nq - 1) / nq));
   size_t lb2_smem = (MEAS == M_DTW || MEAS == M_LCSS) ? qtable_bytes(max_qlen) : 0;
   if (lb2_smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(lb2_kernel<MEAS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)lb2_smem));
   lb2_kernel<MEAS><<<dim3(ch, nq), kLb2Warps * 32, lb2_smem, s>>>(a);
+  seg_select_kernel<MEAS, 0><<<dim3(a.nseg, nq), kSelThreads, 0, s>>>(a, a.M);
   r1_select_kernel<MEAS><<<nq, kSelThreads, 0, s>>>(a);
   TSIM_CUDA(cudaGetLastError());
-  launched(ctx, 4);
+  launched(ctx, 5);
   stage_end(ctx);
 
   // round 1: the best survivors by bound, abandon against the seed threshold
@@ -1133,7 +1259,8 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   launched(ctx, 7);
   stage_end(ctx);
 
-  stage_begin(ctx, TSIM_STAGE_DP);
+  stage_begin(ctx, TSIM_STAGE_DP_SURVIVORS);
+  d.cells = ctx->dcounters + 1;  // counted apart: the survivor round's roofline
   d.pairs = a.flat;
   d.npairs = nq * a.C;
   d.npairs_dev = a.npairs;
@@ -1159,9 +1286,15 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   stage_end(ctx);
 
   stage_begin(ctx, TSIM_STAGE_SELECT);
+  seg_select_kernel<MEAS, 1><<<dim3(a.nseg, nq), kSelThreads, 0, s>>>(a, a.k);
   final_select_kernel<MEAS><<<nq, kSelThreads, 0, s>>>(a);
+  launched(ctx, 2);
+  if (MEAS != M_LCSS) {
+    rescore_collect_kernel<MEAS><<<dim3(a.nseg, nq), kSelThreads, 0, s>>>(a);
+    rescore_pad_kernel<<<(nq + 127) / 128, 128, 0, s>>>(a);
+    launched(ctx, 2);
+  }
   TSIM_CUDA(cudaGetLastError());
-  launched(ctx);
   stage_end(ctx);
   if (MEAS != M_LCSS) {
     stage_begin(ctx, TSIM_STAGE_RESCORE);
@@ -1298,6 +1431,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
   a.eps = p->epsilon;
   a.Cw = (C + 31) / 32;
   a.RC = std::min(256, std::max(4 * k, 64));
+  a.nseg = (a.S + a.M + C + kSeg - 1) / kSeg;
   a.force64 = (p->flags & TSIM_FLAG_FP64_RESCORE) ? 1 : 0;
   const size_t nqC = (size_t)nq * C;
   size_t need = align256(sizeof(float4) * nq) * 2 + align256(sizeof(int) * nq) +
@@ -1307,13 +1441,14 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
                 4 * align256(sizeof(int) * (nq + 1)) + 2 * align256(sizeof(int) * nqC) +
                 align256(sizeof(int) * 4) + align256(sizeof(int2) * nqC) +
                 align256(sizeof(float) * nqC) +
-                align256(sizeof(unsigned long long) * nq * (size_t)(a.S + C)) +
+                align256(sizeof(unsigned long long) * nq * (size_t)a.nseg * 64) +
+                align256(sizeof(unsigned long long) * nq) + align256(sizeof(int) * nq) +
                 2 * align256(sizeof(int2) * nq * a.RC) + 2 * align256(sizeof(double) * nq * a.RC) +
                 align256(sizeof(int) * nqC) + align256(sizeof(int) * kNumShapes) + 256 +
                 align256(sizeof(float) * nqC) + align256(sizeof(int2) * nq * a.M) +
                 align256(sizeof(float) * nq * a.M) + 2 * align256(sizeof(float) * (nq + 1)) +
                 align256(sizeof(float4) * (size_t)nq * a.tstride) +
-                align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 256;
+                2 * align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 2 * 256;
   return need;
 }
 
@@ -1329,6 +1464,7 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   TSIM_CHECK_ARG(db->count >= 1, "database is empty");
   KArgs a{};
   const size_t need = knn_plan(p, nq, max_qlen, db, a);
+  if (ctx->rdiag_override >= 0 && !a.plain && !a.noprune) a.rdiag = ctx->rdiag_override;
   TSIM_CHECK_ARG((size_t)a.nch * a.T * sizeof(unsigned long long) <= 200 * 1024,
                  "database too large for one request (seed selection)");
   a.qpts = qpts;
@@ -1365,7 +1501,9 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.npairs = arena_take<int>(ctx, 4);
   a.flat = arena_take<int2>(ctx, nqC);
   a.flat_vals = arena_take<float>(ctx, nqC);
-  a.fkeys = arena_take<unsigned long long>(ctx, (size_t)nq * (a.S + C));
+  a.segkeys = arena_take<unsigned long long>(ctx, (size_t)nq * a.nseg * 64);
+  a.kthkey = arena_take<unsigned long long>(ctx, nq);
+  a.rraw = arena_take<int>(ctx, nq);
   a.rpairs = arena_take<int2>(ctx, (size_t)nq * a.RC);
   a.r64 = arena_take<double>(ctx, (size_t)nq * a.RC);
   a.rdc = arena_take<double>(ctx, (size_t)nq * a.RC);
@@ -1379,6 +1517,8 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.qtab = arena_take<float4>(ctx, (size_t)nq * a.tstride);
   a.spill = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
   a.nspill = arena_take<int>(ctx, 4);
+  a.spill2 = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
+  a.nspill2 = arena_take<int>(ctx, 4);
   a.csegbox = db->segbox;
   a.order = arena_take<int>(ctx, nqC);
   a.shape_cnt = arena_take<int>(ctx, kNumShapes);
@@ -1410,11 +1550,17 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
 
 }  // namespace tsim
 
-static int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
-                       const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
-                       float* d_dists, double* d_dists64, tsim_stats* stats);
+using tsim::knn_request;
 
 namespace {
+
+// the autotuned choices a request of this shape would use (part of its graph key)
+uint64_t tuned_tag(tsim_ctx* ctx, const tsim_params* p, int nq, int max_qlen, const tsim_db* db) {
+  if (ctx->tuning.empty()) return 0;
+  auto it = ctx->tuning.find(tsim::tune_key(p, nq, max_qlen, db));
+  if (it == ctx->tuning.end()) return 0;
+  return 1 + (uint64_t)(it->second.rdiag + 1) * 64 + (uint64_t)it->second.streams;
+}
 
 std::vector<uint64_t> graph_key(tsim_ctx* ctx, const tsim_params* p, const void* qpts,
                                 const void* qoff, int nq, int max_qlen, const tsim_db* db,
@@ -1425,7 +1571,7 @@ std::vector<uint64_t> graph_key(tsim_ctx* ctx, const tsim_params* p, const void*
           eps, (uint64_t)(uint32_t)p->delta, p->flags, (uint64_t)nq, (uint64_t)max_qlen,
           (uint64_t)(uintptr_t)db, (uint64_t)db->count, (uint64_t)(uintptr_t)qpts,
           (uint64_t)(uintptr_t)qoff, (uint64_t)(uintptr_t)ids, (uint64_t)(uintptr_t)dists,
-          (uint64_t)(uintptr_t)d64, (uint64_t)ctx->concurrency};
+          (uint64_t)(uintptr_t)d64, (uint64_t)ctx->concurrency, tuned_tag(ctx, p, nq, max_qlen, db)};
 }
 
 std::vector<uint64_t> arena_gens(tsim_ctx* ctx) {
@@ -1511,9 +1657,23 @@ extern "C" int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d
   return TSIM_OK;
 }
 
-static int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
-                       const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
-                       float* d_dists, double* d_dists64, tsim_stats* stats) {
+namespace tsim {
+
+static int ceil_log2(long long v) {
+  int l = 0;
+  while ((1ll << l) < v) ++l;
+  return l;
+}
+
+std::vector<int> tune_key(const tsim_params* p, int nq, int max_qlen, const tsim_db* db) {
+  const bool dtw = p->measure == TSIM_DTW, lcss = p->measure == TSIM_LCSS;
+  return {p->measure, dtw ? p->cost : 0, dtw ? p->band_pct : -1, lcss ? p->delta : -1, p->k,
+          ceil_log2(max_qlen), ceil_log2(db->max_len), ceil_log2(db->count), ceil_log2(nq)};
+}
+
+int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
+                const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
+                float* d_dists, double* d_dists64, tsim_stats* stats) {
   TSIM_CHECK_ARG(ctx && p && db, "NULL ctx, params or database");
   TSIM_CHECK_ARG(nq >= 1 && max_qlen >= 1, "nq and max_qlen must be >= 1");
   TSIM_CHECK_ARG(d_qpts && d_qoff && d_ids && d_dists, "NULL device pointer");
@@ -1533,16 +1693,26 @@ static int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_
   const int64_t kMaxPairs = int64_t(1) << 24;
   constexpr int kMinChunk = 8;
   int qb = (int)std::max<int64_t>(1, std::min<int64_t>(nq, kMaxPairs / std::max(db->count, 1)));
-  int nstreams = std::min(ctx->concurrency, std::max(1, nq / kMinChunk));
+  int want = ctx->concurrency, rforce = -1;
+  if (!ctx->tuning.empty()) {  // autotuned choices for this shape class
+    auto it = ctx->tuning.find(tune_key(p, nq, max_qlen, db));
+    if (it != ctx->tuning.end()) {
+      if (it->second.streams > 0) want = it->second.streams;
+      rforce = it->second.rdiag;
+    }
+  }
+  int nstreams = std::min(want, std::max(1, nq / kMinChunk));
   if (p->flags & TSIM_FLAG_PLAIN) nstreams = 1;
   if (nstreams > 1) qb = std::min(qb, (nq + nstreams - 1) / nstreams);
   std::vector<tsim_ctx*> lanes{ctx};
+  ctx->rdiag_override = rforce;
   if (nstreams > 1) {
     TSIM_TRY(tsim::ensure_subs(ctx, nstreams));
     TSIM_CUDA(cudaEventRecord(ctx->fork_ev, ctx->stream));
     lanes.assign(ctx->subs.begin(), ctx->subs.begin() + nstreams);
     for (tsim_ctx* s : lanes) {
       s->profiling = ctx->profiling;
+      s->rdiag_override = rforce;
       TSIM_CUDA(cudaStreamWaitEvent(s->stream, ctx->fork_ev, 0));
     }
   }
@@ -1585,6 +1755,8 @@ static int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_
   }
   return TSIM_OK;
 }
+
+}  // namespace tsim
 
 extern "C" int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_point* h_qpts,
                              const int64_t* h_qoff, int nq, tsim_db* db, int* h_ids,
@@ -1696,11 +1868,12 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   if (kernel == 1 || (kernel == 0 && (!diag_kind || Rd == 0)) || !diag_kind)
     return launch_dp(ctx, kind, G, R, d, max_clen);
   if (Rd == 0) Rd = 4;  // forced: every pair spills to the striped kernel
-  TSIM_TRY(arena_reserve(ctx, align256(sizeof(int) * (size_t)npairs) + 256));
+  TSIM_TRY(arena_reserve(ctx, 2 * align256(sizeof(int) * (size_t)npairs) + 512));
   int* spill = arena_take<int>(ctx, npairs);
   int* nspill = arena_take<int>(ctx, 4);
-  TSIM_CUDA(cudaMemsetAsync(nspill, 0, sizeof(int), ctx->stream));
-  TSIM_TRY(launch_dp_diag(ctx, kind, Rd, d, max_qlen, max_clen, spill, nspill));
+  int* tmp = arena_take<int>(ctx, npairs);
+  int* ntmp = arena_take<int>(ctx, 4);
+  TSIM_TRY(launch_dp_diag(ctx, kind, Rd, d, max_clen, spill, nspill, tmp, ntmp));
   d.order = spill;
   d.npairs_dev = nspill;
   return launch_dp(ctx, kind, G, R, d, max_clen);

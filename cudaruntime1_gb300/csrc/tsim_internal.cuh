@@ -7,6 +7,7 @@
 #include <cfloat>
 #include <cmath>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/tsim.h"
@@ -91,6 +92,14 @@ struct tsim_ctx {
   };
   std::vector<GraphEntry> graphs;
   uint64_t arena_gen = 0;  // bumped whenever the arena is reallocated
+  // autotuned launch choices per request shape class (tune_key), and the
+  // rows per lane-group forced on the next knn() calls (-1: planner's)
+  struct TuneVal {
+    int rdiag = -1, streams = 0;
+    double ms = 0.0;
+  };
+  std::map<std::vector<int>, TuneVal> tuning;
+  int rdiag_override = -1;
   // databases created on this context; destroying the context releases their
   // device memory and detaches them (a later tsim_db_destroy only frees the
   // handle), so destruction order cannot cause a use-after-free
@@ -238,6 +247,12 @@ enum DpKind {
   DP_NUM_KINDS
 };
 
+// shape class of a request for the autotuner's table
+std::vector<int> tune_key(const tsim_params* p, int nq, int max_qlen, const tsim_db* db);
+// one kNN request on device pointers (chunked, on the context's streams)
+int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
+                const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
+                float* d_dists, double* d_dists64, tsim_stats* stats);
 // scratch bytes one knn() call carves from the arena
 size_t knn_scratch_bytes(const tsim_params* p, int nq, int max_qlen, const tsim_db* db);
 int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
@@ -270,10 +285,12 @@ int launch_pairwise64(tsim_ctx* ctx, int measure, const PwArgs& a);
 // G lanes per pair (4, 8, 16 or 32), R rows per lane (1, 2, 4 or 8).
 int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a, int max_m);
 // Anti-diagonal kernel (dp_diag.cu) for DTW/LCSS/Frechet FP32 and compensated
-// kinds, R rows per lane-group (1, 2 or 4); pairs it cannot take are appended
-// to spill[] (count in *nspill) for launch_dp.  max_n bounds the query length.
-int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_n, int max_m,
-                   int* spill, int* nspill);
+// kinds: passes with R, 2R, .. 4 rows per lane-group, each taking the pairs
+// the previous one could not; pairs no pass takes are left in spill[] (count
+// in *nspill) for launch_dp.  tmp/ntmp: a second list of the same size.
+// max_m bounds the candidate length (shared-memory staging).
+int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, int* spill,
+                   int* nspill, int* tmp, int* ntmp);
 bool diag_ok(bool lcss, int n, int m, int wd, int R);
 
 // choose (G, R) for pairs of shape n x m under band w

@@ -27,28 +27,22 @@ MEASURE_PARAMS = {
 
 
 def device_random_walks(count: int, lo: int, hi: int, seed: int, device="cuda"):
-    """``count`` random walks with lengths U[lo, hi] built on the device:
-    start uniform in [0,100]^2, N(0,1) steps per coordinate.  Returns
-    (points float32 [total, 2], offsets int64 [count+1], max_len) as torch
-    tensors on ``device``."""
+    """``count`` random walks with lengths U[lo, hi] (start uniform in
+    [0,100]^2, N(0,1) steps per coordinate), generated on the host with
+    numpy's seeded generator and copied to ``device``.  Returns (points
+    float32 [total, 2], offsets int64 [count+1], max_len) as torch tensors."""
     import torch
     rng = np.random.default_rng(seed)
     lens = rng.integers(lo, hi + 1, count).astype(np.int64)
     off = np.zeros(count + 1, np.int64)
     np.cumsum(lens, out=off[1:])
-    total = int(off[-1])
-    g = torch.Generator(device=device)
-    g.manual_seed(seed)
-    steps = torch.randn(total, 2, generator=g, device=device, dtype=torch.float32)
-    starts = torch.from_numpy(off[:-1]).to(device)
-    steps[starts] = 0.0
-    cs = torch.cumsum(steps.double(), dim=0)
+    steps = rng.standard_normal((int(off[-1]), 2), dtype=np.float32)
+    steps[off[:-1]] = 0.0
+    cs = np.cumsum(steps, axis=0, dtype=np.float64)
     del steps
-    owner = torch.repeat_interleave(torch.arange(count, device=device),
-                                    torch.from_numpy(lens).to(device))
-    origin = torch.rand(count, 2, generator=g, device=device, dtype=torch.float64) * 100.0
-    pts = (cs - cs[starts][owner] + origin[owner]).float().contiguous()
-    del cs, owner
+    origin = rng.random((count, 2)) * 100.0
+    cs -= np.repeat(cs[off[:-1]] - origin, lens, axis=0)
+    pts = torch.from_numpy(cs.astype(np.float32)).to(device)
     return pts, torch.from_numpy(off).to(device), int(lens.max())
 
 

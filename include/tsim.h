@@ -105,10 +105,11 @@ typedef enum tsim_stage {
   TSIM_STAGE_LB1,         /* O(1) bounds of all pairs */
   TSIM_STAGE_SEED,        /* seed selection + seed refinement */
   TSIM_STAGE_FILTER,      /* threshold, compaction, O(length) bounds, scan */
-  TSIM_STAGE_DP,          /* exact FP32 DP / distance of the survivors */
+  TSIM_STAGE_DP,          /* exact FP32 DP / distance of round 1 (best by bound) */
   TSIM_STAGE_SELECT,      /* k-th value and re-score set */
   TSIM_STAGE_RESCORE,     /* compensated / FP64 re-score and final sort */
   TSIM_STAGE_REF,         /* reference-semantics batch calls */
+  TSIM_STAGE_DP_SURVIVORS, /* exact FP32 DP of the pairs left after round 1 */
   TSIM_STAGE_COUNT
 } tsim_stage;
 
@@ -139,6 +140,9 @@ TSIM_API int tsim_ctx_counters(tsim_ctx* ctx, double* ms, int64_t* calls, int64_
  * and joined back to the context stream, so that latency-bound stages of
  * different chunks overlap.  1 runs everything on the context stream. */
 TSIM_API int tsim_ctx_set_concurrency(tsim_ctx* ctx, int streams);
+/* DP cells computed by the survivor round (TSIM_STAGE_DP_SURVIVORS) since the
+ * last counter reset (synchronises). */
+TSIM_API int tsim_ctx_survivor_cells(tsim_ctx* ctx, int64_t* cells);
 /* Measured FP32 FMA throughput of this GPU in TFLOP/s (a short probe kernel,
  * for roofline denominators). */
 TSIM_API int tsim_probe_fp32_tflops(tsim_ctx* ctx, double* tflops);
@@ -174,6 +178,30 @@ TSIM_API int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_q
 TSIM_API int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_point* h_qpts,
                            const int64_t* h_qoff, int nq, tsim_db* db, int* h_ids,
                            float* h_dists, tsim_stats* stats);
+
+/* ---- autotuner --------------------------------------------------------------
+ * Times the launch choices of the exact kNN path on the caller's request
+ * (rows per lane-group of the anti-diagonal DP: 1, 2, 4 or 0 = striped
+ * kernel only; concurrent query chunks: 1, 2, 4, 8) and records the fastest
+ * for the request's shape class (measure, cost, band, window, k, log2 of the
+ * longest query, the longest candidate, the database size and the query
+ * count).  Later tsim_knn calls of that class use it.  Results never depend
+ * on the choices.  The table is per context; save/load keep it in a text
+ * file tagged with the device name (loading a file of another device fails). */
+typedef struct tsim_tune_result {
+  int rdiag;         /* chosen rows per lane-group (0: striped kernel only, -1: n/a) */
+  int streams;       /* chosen concurrent query chunks */
+  double best_ms;    /* median time of the chosen configuration */
+  double default_ms; /* median time of the untuned defaults */
+  int tried;         /* configurations timed */
+} tsim_tune_result;
+TSIM_API int tsim_autotune(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
+                           const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int reps,
+                           tsim_tune_result* out);
+TSIM_API int tsim_tuning_save(tsim_ctx* ctx, const char* path);
+TSIM_API int tsim_tuning_load(tsim_ctx* ctx, const char* path);
+TSIM_API int tsim_tuning_clear(tsim_ctx* ctx);
+TSIM_API int tsim_tuning_count(const tsim_ctx* ctx);
 
 /* Device scratch one tsim_knn call of this shape takes (per query chunk;
  * the server admits requests against it). */
