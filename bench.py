@@ -441,12 +441,14 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(dev) as clk:
+        torch.cuda.nvtx.range_push("timed_steps")  # profilers capture this range alone
         for s, e in evs:
             flush.zero_()
             s.record(stream)
             step()
             e.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     step_ms = [s.elapsed_time(e) for s, e in evs]
     total_ms = sum(step_ms)
     cnt = ctx.counters(reset=True)

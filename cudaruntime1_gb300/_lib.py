@@ -111,6 +111,8 @@ def load(build_if_missing: bool = False):
             "tsim_db_create": ([_vp, _vp, _vp, C.c_int, C.POINTER(_vp)], C.c_int),
             "tsim_db_wrap_device": ([_vp, _vp, _vp, C.c_int, C.c_int, C.POINTER(_vp)], C.c_int),
             "tsim_db_destroy": ([_vp], C.c_int),
+            "tsim_db_save": ([_vp, C.c_char_p], C.c_int),
+            "tsim_db_load": ([_vp, C.c_char_p, C.POINTER(_vp)], C.c_int),
             "tsim_db_count": ([_vp], C.c_int),
             "tsim_db_device_bytes": ([_vp], C.c_int64),
             "tsim_knn": ([_vp, C.POINTER(TsimParams), _vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp,

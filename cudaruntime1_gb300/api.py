@@ -222,11 +222,14 @@ class Database:
     """Device-resident candidate set (CSR trajectories + summaries)."""
 
     def __init__(self, ctx: Context, pts=None, off=None, *, device_pts=None, device_off=None,
-                 count=None, max_len=0):
+                 count=None, max_len=0, path=None):
         self.ctx = ctx
         self.L = ctx.L
         h = C.c_void_p()
-        if device_pts is not None:
+        if path is not None:  # a file written by save()
+            check(self.L.tsim_db_load(ctx.h, str(path).encode(), C.byref(h)))
+            self._keep = None
+        elif device_pts is not None:
             check(self.L.tsim_db_wrap_device(ctx.h, C.c_void_p(device_pts),
                                              C.c_void_p(device_off), count, max_len, C.byref(h)))
             self._keep = None
@@ -243,6 +246,9 @@ class Database:
 
     def device_bytes(self) -> int:
         return self.L.tsim_db_device_bytes(self.h)
+
+    def save(self, path):
+        check(self.L.tsim_db_save(self.h, str(path).encode()))
 
     def close(self):
         if getattr(self, "h", None):

@@ -96,9 +96,10 @@ __global__ void summarize_kernel(const float2* __restrict__ pts, const int64_t* 
   }
 }
 
-// Segment boxes: warp per trajectory, lane s < kSegs reduces segment s.
+// Segment boxes and point sums: warp per trajectory, lane s < kSegs reduces
+// segment s (sums in FP64, rounded once to float).
 __global__ void segments_kernel(const float2* __restrict__ pts, const int64_t* __restrict__ off,
-                                int count, float4* __restrict__ segbox) {
+                                int count, float4* __restrict__ segbox, float2* __restrict__ segsum) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -108,14 +109,18 @@ __global__ void segments_kernel(const float2* __restrict__ pts, const int64_t* _
     const int m = (int)(off[t + 1] - b);
     const int s0 = (int)((long long)lane * m / kSegs), s1 = (int)((long long)(lane + 1) * m / kSegs);
     float x0 = TSIM_INF, y0 = TSIM_INF, x1 = -TSIM_INF, y1 = -TSIM_INF;
+    double sx = 0.0, sy = 0.0;
     for (int j = s0; j < s1; ++j) {
       const float2 p = pts[b + j];
       x0 = fminf(x0, p.x);
       x1 = fmaxf(x1, p.x);
       y0 = fminf(y0, p.y);
       y1 = fmaxf(y1, p.y);
+      sx += p.x;
+      sy += p.y;
     }
     segbox[(size_t)t * kSegs + lane] = make_float4(x0, y0, x1, y1);
+    segsum[(size_t)t * kSegs + lane] = make_float2((float)sx, (float)sy);
   }
 }
 
@@ -136,7 +141,8 @@ int db_summarize(tsim_db* db) {
   int blocks = std::min((db->count + 7) / 8, db->ctx->num_sms * 16);
   summarize_kernel<<<blocks, 256, 0, db->ctx->stream>>>(db->pts, db->off, db->count, db->box,
                                                          db->ends, db->len);
-  segments_kernel<<<blocks, 256, 0, db->ctx->stream>>>(db->pts, db->off, db->count, db->segbox);
+  segments_kernel<<<blocks, 256, 0, db->ctx->stream>>>(db->pts, db->off, db->count, db->segbox,
+                                                        db->segsum);
   TSIM_CUDA(cudaGetLastError());
   return TSIM_OK;
 }
@@ -430,6 +436,7 @@ int64_t tsim_ctx_scratch_bytes(const tsim_ctx* c) { return c ? (int64_t)c->arena
 
 static int db_alloc(tsim_db* db) {
   TSIM_CUDA(cudaMalloc(&db->segbox, sizeof(float4) * kSegs * std::max(db->count, 1)));
+  TSIM_CUDA(cudaMalloc(&db->segsum, sizeof(float2) * kSegs * std::max(db->count, 1)));
   TSIM_CUDA(cudaMalloc(&db->box, sizeof(float4) * std::max(db->count, 1)));
   TSIM_CUDA(cudaMalloc(&db->ends, sizeof(float4) * std::max(db->count, 1)));
   TSIM_CUDA(cudaMalloc(&db->len, sizeof(int) * std::max(db->count, 1)));
@@ -445,7 +452,9 @@ static void db_free(tsim_db* db) {
   cudaFree(db->ends);
   cudaFree(db->len);
   cudaFree(db->segbox);
+  cudaFree(db->segsum);
   db->segbox = nullptr;
+  db->segsum = nullptr;
   db->pts = nullptr;
   db->off = nullptr;
   db->box = db->ends = nullptr;
@@ -563,7 +572,7 @@ int tsim_db_count(const tsim_db* db) { return db ? db->count : 0; }
 int64_t tsim_db_device_bytes(const tsim_db* db) {
   if (!db) return 0;
   return (db->owns ? (int64_t)sizeof(float2) * db->total + 8 * (db->count + 1) : 0) +
-         (int64_t)db->count * (16 + 16 + 4 + 16 * kSegs);
+         (int64_t)db->count * (16 + 16 + 4 + (16 + 8) * kSegs);
 }
 
 }  // extern "C"

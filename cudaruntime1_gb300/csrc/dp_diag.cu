@@ -104,7 +104,8 @@ __device__ __forceinline__ Ramps make_ramps(int n, int m, int wd, bool lcss) {
 // compensated (two-float) values and for R = 4
 template <class P, int R>
 constexpr int diag_min_blocks() {
-  return sizeof(typename P::V) > 4        ? (R == 1 ? 8 : (R == 2 ? 6 : 4))
+  return R >= 8                             ? 1  // long unbanded rows: latency, not occupancy
+         : sizeof(typename P::V) > 4        ? (R == 1 ? 8 : (R == 2 ? 6 : 4))
          : std::is_same<P, PolDtwEu>::value ? (R == 1 ? 8 : (R == 2 ? 6 : 4))
                                             : (R <= 2 ? 8 : 5);
 }
@@ -239,7 +240,6 @@ __global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
         const int inext = t + 1 == ns ? i1 : i0;
         cnext = C[min(max(t + 1 - inext, 0), m - 1)];
       }
-      float mstep = TSIM_INF;
       // row r computes column t - i0 - r: its up neighbour is row r-1 one step
       // ago and its diagonal neighbour row r-1 two steps ago, so rows are
       // visited last to first before row r-1 is overwritten
@@ -251,15 +251,21 @@ __global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
         V v = P::cell(qx[r], qy[r], cw[r].x, cw[r].y, up, lf, dg, a.eps);
         const bool in = (unsigned)(t - base[r]) <= wdt[r];
         v = in ? v : P::masked(lf);
-        if (P::kMin) mstep = fminf(mstep, vf(v));  // masked cells are +inf
         left2[r] = lf;
         left[r] = v;
       }
       out = left[R - 1];
       if (P::kMin && a.thr) {
-        const float two = fminf(mstep, mprev);
+        // minimum of this anti-diagonal's cells (masked cells are +inf)
+        float mstep = vf(left[0]);
+        if (R == 2) mstep = fminf(mstep, vf(left[R > 1 ? 1 : 0]));
+        if (R == 4)
+          mstep = fminf(min3f(mstep, vf(left[R > 1 ? 1 : 0]), vf(left[R > 2 ? 2 : 0])),
+                        vf(left[R > 3 ? 3 : 0]));
+        const float prev = mprev;
         mprev = mstep;
         if ((t & 15) == 15) {
+          const float two = fminf(mstep, prev);
           const unsigned lb = __reduce_min_sync(0xffffffffu, __float_as_uint(two));
           if (__uint_as_float(lb) > thr) {  // uniform across the warp
             alive = false;
@@ -318,21 +324,27 @@ int launch_diag_one(tsim_ctx* ctx, const DpArgs& a, int max_m, int* spill, int* 
 
 template <class P>
 int launch_diag_r(tsim_ctx* ctx, int R, const DpArgs& a, int max_m, int* spill, int* nspill) {
+  constexpr int kTop = sizeof(typename P::V) > 4 ? 8 : 16;
   switch (R) {
     case 1: return launch_diag_one<P, 1>(ctx, a, max_m, spill, nspill);
     case 2: return launch_diag_one<P, 2>(ctx, a, max_m, spill, nspill);
-    default: return launch_diag_one<P, 4>(ctx, a, max_m, spill, nspill);
+    case 4: return launch_diag_one<P, 4>(ctx, a, max_m, spill, nspill);
+    case 8: return launch_diag_one<P, 8>(ctx, a, max_m, spill, nspill);
+    default: return launch_diag_one<P, kTop>(ctx, a, max_m, spill, nspill);
   }
 }
 
 template <class P>
 int launch_chain(tsim_ctx* ctx, int R0, const DpArgs& a, int max_m, int* spill, int* nspill,
                  int* tmp, int* ntmp) {
-  // R0, 2 R0, .., 4: each pass takes the pairs the previous one spilled, so
+  // R0, 2 R0, .., 16: each pass takes the pairs the previous one spilled, so
   // every pair runs with the fewest rows per lane-group its shape admits
-  // (fewer rows in flight, fewer masked cells); the last pass writes `spill`
+  // (fewer rows in flight, fewer masked cells); the last pass writes `spill`.
+  // R = 8 and 16 exist for full rows (no band) of up to 31 R + 1 columns.
+  // (two-float compensated values stop at 8: 16 rows of them exceed the registers)
+  const int rmax = sizeof(typename P::V) > 4 ? 8 : 16;
   std::vector<int> rs;
-  for (int R = std::max(1, R0); R <= 4; R *= 2) rs.push_back(R);
+  for (int R = std::max(1, R0); R <= rmax; R *= 2) rs.push_back(R);
   const int np = (int)rs.size();
   DpArgs in = a;
   for (int p = 0; p < np; ++p) {

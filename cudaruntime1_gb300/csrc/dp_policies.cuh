@@ -7,6 +7,14 @@
 namespace tsim {
 namespace dp {
 
+// min of three floats in one instruction (the three-operand PTX min.f32 of
+// sm_100+; exact, like two fminf, for the non-NaN values of a DP)
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // ---- cell policies ---------------------------------------------------------
 // V: value type; border(): value outside the matrix / band; origin(): D(-1,-1);
 // masked(left): value of a cell outside its row's band.
@@ -46,7 +54,7 @@ struct PolDtwSq {  // squared cost; FMA allowed, error bounded by the caller
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     float dx = qx - cx, dy = qy - cy;
     float c = fmaf(dy, dy, dx * dx);
-    return c + fminf(fminf(up, lf), dg);
+    return c + min3f(up, lf, dg);
   }
 };
 
@@ -59,7 +67,7 @@ struct PolDtwEu {
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     float dx = qx - cx, dy = qy - cy;
     float c = sqrtf(fmaf(dy, dy, dx * dx));
-    return c + fminf(fminf(up, lf), dg);
+    return c + min3f(up, lf, dg);
   }
 };
 
@@ -72,7 +80,7 @@ struct PolFrechetSq {  // squared domain; sqrt is applied once at the end
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     float dx = qx - cx, dy = qy - cy;
     float d2 = fmaf(dy, dy, dx * dx);
-    return fmaxf(d2, fminf(fminf(up, lf), dg));
+    return fmaxf(d2, min3f(up, lf, dg));
   }
 };
 

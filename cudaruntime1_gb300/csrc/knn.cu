@@ -97,6 +97,8 @@ struct KArgs {
   float* thr2;              // [nq]  threshold after round 1
   int* fcnt;                // [nq]  round-2 pairs per query (in list1)
   const float4* csegbox;    // [C*kSegs] candidate segment boxes
+  const float2* csegsum;    // [C*kSegs] sums of the candidate segments' points
+  double2* qpre;            // [nq*(max_qlen+1)] query prefix sums (FP64)
   int* spill;               // pairs the anti-diagonal kernel leaves to the striped one
   int* nspill;
   int* spill2;              // the list between passes of the anti-diagonal kernel
@@ -378,14 +380,45 @@ __device__ __forceinline__ QTable qtable_view(float4* t, int n) {
   return T;
 }
 
-// one CTA per query: its sparse table in global memory (read by the
-// segment bound of every pair of the query)
-__global__ void qtable_global_kernel(KArgs a) {
+// one CTA per query: its sparse table and its FP64 prefix sums in global
+// memory (read by the segment bounds of every pair of the query)
+__global__ void qtable_global_kernel(KArgs a, int sums) {
+  __shared__ double2 part[256];
   const int q = blockIdx.x;
   const int n = a.qlen[q];
   if (n <= 0 || n > a.max_qlen) return;
+  const float2* A = a.qpts + a.qoff[q];
   QTable T;
-  qtable_build(T, a.qpts + a.qoff[q], n, a.qtab + (size_t)q * a.tstride);
+  qtable_build(T, A, n, a.qtab + (size_t)q * a.tstride);
+  if (!sums) return;  // prefix sums: lock-step Euclidean only
+  // prefix sums P[j] = sum of points 0 .. j-1, j = 0 .. n: a chunk per thread
+  double2* P = a.qpre + (size_t)q * (a.max_qlen + 1);
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int j0 = min(n, (int)threadIdx.x * per), j1 = min(n, j0 + per);
+  double sx = 0.0, sy = 0.0;
+  for (int j = j0; j < j1; ++j) {
+    sx += A[j].x;
+    sy += A[j].y;
+  }
+  part[threadIdx.x] = make_double2(sx, sy);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double rx = 0.0, ry = 0.0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      const double2 v = part[i];
+      part[i] = make_double2(rx, ry);
+      rx += v.x;
+      ry += v.y;
+    }
+    P[n] = make_double2(rx, ry);
+  }
+  __syncthreads();
+  double rx = part[threadIdx.x].x, ry = part[threadIdx.x].y;
+  for (int j = j0; j < j1; ++j) {
+    P[j] = make_double2(rx, ry);
+    rx += A[j].x;
+    ry += A[j].y;
+  }
 }
 
 // Segment bound of one pair: every column of candidate segment s lies in the
@@ -427,15 +460,34 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
   const float4 qb = a.qbox[q];
   const QTable T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
   if (MEAS == M_EUCLID) {
-    // lock-step: column j meets row j only, so segment s of the candidate
-    // costs at least its box's distance to the box of the same query rows
+    // lock-step: column j meets row j only, so segment s (L points) costs at
+    // least L times its box's squared distance to the box of the same query
+    // rows, and at least |sum of the query's points - sum of the candidate's|^2
+    // / L per coordinate (Cauchy-Schwarz); the larger of the two per segment
     if (n < m) return TSIM_INF;
+    const float2* ss = a.csegsum + (size_t)c * kSegs;
+    const double2* P = a.qpre + (size_t)q * (a.max_qlen + 1);
     float acc = 0.0f;
-    for (int s = 0; s < kSegs; ++s) {
+    for (int s = 0; s < kSegs && acc <= t; ++s) {
       const int b0 = seg_first(s, m), b1 = seg_first(s + 1, m) - 1;
       if (b1 < b0) continue;
+      const float L = (float)(b1 - b0 + 1);
       const float d = box_box_d2_rd(qtable_box(T, b0, b1), sb[s]);
-      acc = __fadd_rd(acc, __fmul_rd((float)(b1 - b0 + 1), d));
+      const float2 sc = ss[s];
+      const double2 p1 = P[b1 + 1], p0 = P[b0];
+      // error margins: the candidate sum's float rounding and the rounding of
+      // the difference to float (each <= 2^-24 relative; 4x slack), and the
+      // FP64 prefix sums' accumulated rounding (<= (n+1) 2^-53 of their size)
+      const float dx = fabsf((float)(p1.x - p0.x - (double)sc.x));
+      const float dy = fabsf((float)(p1.y - p0.y - (double)sc.y));
+      const float pe = (float)(n + 1) * (1.0f / 2251799813685248.0f);  // (n+1) 2^-51
+      const float ex = __fadd_ru(__fmul_ru(fabsf(sc.x) + dx, 1.0f / 4194304.0f),
+                                 __fmul_ru(fabsf((float)p1.x) + fabsf((float)p0.x), pe));
+      const float ey = __fadd_ru(__fmul_ru(fabsf(sc.y) + dy, 1.0f / 4194304.0f),
+                                 __fmul_ru(fabsf((float)p1.y) + fabsf((float)p0.y), pe));
+      const float ax = fmaxf(0.0f, __fsub_rd(dx, ex)), ay = fmaxf(0.0f, __fsub_rd(dy, ey));
+      const float cs = __fdiv_rd(__fadd_rd(__fmul_rd(ax, ax), __fmul_rd(ay, ay)), L);
+      acc = __fadd_rd(acc, fmaxf(__fmul_rd(L, d), cs));
     }
     return fmaxf(acc, lb1);
   }
@@ -560,6 +612,9 @@ __global__ void __launch_bounds__(kChunk) compact_kernel(KArgs a) {
     if (pass) {  // the segment bound, only for pairs the O(1) bound keeps
       const float sbnd = seg_bound<MEAS>(a, q, c, a.qlen[q], a.clen[c], b, t);
       pass = MEAS == M_LCSS ? (sbnd >= t) : (sbnd <= t);
+      // kept in place of the O(1) bound: the O(length) stage and the round-1
+      // order use the tighter of it and their own bound
+      if (pass) a.lb1[(size_t)q * a.C + c] = sbnd;
     }
   }
   const unsigned ball = __ballot_sync(0xffffffffu, pass);
@@ -596,12 +651,12 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
     const float2* B = a.cpts + a.coff[c];
     const int m = a.clen[c];
     bool pass;
-    float lbv = MEAS == M_LCSS ? (float)min(n, m) : 0.0f;  // the bound (no bound: trivial)
+    const float sbnd = a.lb1[(size_t)q * a.C + c];  // the segment bound of stage A
+    float lbv = sbnd;  // the bound (no O(length) bound: stage A's)
     if (n <= 0 || m <= 0) {
       pass = false;
     } else if (MEAS == M_EUCLID) {
       // no O(length) bound: the exact sum costs the same
-      lbv = a.lb1[(size_t)q * a.C + c];
       pass = true;
     } else if (kTable && !use_table) {
       pass = true;
@@ -659,8 +714,8 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
       }
       for (int o = 16; o; o >>= 1) acc = __fadd_rd(acc, __shfl_xor_sync(0xffffffffu, acc, o));
       feasible = __all_sync(0xffffffffu, feasible);
-      pass = feasible && acc <= t;
-      lbv = feasible ? acc : TSIM_INF;
+      lbv = feasible ? fmaxf(acc, sbnd) : TSIM_INF;
+      pass = lbv <= t;
     } else if (MEAS == M_FRECHET || MEAS == M_HAUSDORFF) {
       // every point of either trajectory is coupled to (Frechet) or has a
       // nearest point in (Hausdorff) the other, so the squared distance is
@@ -676,8 +731,8 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
         mx = fmaxf(mx, box_pt_d2_rd(cb.x, cb.y, cb.z, cb.w, p.x, p.y));
       }
       for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      pass = mx <= t;
-      lbv = mx;
+      lbv = fmaxf(mx, sbnd);
+      pass = lbv <= t;
     } else {
       // LCSS: candidate points that can match some query point of their
       // window (rows [j-delta, j+delta]) inside the eps-inflated box
@@ -696,7 +751,7 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
           ++count;
       }
       for (int o = 16; o; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
-      lbv = (float)min(count, min(n, m));
+      lbv = fminf((float)min(count, min(n, m)), sbnd);  // an upper bound on the count
       pass = lbv >= t;
     }
     if (pass && lane == 0) {
@@ -1205,7 +1260,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
 
   stage_begin(ctx, TSIM_STAGE_FILTER);
   thresh_kernel<MEAS><<<(nq + 3) / 4, 128, 0, s>>>(a);
-  qtable_global_kernel<<<nq, 256, 0, s>>>(a);  // segment bounds of every measure
+  qtable_global_kernel<<<nq, 256, 0, s>>>(a, MEAS == M_EUCLID);  // segment bounds
   launched(ctx);
   compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
   launched(ctx, 2);
@@ -1448,6 +1503,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
                 align256(sizeof(float) * nqC) + align256(sizeof(int2) * nq * a.M) +
                 align256(sizeof(float) * nq * a.M) + 2 * align256(sizeof(float) * (nq + 1)) +
                 align256(sizeof(float4) * (size_t)nq * a.tstride) +
+                align256(sizeof(double2) * (size_t)nq * (max_qlen + 1)) +
                 2 * align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 2 * 256;
   return need;
 }
@@ -1515,11 +1571,13 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.thr2 = arena_take<float>(ctx, nq + 1);
   a.fcnt = arena_take<int>(ctx, nq + 1);
   a.qtab = arena_take<float4>(ctx, (size_t)nq * a.tstride);
+  a.qpre = arena_take<double2>(ctx, (size_t)nq * (max_qlen + 1));
   a.spill = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
   a.nspill = arena_take<int>(ctx, 4);
   a.spill2 = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
   a.nspill2 = arena_take<int>(ctx, 4);
   a.csegbox = db->segbox;
+  a.csegsum = db->segsum;
   a.order = arena_take<int>(ctx, nqC);
   a.shape_cnt = arena_take<int>(ctx, kNumShapes);
   if (!a.shape_cnt) return fail(TSIM_ERR_OUT_OF_MEMORY, "knn scratch carve failed");

@@ -42,8 +42,9 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
     if (_s != TSIM_OK) return _s; \
   } while (0)
 
-// Candidate trajectories carry the bounding boxes of kSegs consecutive
-// column segments: segment s covers columns [s*m/kSegs, (s+1)*m/kSegs).
+// Candidate trajectories carry the bounding boxes and point sums of kSegs
+// consecutive column segments: segment s covers columns [s*m/kSegs,
+// (s+1)*m/kSegs).  At most 32 (one lane per segment builds them).
 constexpr int kSegs = 8;
 
 // ---------------------------------------------------------------------------
@@ -118,6 +119,7 @@ struct tsim_db {
   float4* ends = nullptr;     // device [count] (first.x, first.y, last.x, last.y)
   int* len = nullptr;         // device [count]
   float4* segbox = nullptr;   // device [count * kSegs]: boxes of kSegs equal column segments
+  float2* segsum = nullptr;   // device [count * kSegs]: sums of those segments' points
   std::vector<int64_t> h_off; // host copy of offsets (lengths for scheduling)
 };
 

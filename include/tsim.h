@@ -157,6 +157,12 @@ TSIM_API int tsim_db_create(tsim_ctx* ctx, const tsim_point* host_pts, const int
 TSIM_API int tsim_db_wrap_device(tsim_ctx* ctx, const tsim_point* dev_pts,
                                  const int64_t* dev_off, int count, int max_len, tsim_db** out);
 TSIM_API int tsim_db_destroy(tsim_db* db);
+/* On-disk form of a database: points, offsets and the resident summaries in
+ * one flat little-endian file with a checksum; loading copies it straight
+ * into device memory (no summary rebuild).  Corrupt, truncated or foreign
+ * files are refused. */
+TSIM_API int tsim_db_save(const tsim_db* db, const char* path);
+TSIM_API int tsim_db_load(tsim_ctx* ctx, const char* path, tsim_db** out);
 TSIM_API int tsim_db_count(const tsim_db* db);
 TSIM_API int64_t tsim_db_device_bytes(const tsim_db* db);
 

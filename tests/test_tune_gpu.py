@@ -49,3 +49,4 @@ def test_autotune_keeps_results_and_round_trips(tsim, tmp_path, measure, kw):
         ctx.load_tuning(bad)
     db.close()
     ctx.close()
+
