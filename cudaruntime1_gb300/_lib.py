@@ -21,7 +21,7 @@ TSIM_ERR_BUDGET, TSIM_PENDING, TSIM_ERR_BUSY = 6, 7, 8
 
 DTW, LCSS, FRECHET, HAUSDORFF, EUCLIDEAN = range(5)
 COST_SQEUCLID, COST_EUCLID = 0, 1
-FLAG_NO_PRUNE, FLAG_PLAIN, FLAG_NO_GRAPH, FLAG_FP64_RESCORE = 1, 2, 4, 8
+FLAG_NO_PRUNE, FLAG_PLAIN, FLAG_NO_GRAPH, FLAG_FP64_RESCORE, FLAG_ALWAYS_PRUNE = 1, 2, 4, 8, 16
 STAGES = ["summary", "lb1", "seed", "filter", "dp", "select", "rescore", "ref", "dp_survivors"]
 
 _vp = C.c_void_p

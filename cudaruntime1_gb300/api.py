@@ -18,7 +18,8 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import (COST_EUCLID, COST_SQEUCLID, DTW, EUCLIDEAN, FLAG_FP64_RESCORE,  # noqa: F401
+from ._lib import (COST_EUCLID, COST_SQEUCLID, DTW, EUCLIDEAN, FLAG_ALWAYS_PRUNE,  # noqa: F401
+                   FLAG_FP64_RESCORE,
                    FLAG_NO_GRAPH, FLAG_NO_PRUNE, FLAG_PLAIN, FRECHET, HAUSDORFF, LCSS,
                    TSIM_PENDING, TsimParams, TsimRequestInfo, TsimServerOpts, TsimServerStats,
                    TsimStats, check)

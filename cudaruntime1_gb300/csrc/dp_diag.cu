@@ -256,12 +256,13 @@ __global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
       }
       out = left[R - 1];
       if (P::kMin && a.thr) {
-        // minimum of this anti-diagonal's cells (masked cells are +inf)
+        // minimum of this anti-diagonal's cells, all R rows (masked cells are
+        // +inf): three-operand mins, then a last two-operand one if needed
         float mstep = vf(left[0]);
-        if (R == 2) mstep = fminf(mstep, vf(left[R > 1 ? 1 : 0]));
-        if (R == 4)
-          mstep = fminf(min3f(mstep, vf(left[R > 1 ? 1 : 0]), vf(left[R > 2 ? 2 : 0])),
-                        vf(left[R > 3 ? 3 : 0]));
+        int r = 1;
+#pragma unroll
+        for (; r + 1 < R; r += 2) mstep = min3f(mstep, vf(left[r]), vf(left[r + 1]));
+        if (r < R) mstep = fminf(mstep, vf(left[r < R ? r : 0]));
         const float prev = mprev;
         mprev = mstep;
         if ((t & 15) == 15) {
@@ -324,13 +325,12 @@ int launch_diag_one(tsim_ctx* ctx, const DpArgs& a, int max_m, int* spill, int* 
 
 template <class P>
 int launch_diag_r(tsim_ctx* ctx, int R, const DpArgs& a, int max_m, int* spill, int* nspill) {
-  constexpr int kTop = sizeof(typename P::V) > 4 ? 8 : 16;
   switch (R) {
     case 1: return launch_diag_one<P, 1>(ctx, a, max_m, spill, nspill);
     case 2: return launch_diag_one<P, 2>(ctx, a, max_m, spill, nspill);
     case 4: return launch_diag_one<P, 4>(ctx, a, max_m, spill, nspill);
     case 8: return launch_diag_one<P, 8>(ctx, a, max_m, spill, nspill);
-    default: return launch_diag_one<P, kTop>(ctx, a, max_m, spill, nspill);
+    default: return launch_diag_one<P, 16>(ctx, a, max_m, spill, nspill);
   }
 }
 
@@ -341,10 +341,8 @@ int launch_chain(tsim_ctx* ctx, int R0, const DpArgs& a, int max_m, int* spill, 
   // every pair runs with the fewest rows per lane-group its shape admits
   // (fewer rows in flight, fewer masked cells); the last pass writes `spill`.
   // R = 8 and 16 exist for full rows (no band) of up to 31 R + 1 columns.
-  // (two-float compensated values stop at 8: 16 rows of them exceed the registers)
-  const int rmax = sizeof(typename P::V) > 4 ? 8 : 16;
   std::vector<int> rs;
-  for (int R = std::max(1, R0); R <= rmax; R *= 2) rs.push_back(R);
+  for (int R = std::max(1, std::min(R0, 16)); R <= 16; R *= 2) rs.push_back(R);
   const int np = (int)rs.size();
   DpArgs in = a;
   for (int p = 0; p < np; ++p) {

@@ -50,6 +50,10 @@ enum Meas { M_DTW = 0, M_LCSS = 1, M_FRECHET = 2, M_HAUSDORFF = 3, M_EUCLID = 4 
 
 // measures refined by the wavefront DP (the others by pairwise kernels)
 constexpr bool is_dp(int meas) { return meas <= M_FRECHET; }
+// re-score set ordered by compensated values (DTW: an FP32 path sum's error
+// grows with the path); the others' FP32 value is one rounded cost (Frechet,
+// Hausdorff) or a compensated sum (Euclidean) and is used as it is
+constexpr bool compensated_rescore(int meas) { return meas == M_DTW; }
 // values carried in the squared domain (sqrt applied to the reported distance)
 constexpr bool is_squared(int meas) { return meas >= M_FRECHET; }
 
@@ -73,6 +77,7 @@ struct KArgs {
   // parameters
   int k, S, T, nch;
   int plain;    // one DP pair per kernel launch (the unbatched comparison form)
+  int brute;    // small request: every pair refined exactly, no bound stages
   int noprune;  // thresholds stay open: every pair is refined
   int cost;  // DTW: 0 squared, 1 Euclidean
   int band_pct;
@@ -189,6 +194,19 @@ __device__ __forceinline__ float bound1(const KArgs& a, float4 qb, float4 qe, in
   return __fadd_rd(__fadd_rd(first, last), __fmul_rd((float)(L - 2), bb));
 }
 
+// Order in which candidates are tried as seeds (lower first).  Any order
+// gives a valid threshold -- the seeds' exact values -- but a good one gives
+// a tight threshold.  Distance measures use their O(1) bound; the LCSS bound
+// (min(n, m) unless the eps-inflated boxes are disjoint) hardly ranks, so
+// LCSS tries the candidates whose end points lie nearest the query's first.
+template <int MEAS>
+__device__ __forceinline__ float seed_score(float b, const float4& qe, const float4& ce) {
+  if (MEAS != M_LCSS) return b;
+  if (b <= 0.0f) return TSIM_INF;  // no match possible
+  const float d0x = qe.x - ce.x, d0y = qe.y - ce.y, d1x = qe.z - ce.z, d1y = qe.w - ce.w;
+  return d0x * d0x + d0y * d0y + d1x * d1x + d1y * d1y;
+}
+
 template <int MEAS>
 __global__ void __launch_bounds__(kChunk) lb1_kernel(KArgs a) {
   __shared__ unsigned long long keys[kChunk];
@@ -200,9 +218,10 @@ __global__ void __launch_bounds__(kChunk) lb1_kernel(KArgs a) {
   const int n = a.qlen[q];
   unsigned long long key = ~0ull;
   if (c < a.C) {
-    float b = bound1<MEAS>(a, qb, qe, n, a.cbox[c], a.cends[c], a.clen[c]);
+    const float4 ce = a.cends[c];
+    float b = bound1<MEAS>(a, qb, qe, n, a.cbox[c], ce, a.clen[c]);
     a.lb1[(size_t)q * a.C + c] = b;
-    key = pack_key(MEAS == M_LCSS ? -b : b, threadIdx.x);
+    key = pack_key(seed_score<MEAS>(b, qe, ce), threadIdx.x);
   }
   keys[threadIdx.x] = key;
   __syncthreads();
@@ -230,7 +249,7 @@ __global__ void __launch_bounds__(kSelThreads) seed_kernel(KArgs a) {
     unsigned long long key = ~0ull;
     if (c >= 0) {
       float b = a.lb1[(size_t)q * a.C + c];
-      key = pack_key(MEAS == M_LCSS ? -b : b, c);
+      key = pack_key(seed_score<MEAS>(b, a.qends[q], a.cends[c]), c);
     }
     keys[i] = key;
   }
@@ -1064,9 +1083,9 @@ __global__ void cluster_kernel(KArgs a) {
   const int2* rp = a.rpairs + (size_t)q * a.RC;
   const double* rv = a.rdc + (size_t)q * a.RC;
   int2* r64p = a.r64pairs + (size_t)q * a.RC;
-  // compensated DP values: gamma_c; FP32 pairwise values: twice their bound
-  const double g = is_dp(MEAS) ? gamma_c(MEAS, a.qlen[q] + a.max_clen)
-                               : 2.0 * gamma_dp(MEAS, a.qlen[q], a.max_clen);
+  // compensated DTW values: gamma_c; FP32 values: twice their bound
+  const double g = compensated_rescore(MEAS) ? gamma_c(MEAS, a.qlen[q] + a.max_clen)
+                                             : 2.0 * gamma_dp(MEAS, a.qlen[q], a.max_clen);
   unsigned char ord[256];
   int n = 0;
   for (int i = 0; i < cnt && i < 256; ++i) {
@@ -1174,7 +1193,8 @@ __global__ void stats_kernel(KArgs a, unsigned long long* counters, int with_res
     atomicAdd(counters + 5, rc);
   }
   if (threadIdx.x == 0) {
-    atomicAdd(counters + 4, (unsigned long long)(*a.npairs) + (unsigned long long)a.nq * (a.S + a.M));
+    atomicAdd(counters + 4, (unsigned long long)(*a.npairs) +
+                                (a.brute ? 0ull : (unsigned long long)a.nq * (a.S + a.M)));
     if (with_rescore) atomicAdd(counters + 6, (unsigned long long)(*a.n64));
   }
 }
@@ -1203,8 +1223,119 @@ int refine32(tsim_ctx* ctx, const KArgs& a, int dp32, int G, int R, const DpArgs
   return launch_pairwise(ctx, MEAS == M_HAUSDORFF ? TSIM_HAUSDORFF : TSIM_EUCLIDEAN, p);
 }
 
+// Stage E (shared by the pruned and the brute-force pipelines): k-th value,
+// re-score set, compensated / FP64 re-score, final order, counters.
+template <int MEAS>
+int finish_knn(tsim_ctx* ctx, KArgs& a, int dpc, int dp64) {
+  cudaStream_t s = ctx->stream;
+  const int nq = a.nq;
+  DpArgs d{};
+  d.band_pct = MEAS == M_DTW ? a.band_pct : -1;
+  stage_begin(ctx, TSIM_STAGE_SELECT);
+  seg_select_kernel<MEAS, 1><<<dim3(a.nseg, nq), kSelThreads, 0, s>>>(a, a.k);
+  final_select_kernel<MEAS><<<nq, kSelThreads, 0, s>>>(a);
+  launched(ctx, 2);
+  if (MEAS != M_LCSS) {
+    rescore_collect_kernel<MEAS><<<dim3(a.nseg, nq), kSelThreads, 0, s>>>(a);
+    rescore_pad_kernel<<<(nq + 127) / 128, 128, 0, s>>>(a);
+    launched(ctx, 2);
+  }
+  TSIM_CUDA(cudaGetLastError());
+  stage_end(ctx);
+  if (MEAS != M_LCSS) {
+    stage_begin(ctx, TSIM_STAGE_RESCORE);
+    DpArgs r{};
+    r.qpts = a.qpts;
+    r.qoff = a.qoff;
+    r.cpts = a.cpts;
+    r.coff = a.coff;
+    r.pairs = a.rpairs;
+    r.npairs = nq * a.RC;
+    r.out64 = a.rdc;
+    r.band_pct = d.band_pct;
+    r.delta = -1;
+    // compensated FP32 re-score of the set, then FP64 only for the pairs it
+    // cannot order (near-ties within the compensated error bound)
+    if (compensated_rescore(MEAS)) TSIM_TRY(run_dp(ctx, a, dpc, 32, 1, r));
+    cluster_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+    r.pairs = a.r64pairs;
+    r.out64 = a.r64;
+    if (is_dp(MEAS)) {
+      TSIM_TRY(launch_dp(ctx, dp64, 32, 1, r, a.max_clen));
+    } else {
+      PwArgs p{a.qpts, a.qoff, a.cpts, a.coff, a.r64pairs, nq * a.RC, nullptr, nullptr, nullptr,
+               a.r64, nullptr};
+      TSIM_TRY(launch_pairwise64(ctx, MEAS == M_HAUSDORFF ? TSIM_HAUSDORFF : TSIM_EUCLIDEAN, p));
+    }
+    final_sort_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+    TSIM_CUDA(cudaGetLastError());
+    launched(ctx, 2);
+    stage_end(ctx);
+  }
+  stats_kernel<<<1, 256, 0, s>>>(a, ctx->dcounters, MEAS != M_LCSS ? 1 : 0);
+  TSIM_CUDA(cudaGetLastError());
+  launched(ctx);
+  return TSIM_OK;
+}
+
+// Every pair of a small request refined exactly: the bound stages cost more
+// (a chain of dependent launches) than they save.  Seeds and round 1 are
+// left empty; the flat list holds all pairs, query by query.
+__global__ void brute_setup_kernel(KArgs a) {
+  const size_t np = (size_t)a.nq * a.C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < np;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int q = (int)(i / a.C), c = (int)(i % a.C);
+    a.flat[i] = make_int2(q, c);
+    if (c == 0) {
+      a.off2[q] = q * a.C;
+      a.fcnt[q] = a.C;
+      a.cnt1[q] = a.C;
+      a.cnt2[q] = a.C;
+      a.rcnt[q] = 0;
+      for (int k = 0; k < a.S; ++k) a.seeds[(size_t)q * a.S + k] = make_int2(q, -1);
+      for (int k = 0; k < a.M; ++k) a.r1pairs[(size_t)q * a.M + k] = make_int2(q, -1);
+    }
+    if (i == 0) *a.npairs = (int)np;
+  }
+}
+
+template <int MEAS>
+int run_brute(tsim_ctx* ctx, KArgs& a, int dp32, int dpc, int dp64) {
+  cudaStream_t s = ctx->stream;
+  const int nq = a.nq;
+  const size_t np = (size_t)nq * a.C;
+  TSIM_CUDA(cudaMemsetAsync(a.n64, 0, sizeof(int), s));
+  stage_begin(ctx, TSIM_STAGE_FILTER);
+  brute_setup_kernel<<<(unsigned)std::min<size_t>((np + 255) / 256, 4096), 256, 0, s>>>(a);
+  TSIM_CUDA(cudaGetLastError());
+  launched(ctx);
+  stage_end(ctx);
+  stage_begin(ctx, TSIM_STAGE_DP_SURVIVORS);
+  DpArgs d{};
+  d.qpts = a.qpts;
+  d.qoff = a.qoff;
+  d.cpts = a.cpts;
+  d.coff = a.coff;
+  d.band_pct = MEAS == M_DTW ? a.band_pct : -1;
+  d.delta = a.delta;
+  d.eps = a.eps;
+  d.cells = ctx->dcounters + 1;
+  d.pairs = a.flat;
+  d.npairs = (int)np;
+  d.out = a.flat_vals;
+  int G, R;
+  const int wd = MEAS == M_LCSS ? a.delta : band_w(a.max_qlen, a.max_clen, d.band_pct);
+  dp_shape(dp32, a.max_qlen, a.max_clen, wd, G, R);
+  TSIM_TRY(refine32<MEAS>(ctx, a, dp32, G, R, d));
+  stage_end(ctx);
+  return finish_knn<MEAS>(ctx, a, dpc, dp64);
+}
+
 template <int MEAS>
 int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, tsim_stats* st) {
+  (void)st;
+  if (a.brute) return run_brute<MEAS>(ctx, a, dp32, dpc, dp64);
   cudaStream_t s = ctx->stream;
   const int nq = a.nq;
   dim3 g1(a.nch, nq);
@@ -1340,52 +1471,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   }
   stage_end(ctx);
 
-  stage_begin(ctx, TSIM_STAGE_SELECT);
-  seg_select_kernel<MEAS, 1><<<dim3(a.nseg, nq), kSelThreads, 0, s>>>(a, a.k);
-  final_select_kernel<MEAS><<<nq, kSelThreads, 0, s>>>(a);
-  launched(ctx, 2);
-  if (MEAS != M_LCSS) {
-    rescore_collect_kernel<MEAS><<<dim3(a.nseg, nq), kSelThreads, 0, s>>>(a);
-    rescore_pad_kernel<<<(nq + 127) / 128, 128, 0, s>>>(a);
-    launched(ctx, 2);
-  }
-  TSIM_CUDA(cudaGetLastError());
-  stage_end(ctx);
-  if (MEAS != M_LCSS) {
-    stage_begin(ctx, TSIM_STAGE_RESCORE);
-    DpArgs r{};
-    r.qpts = a.qpts;
-    r.qoff = a.qoff;
-    r.cpts = a.cpts;
-    r.coff = a.coff;
-    r.pairs = a.rpairs;
-    r.npairs = nq * a.RC;
-    r.out64 = a.rdc;
-    r.band_pct = d.band_pct;
-    r.delta = -1;
-    // compensated FP32 re-score of the set, then FP64 only for the pairs it
-    // cannot order (near-ties within the compensated error bound)
-    if (is_dp(MEAS)) TSIM_TRY(run_dp(ctx, a, dpc, 32, 1, r));
-    cluster_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
-    r.pairs = a.r64pairs;
-    r.out64 = a.r64;
-    if (is_dp(MEAS)) {
-      TSIM_TRY(launch_dp(ctx, dp64, 32, 1, r, a.max_clen));
-    } else {
-      PwArgs p{a.qpts, a.qoff, a.cpts, a.coff, a.r64pairs, nq * a.RC, nullptr, nullptr, nullptr,
-               a.r64, nullptr};
-      TSIM_TRY(launch_pairwise64(ctx, MEAS == M_HAUSDORFF ? TSIM_HAUSDORFF : TSIM_EUCLIDEAN, p));
-    }
-    final_sort_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
-    TSIM_CUDA(cudaGetLastError());
-    launched(ctx, 2);
-    stage_end(ctx);
-  }
-  stats_kernel<<<1, 256, 0, s>>>(a, ctx->dcounters, MEAS != M_LCSS ? 1 : 0);
-  TSIM_CUDA(cudaGetLastError());
-  launched(ctx);
-  (void)st;
-  return TSIM_OK;
+  return finish_knn<MEAS>(ctx, a, dpc, dp64);
 }
 
 // Band cells of every (query, candidate) pair: sum over rows of the row's
@@ -1464,6 +1550,15 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
   a.plain = (p->flags & TSIM_FLAG_PLAIN) ? 1 : 0;
   a.noprune = (p->flags & TSIM_FLAG_NO_PRUNE) ? 1 : 0;
   {
+    // small requests skip the bound stages: their dependent launches cost
+    // more than computing every pair (cells or point pairs, upper bound)
+    const double pairs = (double)nq * C;
+    const double work = pairs * (p->measure == TSIM_EUCLIDEAN ? (double)db->max_len
+                                                              : (double)max_qlen * db->max_len);
+    const bool small = pairs <= 65536.0 && work <= 2.5e8 && !(p->flags & TSIM_FLAG_ALWAYS_PRUNE);
+    a.brute = !a.plain && (a.noprune || small) ? 1 : 0;
+  }
+  {
     // rows per lane-group of the anti-diagonal kernel: the smallest R whose
     // validity condition holds for every pair shape.  2 w(max(n,m)) (min(n,m)-1)
     // / (n+m-2) grows with both lengths, so the longest query against the
@@ -1472,8 +1567,8 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
     const int n = max_qlen, m = db->max_len;
     const int wd = p->measure == TSIM_LCSS ? p->delta
                                            : (p->measure == TSIM_DTW ? band_w(n, m, p->band_pct) : -1);
-    a.rdiag = 0;
-    for (int R : {1, 2, 4})
+    a.rdiag = 16;  // none fits the worst case: the widest still takes the shorter pairs
+    for (int R : {1, 2, 4, 8, 16})
       if (diag_ok(p->measure == TSIM_LCSS, n, m, wd, R)) {
         a.rdiag = R;
         break;
@@ -1915,7 +2010,7 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   d.eps = p->epsilon;
   const int wd = p->measure == TSIM_LCSS ? p->delta : band_w(max_qlen, max_clen, d.band_pct);
   int Rd = 0;
-  for (int R : {1, 2, 4})
+  for (int R : {1, 2, 4, 8, 16})
     if (diag_ok(p->measure == TSIM_LCSS, max_qlen, max_clen, wd, R)) {
       Rd = R;
       break;
@@ -1925,7 +2020,7 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   const bool diag_kind = precision < 2;
   if (kernel == 1 || (kernel == 0 && (!diag_kind || Rd == 0)) || !diag_kind)
     return launch_dp(ctx, kind, G, R, d, max_clen);
-  if (Rd == 0) Rd = 4;  // forced: every pair spills to the striped kernel
+  if (Rd == 0) Rd = 16;  // none fits the longest pair: the widest takes the rest
   TSIM_TRY(arena_reserve(ctx, 2 * align256(sizeof(int) * (size_t)npairs) + 512));
   int* spill = arena_take<int>(ctx, npairs);
   int* nspill = arena_take<int>(ctx, 4);

@@ -1,8 +1,8 @@
 // tune.cu -- the autotuner: launch choices of the exact kNN path picked by
 // measurement on this GPU, per request shape class.
 //
-// Two choices are tuned: the rows per lane-group R of the anti-diagonal DP
-// (1, 2 or 4; 0 runs every pair on the round-striped kernel) and the number
+// Two choices are tuned: the first rows per lane-group R of the anti-diagonal
+// DP's passes (1 .. 16; 0 runs every pair on the round-striped kernel) and the number
 // of query chunks a request runs concurrently on child streams (1, 2, 4, 8).
 // tsim_autotune times every admissible pair of choices on the caller's own
 // request (device pointers, CUDA events on the context stream, the median of
@@ -35,14 +35,14 @@ std::string device_name(int dev) {
 }
 
 // smallest R whose anti-diagonal validity condition holds for the longest
-// query against the longest candidate (0: none)
+// query against the longest candidate (16 when none does)
 int min_rdiag(const tsim_params* p, int max_qlen, const tsim_db* db) {
   const int n = max_qlen, m = db->max_len;
   const int wd = p->measure == TSIM_LCSS ? p->delta
                                          : (p->measure == TSIM_DTW ? band_w(n, m, p->band_pct) : -1);
-  for (int R : {1, 2, 4})
+  for (int R : {1, 2, 4, 8, 16})
     if (diag_ok(p->measure == TSIM_LCSS, n, m, wd, R)) return R;
-  return 0;
+  return 16;
 }
 
 }  // namespace
@@ -66,8 +66,8 @@ extern "C" int tsim_autotune(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
   const bool dp = p->measure == TSIM_DTW || p->measure == TSIM_LCSS || p->measure == TSIM_FRECHET;
   if (dp) {
     const int r0 = min_rdiag(p, max_qlen, db);
-    for (int R : {1, 2, 4})
-      if (r0 > 0 ? R >= r0 : R == 4) rs.push_back(R);
+    for (int R : {1, 2, 4, 8, 16})
+      if (R >= r0 && R <= 4 * r0) rs.push_back(R);
   }
   std::vector<int> ss;
   for (int s : {1, 2, 4, 8})
@@ -198,7 +198,7 @@ extern "C" int tsim_tuning_load(tsim_ctx* ctx, const char* path) {
                            &key[3], &key[4], &key[5], &key[6], &key[7], &key[8], &v.rdiag,
                            &v.streams, &v.ms);
     if (got == EOF || (got == 0 && strspn(line, " \t\r\n") == strlen(line))) continue;
-    if (got != 12 || v.rdiag < -1 || v.rdiag > 4 || v.streams < 1 || v.streams > 64) {
+    if (got != 12 || v.rdiag < -1 || v.rdiag > 16 || v.streams < 1 || v.streams > 64) {
       st = fail(TSIM_ERR_INVALID_ARG, std::string("malformed tuning line: ") + line);
       break;
     }

@@ -74,6 +74,8 @@ typedef enum tsim_cost {
 #define TSIM_FLAG_NO_GRAPH 0x4u /* do not replay through a captured CUDA graph */
 #define TSIM_FLAG_FP64_RESCORE 0x8u /* re-score every top-k pair in FP64: distances
                                        bit-identical to an FP64 evaluation */
+#define TSIM_FLAG_ALWAYS_PRUNE 0x10u /* run the bound stages even for requests small
+                                        enough to refine every pair (the default) */
 
 typedef struct tsim_params {
   int measure;    /* tsim_measure */
@@ -172,8 +174,10 @@ TSIM_API int64_t tsim_db_device_bytes(const tsim_db* db);
 TSIM_API int tsim_band_cells(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
                              const int64_t* d_qoff, int nq, tsim_db* db, int64_t* cells);
 /* Device pointers; results d_ids[nq*k], d_dists[nq*k] (float), d_dists64
- * optional (may be NULL): the compensated FP32 value (relative error below
- * ~1e-10 of FP64), or the FP64 value for near-tied pairs and with
+ * optional (may be NULL): DTW's compensated FP32 value (FP32 cell costs, path
+ * sum compensated: within 4 2^-24 + O(P 2^-48) relative of FP64); Frechet's
+ * and Hausdorff's FP32 value (one rounded cost, within 8 2^-24); Euclidean's compensated FP32 sum (or FP64 beyond 1024
+ * points); the FP64 value for near-tied pairs and with
  * TSIM_FLAG_FP64_RESCORE.  Ids are exact in every case.  LCSS distances are
  * the integer match counts.  Asynchronous on the context stream unless stats
  * is non-NULL (then the call synchronises to fill it). */
@@ -187,8 +191,8 @@ TSIM_API int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_point
 
 /* ---- autotuner --------------------------------------------------------------
  * Times the launch choices of the exact kNN path on the caller's request
- * (rows per lane-group of the anti-diagonal DP: 1, 2, 4 or 0 = striped
- * kernel only; concurrent query chunks: 1, 2, 4, 8) and records the fastest
+ * (first rows per lane-group of the anti-diagonal DP's passes: 1 .. 16, or
+ * 0 = striped kernel only; concurrent query chunks: 1, 2, 4, 8) and records the fastest
  * for the request's shape class (measure, cost, band, window, k, log2 of the
  * longest query, the longest candidate, the database size and the query
  * count).  Later tsim_knn calls of that class use it.  Results never depend

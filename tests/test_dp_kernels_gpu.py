@@ -39,6 +39,10 @@ CASES = [
     ("frechet", dict(), 20, 90),
     ("lcss", dict(epsilon=1.0, delta=5), 10, 150),
     ("lcss", dict(epsilon=0.5, delta=-1), 2, 28),
+    # full rows past 31*4+1 columns: anti-diagonal passes with R = 8 and 16
+    ("dtw", dict(band_pct=-1, cost=0), 130, 480),
+    ("frechet", dict(), 130, 240),
+    ("lcss", dict(epsilon=0.5, delta=200), 130, 300),
 ]
 
 

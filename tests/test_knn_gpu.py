@@ -43,8 +43,9 @@ CASES = [
 ]
 
 
+@pytest.mark.parametrize("pruned", [False, True])
 @pytest.mark.parametrize("measure,kw", CASES)
-def test_knn_matches_fp64_oracle(tsim, cuda_ctx, oracle, measure, kw):
+def test_knn_matches_fp64_oracle(tsim, cuda_ctx, oracle, measure, kw, pruned):
     cp, co = _db(700, 16, 120, 100)
     ql = G.uniform_lengths(9, 16, 120, 7)
     qp, qo = G.random_walks(9, ql, 8)
@@ -54,6 +55,8 @@ def test_knn_matches_fp64_oracle(tsim, cuda_ctx, oracle, measure, kw):
     if "epsilon" in okw:
         okw["eps"] = okw.pop("epsilon")
     want_ids, want_d = oracle.knn(measure, qp, qo, cp, co, k, **okw)
+    if pruned:  # the bound stages, which a request this small skips by default
+        kw = dict(kw, flags=tsim.api.FLAG_ALWAYS_PRUNE)
     ids, d, d64, st = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, k, **kw)
     assert np.array_equal(ids, want_ids), (ids, want_ids)
     if measure == "lcss":
@@ -63,13 +66,14 @@ def test_knn_matches_fp64_oracle(tsim, cuda_ctx, oracle, measure, kw):
         assert np.array_equal(np.isfinite(d64), fin)
         rel = np.abs(d.astype(np.float64)[fin] - want_d[fin]) / np.maximum(want_d[fin], 1e-30)
         assert rel.max() <= REL_TOL
-        # compensated DP re-score: double-float accuracy against FP64;
-        # pairwise measures report their FP32 values (FP64 only for near-ties)
+        # DTW's compensated re-score (FP32 costs within 4 2^-24, path sum
+        # compensated) and the other measures' FP32 values (FP64 only for
+        # near-ties) are all within a few 2^-24 of FP64
         rel64 = np.abs(d64[fin] - want_d[fin]) / np.maximum(want_d[fin], 1e-30)
-        assert rel64.max() <= (1e-9 if measure == "frechet" else 1e-6), rel64.max()
+        assert rel64.max() <= 1e-6, rel64.max()
         # forced FP64 re-score: bit-identical to the FP64 oracle
-        ids2, _, d64b, st2 = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, k,
-                                         flags=tsim.api.FLAG_FP64_RESCORE, **kw)
+        kw64 = dict(kw, flags=kw.get("flags", 0) | tsim.api.FLAG_FP64_RESCORE)
+        ids2, _, d64b, st2 = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, k, **kw64)
         assert np.array_equal(ids2, want_ids)
         assert np.array_equal(d64b, want_d)
         assert st2["rescored_fp64"] >= np.isfinite(want_d).sum()
@@ -183,7 +187,8 @@ def test_pruning_never_changes_the_answer(tsim, cuda_ctx, measure, kw):
     cp, co = _db(1500, 20, 90, 1200)
     qp, qo = G.random_walks(6, G.uniform_lengths(6, 20, 90, 1201), 1202)
     db = tsim.Database(cuda_ctx, cp, co)
-    ids, d, _, st = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 10, **kw)
+    ids, d, _, st = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 10,
+                                flags=tsim.api.FLAG_ALWAYS_PRUNE, **kw)
     ids2, d2, _, st2 = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 10,
                                    flags=tsim.api.FLAG_NO_PRUNE, **kw)
     assert np.array_equal(ids, ids2) and np.array_equal(d, d2)
@@ -223,4 +228,20 @@ def test_graph_replay_follows_inputs(tsim, cuda_ctx, oracle):
     want2, _ = oracle.knn("dtw", qp2, qo, cp, co, k, band_pct=10)
     assert np.array_equal(ids.cpu().numpy().reshape(24, k), want2)
     cuda_ctx.set_stream(None)
+    db.close()
+
+
+@pytest.mark.parametrize("measure,kw", [("dtw", dict(band_pct=-1, cost=0)), ("frechet", dict())])
+def test_knn_full_rows_long_candidates(tsim, cuda_ctx, oracle, measure, kw):
+    """Full-row DP of candidates longer than 31*4+1 points: anti-diagonal
+    passes with 8 and 16 rows per lane-group, with early abandon."""
+    cp, co = _db(600, 130, 480, 300)
+    ql = G.uniform_lengths(6, 130, 480, 301)
+    qp, qo = G.random_walks(6, ql, 302)
+    db = tsim.Database(cuda_ctx, cp, co)
+    want_ids, want_d = oracle.knn(measure, qp, qo, cp, co, 10, **kw)
+    ids, d, d64, st = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 10, **kw)
+    assert np.array_equal(ids, want_ids)
+    rel = np.abs(d.astype(np.float64) - want_d) / np.maximum(want_d, 1e-30)
+    assert rel.max() <= REL_TOL
     db.close()
