@@ -35,17 +35,20 @@ namespace {
 using namespace dp;
 
 constexpr int kDiagThreads = 128;
-constexpr int kMaxStagedCols = 768;  // candidate points staged per warp (6 KiB)
+constexpr int kMaxStagedCols = 768;      // candidate points staged per warp (6 KiB)
+constexpr int kCtaWarps = 8;             // warps of a CTA-per-pair launch
+constexpr int kMaxStagedColsCta = 4096;  // candidate points staged per CTA (32 KiB)
 constexpr int kNone = 1 << 30;
 
 }  // namespace
 
-__host__ __device__ bool diag_ok(bool lcss, int n, int m, int wd, int R) {
+__host__ __device__ bool diag_ok(bool lcss, int n, int m, int wd, int R, int lanes) {
   if (n < 2 || m < 2) return false;
-  if (wd < 0) return m <= 31 * R + 1;
-  if (lcss) return wd <= 31 * R;
+  const long long span = (long long)(lanes - 1) * R;  // rows between a lane's groups, less one group
+  if (wd < 0) return m <= span + 1;
+  if (lcss) return wd <= span;
   const long long W = (long long)wd * ((n < m ? n : m) - 1);
-  return 2 * W < 31ll * R * (n + m - 2);
+  return 2 * W < span * (n + m - 2);
 }
 
 namespace {
@@ -110,20 +113,29 @@ constexpr int diag_min_blocks() {
                                             : (R <= 2 ? 8 : 5);
 }
 
-template <class P, int R>
-__global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
+// W warps per pair: 1 (a warp per pair, kDiagThreads per CTA) or kCtaWarps
+// (a CTA per pair: its 32 W lanes share the rows, the row above a warp's
+// first lane crosses warps through shared memory once per step)
+template <class P, int R, int W>
+__global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
+                                  (W == 1 ? diag_min_blocks<P, R>() : 1))
     dp_diag_kernel(DpArgs a, int col_cap, int* spill, int* nspill) {
   using V = typename P::V;
   extern __shared__ __align__(16) float2 diag_cand[];
+  __shared__ V xbuf[2][W];  // W > 1: last lane's value of each warp, by step parity
+  __shared__ float xred[W];  // W > 1: each warp's abandon bound
   constexpr bool kLcss = !P::kMin;
-  constexpr int kRound = 32 * R;  // rows between two groups of one lane
+  constexpr int kLanes = 32 * W;     // lanes per pair
+  constexpr int kRound = kLanes * R;  // rows between two groups of one lane
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int warp = threadIdx.x >> 5;
+  const int pl = W == 1 ? lane : (int)threadIdx.x;  // lane within the pair
+  const int slot = W == 1 ? (blockIdx.x * blockDim.x + threadIdx.x) >> 5 : blockIdx.x;
+  const int nslots = W == 1 ? (gridDim.x * blockDim.x) >> 5 : gridDim.x;
   const int npairs = a.npairs_dev ? min(*a.npairs_dev, a.npairs) : a.npairs;
-  float2* cs = diag_cand + (size_t)(threadIdx.x >> 5) * col_cap;  // this warp's candidate
+  float2* cs = diag_cand + (W == 1 ? (size_t)warp * col_cap : 0);  // this pair's candidate
 
-  for (int wk = gw; wk < npairs; wk += nw) {
+  for (int wk = slot; wk < npairs; wk += nslots) {
     const int pid = a.order ? a.order[wk] : wk;
     const int2 pr = a.pairs[pid];
     if (pr.y < 0) continue;
@@ -137,20 +149,20 @@ __global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
     const bool staged = m <= col_cap;
     const int w = band_w(n, m, a.band_pct);
     const int wd = kLcss ? a.delta : w;
-    if (!diag_ok(kLcss, n, m, wd, R)) {
-      if (lane == 0 && spill) spill[atomicAdd(nspill, 1)] = pid;
+    if (!diag_ok(kLcss, n, m, wd, R, kLanes)) {
+      if (pl == 0 && spill) spill[atomicAdd(nspill, 1)] = pid;
       continue;
     }
     const float thr = a.thr ? a.thr[q] : TSIM_INF;
     const int rrow = result_row<P>(n, m, a.delta);
-    if (lane == 0) store_result(a, pid, P::border());
+    if (pl == 0) store_result(a, pid, P::border());
 
     const Ramps rp = make_ramps(n, m, wd, kLcss);
     const int row_q = (int)(rp.a / rp.d), row_r = (int)(rp.a % rp.d);
     const int rnd_q = (int)(kRound * rp.a / rp.d), rnd_r = (int)(kRound * rp.a % rp.d);
 
     // the lane's next group (first row i1, its band ramps, prefetched points)
-    int i1 = R * lane;
+    int i1 = R * pl;
     Ramp L1 = rp.lo_at(i1), H1 = rp.hi_at(i1);
     float nqx[R], nqy[R];
 #pragma unroll
@@ -196,10 +208,18 @@ __global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
       return hi >= lo ? i1 + lo : 0x7fffffff;
     };
     int ns = take_next();
-    __syncwarp();
-    if (staged)
-      for (int j = lane; j < m; j += 32) cs[j] = __ldg(B + j);
-    __syncwarp();
+    if (W == 1) {
+      __syncwarp();
+      if (staged)
+        for (int j = lane; j < m; j += 32) cs[j] = __ldg(B + j);
+      __syncwarp();
+    } else {
+      __syncthreads();  // the previous pair is done with the staging and the exchange
+      if (staged)
+        for (int j = pl; j < m; j += kLanes) cs[j] = __ldg(B + j);
+      if (lane == 31) xbuf[0][warp] = xbuf[1][warp] = P::border();
+      __syncthreads();
+    }
     const float2* C = staged ? cs : B;
     V out = P::border();
     V prev_raw = P::border();  // the shuffled value of the previous step
@@ -228,8 +248,9 @@ __global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
       // the last row of the previous lane's group, one column back: the row
       // above this lane's first row (lane 0's first group reads the virtual
       // row -1 instead, whose only finite cell is D(-1,-1) = origin)
-      const V raw = shfl_lane(out, (lane + 31) & 31);
-      const bool first = lane == 0 && i0 == 0;
+      V raw = shfl_lane(out, (lane + 31) & 31);
+      if (W > 1 && lane == 0) raw = xbuf[(t + 1) & 1][(warp + W - 1) % W];  // the previous warp's
+      const bool first = pl == 0 && i0 == 0;
       const V up_in = first ? P::border() : raw;
       const V dg_in = first ? (t == 0 ? P::origin() : P::border()) : prev_raw;
       prev_raw = raw;
@@ -267,13 +288,25 @@ __global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
         mprev = mstep;
         if ((t & 15) == 15) {
           const float two = fminf(mstep, prev);
-          const unsigned lb = __reduce_min_sync(0xffffffffu, __float_as_uint(two));
-          if (__uint_as_float(lb) > thr) {  // uniform across the warp
+          float lb = __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(two)));
+          if (W > 1) {  // over the pair's warps (reads after this step's barrier)
+            if (lane == 0) xred[warp] = lb;
+            if (lane == 31) xbuf[t & 1][warp] = out;
+            __syncthreads();
+#pragma unroll
+            for (int w2 = 0; w2 < W; ++w2) lb = fminf(lb, xred[w2]);
+          }
+          if (lb > thr) {  // uniform across the pair
             alive = false;
             t_ab = t;
             break;
           }
+          if (W > 1) continue;  // this step's exchange and barrier are done
         }
+      }
+      if (W > 1) {  // hand the last lane's value to the next warp
+        if (lane == 31) xbuf[t & 1][warp] = out;
+        __syncthreads();
       }
     }
 #pragma unroll
@@ -285,9 +318,9 @@ __global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
     if (a.cells) {  // cells of the anti-diagonals 0 .. t_ab inside the band
       const Ramps rp = make_ramps(n, m, kLcss ? a.delta : band_w(n, m, a.band_pct), kLcss);
       long long cells = 0;
-      const int q32 = (int)(32 * rp.a / rp.d), r32 = (int)(32 * rp.a % rp.d);
-      Ramp L = rp.lo_at(lane), H = rp.hi_at(lane);
-      for (int i = lane; i < n; i += 32) {
+      const int q32 = (int)(kLanes * rp.a / rp.d), r32 = (int)(kLanes * rp.a % rp.d);
+      Ramp L = rp.lo_at(pl), H = rp.hi_at(pl);
+      for (int i = pl; i < n; i += kLanes) {
         const int lo = rp.lo(L), hi = min(rp.hi(H), t_ab - i);
         if (hi >= lo) cells += hi - lo + 1;
         rp.step(L, q32, r32);
@@ -296,53 +329,60 @@ __global__ void __launch_bounds__(kDiagThreads, (diag_min_blocks<P, R>()))
       for (int o = 16; o; o >>= 1) cells += __shfl_xor_sync(0xffffffffu, cells, o);
       if (lane == 0) atomicAdd(a.cells, (unsigned long long)cells);
     }
-    __syncwarp();
+    if (W == 1) __syncwarp(); else __syncthreads();
     if (holds) store_result(a, pid, alive ? result : P::border());
-    if (!alive && lane == 0) store_result(a, pid, P::border());
-    __syncwarp();
+    if (!alive && pl == 0) store_result(a, pid, P::border());
+    if (W == 1) __syncwarp(); else __syncthreads();
   }
 }
 
-template <class P, int R>
+template <class P, int R, int W>
 int launch_diag_one(tsim_ctx* ctx, const DpArgs& a, int max_m, int* spill, int* nspill) {
   if (a.npairs <= 0) return TSIM_OK;
-  const int warps = kDiagThreads / 32;
-  const int col_cap = (std::min(max_m, kMaxStagedCols) + 1) & ~1;
-  const size_t smem = (size_t)warps * col_cap * sizeof(float2);
-  auto kern = dp_diag_kernel<P, R>;
+  const int threads = W == 1 ? kDiagThreads : 32 * W;
+  const int pairs_per_cta = W == 1 ? kDiagThreads / 32 : 1;
+  const int col_cap = (std::min(max_m, W == 1 ? kMaxStagedCols : kMaxStagedColsCta) + 1) & ~1;
+  const size_t smem = (size_t)pairs_per_cta * col_cap * sizeof(float2);
+  auto kern = dp_diag_kernel<P, R, W>;
   if (smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  TSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kDiagThreads, smem));
-  long long blocks = std::min<long long>((a.npairs + warps - 1) / warps,
+  TSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+  long long blocks = std::min<long long>((a.npairs + pairs_per_cta - 1) / pairs_per_cta,
                                          (long long)std::max(per_sm, 1) * ctx->num_sms);
-  kern<<<(unsigned)std::max(blocks, 1ll), kDiagThreads, smem, ctx->stream>>>(a, col_cap, spill,
-                                                                            nspill);
+  kern<<<(unsigned)std::max(blocks, 1ll), threads, smem, ctx->stream>>>(a, col_cap, spill, nspill);
   TSIM_CUDA(cudaGetLastError());
   launched(ctx);
   return TSIM_OK;
 }
 
-template <class P>
+template <class P, int W>
 int launch_diag_r(tsim_ctx* ctx, int R, const DpArgs& a, int max_m, int* spill, int* nspill) {
   switch (R) {
-    case 1: return launch_diag_one<P, 1>(ctx, a, max_m, spill, nspill);
-    case 2: return launch_diag_one<P, 2>(ctx, a, max_m, spill, nspill);
-    case 4: return launch_diag_one<P, 4>(ctx, a, max_m, spill, nspill);
-    case 8: return launch_diag_one<P, 8>(ctx, a, max_m, spill, nspill);
-    default: return launch_diag_one<P, 16>(ctx, a, max_m, spill, nspill);
+    case 1: return launch_diag_one<P, 1, W>(ctx, a, max_m, spill, nspill);
+    case 2: return launch_diag_one<P, 2, W>(ctx, a, max_m, spill, nspill);
+    case 4: return launch_diag_one<P, 4, W>(ctx, a, max_m, spill, nspill);
+    case 8:
+      if (W == 1) return launch_diag_one<P, 8, 1>(ctx, a, max_m, spill, nspill);
+      break;
+    default:
+      if (W == 1) return launch_diag_one<P, 16, 1>(ctx, a, max_m, spill, nspill);
+      break;
   }
+  return fail(TSIM_ERR_UNSUPPORTED, "no CTA-per-pair kernel with this many rows per lane");
 }
 
 template <class P>
-int launch_chain(tsim_ctx* ctx, int R0, const DpArgs& a, int max_m, int* spill, int* nspill,
-                 int* tmp, int* ntmp) {
-  // R0, 2 R0, .., 16: each pass takes the pairs the previous one spilled, so
+int launch_chain(tsim_ctx* ctx, int R0, int warps, const DpArgs& a, int max_m, int* spill,
+                 int* nspill, int* tmp, int* ntmp) {
+  // R0, 2 R0, .. Rmax: each pass takes the pairs the previous one spilled, so
   // every pair runs with the fewest rows per lane-group its shape admits
   // (fewer rows in flight, fewer masked cells); the last pass writes `spill`.
-  // R = 8 and 16 exist for full rows (no band) of up to 31 R + 1 columns.
+  // A warp per pair goes to R = 16 (full rows of up to 497 columns), a CTA
+  // per pair to R = 4 (1021 columns).
+  const int rmax = warps == 1 ? 16 : 4;
   std::vector<int> rs;
-  for (int R = std::max(1, std::min(R0, 16)); R <= 16; R *= 2) rs.push_back(R);
+  for (int R = std::max(1, std::min(R0, rmax)); R <= rmax; R *= 2) rs.push_back(R);
   const int np = (int)rs.size();
   DpArgs in = a;
   for (int p = 0; p < np; ++p) {
@@ -350,7 +390,10 @@ int launch_chain(tsim_ctx* ctx, int R0, const DpArgs& a, int max_m, int* spill, 
     int* out = to_spill ? spill : tmp;
     int* nout = to_spill ? nspill : ntmp;
     TSIM_CUDA(cudaMemsetAsync(nout, 0, sizeof(int), ctx->stream));
-    TSIM_TRY(launch_diag_r<P>(ctx, rs[p], in, max_m, out, nout));
+    if (warps == 1)
+      TSIM_TRY((launch_diag_r<P, 1>(ctx, rs[p], in, max_m, out, nout)));
+    else
+      TSIM_TRY((launch_diag_r<P, kCtaWarps>(ctx, rs[p], in, max_m, out, nout)));
     in.order = out;
     in.npairs_dev = nout;
   }
@@ -360,16 +403,18 @@ int launch_chain(tsim_ctx* ctx, int R0, const DpArgs& a, int max_m, int* spill, 
 }  // namespace
 
 int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, int* spill,
-                   int* nspill, int* tmp, int* ntmp) {
+                   int* nspill, int* tmp, int* ntmp, int warps) {
+  const int W = warps > 1 ? kCtaWarps : 1;
   switch (kind) {
-    case DP_DTW_SQ: return launch_chain<PolDtwSq>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
-    case DP_DTW_EU: return launch_chain<PolDtwEu>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
-    case DP_LCSS: return launch_chain<PolLcss>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
-    case DP_FRECHET_SQ: return launch_chain<PolFrechetSq>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
-    case DP_DTW_SQC: return launch_chain<PolDtwSqC>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
-    case DP_DTW_EUC: return launch_chain<PolDtwEuC>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_SQ: return launch_chain<PolDtwSq>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_EU: return launch_chain<PolDtwEu>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_LCSS: return launch_chain<PolLcss>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_FRECHET_SQ:
+      return launch_chain<PolFrechetSq>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_SQC: return launch_chain<PolDtwSqC>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_EUC: return launch_chain<PolDtwEuC>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
     case DP_FRECHET_SQC:
-      return launch_chain<PolFrechetSqC>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
+      return launch_chain<PolFrechetSqC>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
   }
   return fail(TSIM_ERR_UNSUPPORTED, "no anti-diagonal kernel for this DP kind");
 }

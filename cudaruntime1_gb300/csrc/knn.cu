@@ -109,6 +109,7 @@ struct KArgs {
   int* spill2;              // the list between passes of the anti-diagonal kernel
   int* nspill2;
   int rdiag;                // rows per lane-group of the anti-diagonal kernel (0: off)
+  int rdiag_cta;            // the same for a CTA per pair (0: no R fits the longest pair)
   float4* qtab;             // [nq*tstride] query sparse tables (global memory)
   int tstride;
   int* off2;                // [nq+1]
@@ -1201,13 +1202,22 @@ __global__ void stats_kernel(KArgs a, unsigned long long* counters, int with_res
 
 // DP of a pair list: the anti-diagonal kernel for the pairs it can take,
 // the round-striped kernel (G lanes x R rows) for the rest
-int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& d) {
+// latency: a round of few pairs (seeds, round 1, re-score), whose launch
+// lasts as long as its longest pair.  When a warp per pair would need 8 or
+// more rows per lane (long full rows) such a round runs a CTA per pair.
+int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& d,
+           bool latency = false) {
   const bool diag_kind = kind == DP_DTW_SQ || kind == DP_DTW_EU || kind == DP_LCSS ||
                          kind == DP_FRECHET_SQ || kind == DP_DTW_SQC || kind == DP_DTW_EUC ||
                          kind == DP_FRECHET_SQC;
   if (!diag_kind || a.rdiag == 0) return launch_dp(ctx, kind, G, R, d, a.max_clen);
-  TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag, d, a.max_clen, a.spill, a.nspill, a.spill2,
-                          a.nspill2));
+  if (latency && a.rdiag >= 8 && a.rdiag_cta > 0) {
+    TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag_cta, d, a.max_clen, a.spill, a.nspill, a.spill2,
+                            a.nspill2, 8));
+  } else {
+    TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag, d, a.max_clen, a.spill, a.nspill, a.spill2,
+                            a.nspill2));
+  }
   DpArgs sp = d;
   sp.order = a.spill;
   sp.npairs_dev = a.nspill;
@@ -1216,8 +1226,9 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
 
 // the FP32 refine of a pair list: wavefront DP or a pairwise kernel
 template <int MEAS>
-int refine32(tsim_ctx* ctx, const KArgs& a, int dp32, int G, int R, const DpArgs& d) {
-  if (is_dp(MEAS)) return run_dp(ctx, a, dp32, G, R, d);
+int refine32(tsim_ctx* ctx, const KArgs& a, int dp32, int G, int R, const DpArgs& d,
+             bool latency = false) {
+  if (is_dp(MEAS)) return run_dp(ctx, a, dp32, G, R, d, latency);
   PwArgs p{d.qpts, d.qoff, d.cpts, d.coff, d.pairs, d.npairs, d.npairs_dev, d.order, d.out,
            nullptr, d.thr};
   return launch_pairwise(ctx, MEAS == M_HAUSDORFF ? TSIM_HAUSDORFF : TSIM_EUCLIDEAN, p);
@@ -1256,7 +1267,7 @@ int finish_knn(tsim_ctx* ctx, KArgs& a, int dpc, int dp64) {
     r.delta = -1;
     // compensated FP32 re-score of the set, then FP64 only for the pairs it
     // cannot order (near-ties within the compensated error bound)
-    if (compensated_rescore(MEAS)) TSIM_TRY(run_dp(ctx, a, dpc, 32, 1, r));
+    if (compensated_rescore(MEAS)) TSIM_TRY(run_dp(ctx, a, dpc, 32, 1, r, true));
     cluster_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
     r.pairs = a.r64pairs;
     r.out64 = a.r64;
@@ -1385,7 +1396,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
       TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, one));
     }
   } else {
-    TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, d));
+    TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, d, true));
   }
   stage_end(ctx);
 
@@ -1426,7 +1437,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
         TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, one));
       }
     } else {
-      TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, r1));
+      TSIM_TRY(refine32<MEAS>(ctx, a, dp32, Gs, Rs, r1, true));
     }
   }
   stage_end(ctx);
@@ -1571,6 +1582,12 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
     for (int R : {1, 2, 4, 8, 16})
       if (diag_ok(p->measure == TSIM_LCSS, n, m, wd, R)) {
         a.rdiag = R;
+        break;
+      }
+    a.rdiag_cta = 0;
+    for (int R : {1, 2, 4})
+      if (diag_ok(p->measure == TSIM_LCSS, n, m, wd, R, 256)) {
+        a.rdiag_cta = R;
         break;
       }
     if (a.plain || (p->flags & TSIM_FLAG_NO_PRUNE)) a.rdiag = 0;
@@ -1976,7 +1993,7 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   using namespace tsim;
   TSIM_CHECK_ARG(ctx && p && d_qpts && d_qoff && d_cpts && d_coff && d_pairs, "NULL argument");
   TSIM_CHECK_ARG(npairs >= 0 && max_qlen >= 1 && max_clen >= 1, "bad sizes");
-  TSIM_CHECK_ARG(precision >= 0 && precision <= 2 && kernel >= 0 && kernel <= 2, "bad mode");
+  TSIM_CHECK_ARG(precision >= 0 && precision <= 2 && kernel >= 0 && kernel <= 3, "bad mode");
   TSIM_CHECK_ARG(precision == 0 ? d_out32 != nullptr : d_out64 != nullptr, "NULL output");
   int kinds[3];
   if (p->measure == TSIM_DTW) {
@@ -2021,12 +2038,18 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   if (kernel == 1 || (kernel == 0 && (!diag_kind || Rd == 0)) || !diag_kind)
     return launch_dp(ctx, kind, G, R, d, max_clen);
   if (Rd == 0) Rd = 16;  // none fits the longest pair: the widest takes the rest
+  int Rc = 4;  // a CTA per pair: the smallest R that fits the longest pair
+  for (int R2 : {4, 2, 1})
+    if (diag_ok(p->measure == TSIM_LCSS, max_qlen, max_clen, wd, R2, 256)) Rc = R2;
   TSIM_TRY(arena_reserve(ctx, 2 * align256(sizeof(int) * (size_t)npairs) + 512));
   int* spill = arena_take<int>(ctx, npairs);
   int* nspill = arena_take<int>(ctx, 4);
   int* tmp = arena_take<int>(ctx, npairs);
   int* ntmp = arena_take<int>(ctx, 4);
-  TSIM_TRY(launch_dp_diag(ctx, kind, Rd, d, max_clen, spill, nspill, tmp, ntmp));
+  if (kernel == 3)
+    TSIM_TRY(launch_dp_diag(ctx, kind, Rc, d, max_clen, spill, nspill, tmp, ntmp, 8));
+  else
+    TSIM_TRY(launch_dp_diag(ctx, kind, Rd, d, max_clen, spill, nspill, tmp, ntmp));
   d.order = spill;
   d.npairs_dev = nspill;
   return launch_dp(ctx, kind, G, R, d, max_clen);

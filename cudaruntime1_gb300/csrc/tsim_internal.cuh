@@ -287,13 +287,17 @@ int launch_pairwise64(tsim_ctx* ctx, int measure, const PwArgs& a);
 // G lanes per pair (4, 8, 16 or 32), R rows per lane (1, 2, 4 or 8).
 int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a, int max_m);
 // Anti-diagonal kernel (dp_diag.cu) for DTW/LCSS/Frechet FP32 and compensated
-// kinds: passes with R, 2R, .. 4 rows per lane-group, each taking the pairs
-// the previous one could not; pairs no pass takes are left in spill[] (count
-// in *nspill) for launch_dp.  tmp/ntmp: a second list of the same size.
-// max_m bounds the candidate length (shared-memory staging).
+// kinds: passes with R, 2R, .. rows per lane-group, each taking the pairs the
+// previous one could not; pairs no pass takes are left in spill[] (count in
+// *nspill) for launch_dp.  tmp/ntmp: a second list of the same size.  max_m
+// bounds the candidate length (shared-memory staging).  warps: 1 = a warp
+// per pair (R up to 16), > 1 = a CTA of 8 warps per pair (R up to 4; for few,
+// long, full-row pairs, where the latency of one pair is the launch's).
 int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, int* spill,
-                   int* nspill, int* tmp, int* ntmp);
-bool diag_ok(bool lcss, int n, int m, int wd, int R);
+                   int* nspill, int* tmp, int* ntmp, int warps = 1);
+// the anti-diagonal kernel's validity condition for a pair shape, R rows
+// per lane-group and `lanes` lanes per pair
+bool diag_ok(bool lcss, int n, int m, int wd, int R, int lanes = 32);
 
 // choose (G, R) for pairs of shape n x m under band w
 void dp_shape(int kind, int n, int m, int band_w_or_delta, int& G, int& R);
