@@ -332,6 +332,9 @@ def run_serving(args):
     """Serving loop: a resident 1M-trajectory database, Poisson arrivals of
     single-query kNN requests of uniformly drawn measures and lengths,
     admitted by device-memory budget; p50/p99 latency and achieved rate."""
+    # one hardware work queue per slot stream (the process default is 8, which
+    # would serialise the slots' streams); read when CUDA initialises
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", str(max(8, min(32, args.slots))))
     import torch
 
     import cudaruntime1_gb300 as T

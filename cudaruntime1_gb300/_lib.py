@@ -62,7 +62,8 @@ class TsimServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
                 ("rejected", C.c_int64), ("queued", C.c_int), ("in_flight", C.c_int),
                 ("peak_in_flight", C.c_int), ("slots", C.c_int), ("budget_bytes", C.c_int64),
-                ("scratch_in_use", C.c_int64), ("peak_scratch_bytes", C.c_int64)]
+                ("scratch_in_use", C.c_int64), ("peak_scratch_bytes", C.c_int64),
+                ("launch_ms", C.c_double), ("busy_ms", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

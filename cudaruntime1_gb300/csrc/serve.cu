@@ -123,6 +123,7 @@ struct tsim_server {
   int64_t submitted = 0, completed = 0, failed = 0, rejected = 0;
   int in_flight = 0, peak_in_flight = 0;
   size_t in_use = 0, peak_in_use = 0;
+  double launch_ms = 0.0, busy_ms = 0.0;
   std::thread worker;
 };
 
@@ -197,6 +198,7 @@ void worker_loop(tsim_server* s) {
   cudaSetDevice(s->ctx->device);
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
+    const Clock::time_point t_round = Clock::now();
     bool progressed = false;
     for (Slot& sl : s->slots) {  // completions
       if (!sl.req) continue;
@@ -232,16 +234,20 @@ void worker_loop(tsim_server* s) {
       s->in_use += bytes;
       s->peak_in_use = std::max(s->peak_in_use, s->in_use);
       lk.unlock();
+      const Clock::time_point t0 = Clock::now();
       const int st = launch(s, *sl);
+      const double lms = ms_between(t0, Clock::now());
       std::string err;
       if (st != TSIM_OK) {
         err = tsim_last_error();
         cudaStreamSynchronize(sl->ctx->stream);  // what was enqueued must end before the block is reused
       }
       lk.lock();
+      s->launch_ms += lms;
       if (st != TSIM_OK) finish(s, *sl, st, err);
       progressed = true;
     }
+    s->busy_ms += ms_between(t_round, Clock::now());
     if (s->stop && s->queue.empty() && s->in_flight == 0) break;
     if (!progressed) {
       if (s->in_flight == 0)
@@ -422,6 +428,8 @@ extern "C" int tsim_server_get_stats(tsim_server* s, tsim_server_stats* st) {
   st->budget_bytes = (int64_t)s->budget;
   st->scratch_in_use = (int64_t)s->in_use;
   st->peak_scratch_bytes = (int64_t)s->peak_in_use;
+  st->launch_ms = s->launch_ms;
+  st->busy_ms = s->busy_ms;
   return TSIM_OK;
 }
 

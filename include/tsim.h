@@ -225,7 +225,9 @@ TSIM_API int64_t tsim_knn_scratch_bytes(const tsim_params* p, int nq, int max_ql
  * slot is free and its scratch (tsim_knn_scratch_bytes + staging) fits in the
  * pool, so requests that arrive while others run start at once and their
  * kernels overlap on the GPU.  The database stays resident.  A request's
- * results do not depend on what else is in flight. */
+ * results do not depend on what else is in flight.  The streams of the slots
+ * share the process's hardware work queues: set CUDA_DEVICE_MAX_CONNECTIONS
+ * (default 8, at most 32) to the slot count before CUDA initialises. */
 typedef struct tsim_server tsim_server;
 typedef struct tsim_server_opts {
   int slots;                /* requests in flight at once (0: 16) */
@@ -245,6 +247,8 @@ typedef struct tsim_server_stats {
   int64_t submitted, completed, failed, rejected;
   int queued, in_flight, peak_in_flight, slots;
   int64_t budget_bytes, scratch_in_use, peak_scratch_bytes;
+  double launch_ms;   /* host time the worker spent enqueueing requests */
+  double busy_ms;     /* host time the worker spent on anything but waiting */
 } tsim_server_stats;
 
 TSIM_API int tsim_server_create(tsim_ctx* ctx, tsim_db* db, const tsim_server_opts* opts,
