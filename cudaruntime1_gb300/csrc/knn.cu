@@ -44,6 +44,7 @@ constexpr int kChunk = 256;     // candidates per stage-A CTA
 constexpr int kSelThreads = 256;
 constexpr int kSeg = 2048;       // list entries per CTA of the two-level selections
 constexpr int kLb2Warps = 8;
+constexpr int kGridWords = 4096;  // LCSS occupancy grid of a query: 131,072 cells (16 KiB)
 constexpr int kMaxTable = 512;  // sparse-table columns (query rows, downsampled beyond)
 
 enum Meas { M_DTW = 0, M_LCSS = 1, M_FRECHET = 2, M_HAUSDORFF = 3, M_EUCLID = 4 };
@@ -201,11 +202,18 @@ __device__ __forceinline__ float bound1(const KArgs& a, float4 qb, float4 qe, in
 // (min(n, m) unless the eps-inflated boxes are disjoint) hardly ranks, so
 // LCSS tries the candidates whose end points lie nearest the query's first.
 template <int MEAS>
-__device__ __forceinline__ float seed_score(float b, const float4& qe, const float4& ce) {
+__device__ __forceinline__ float seed_score(float b, const float4& qe, const float4& ce,
+                                            bool ends) {
   if (MEAS != M_LCSS) return b;
   if (b <= 0.0f) return TSIM_INF;  // no match possible
   const float d0x = qe.x - ce.x, d0y = qe.y - ce.y, d1x = qe.z - ce.z, d1y = qe.w - ce.w;
-  return d0x * d0x + d0y * d0y + d1x * d1x + d1y * d1y;
+  return d0x * d0x + d0y * d0y + (ends ? d1x * d1x + d1y * d1y : 0.0f);
+}
+
+// the last points can only be matched to each other when the index window
+// lets the ends align (|n - m| <= delta, or no window)
+__device__ __forceinline__ bool ends_align(int n, int m, int delta) {
+  return delta < 0 || abs(n - m) <= delta;
 }
 
 template <int MEAS>
@@ -222,7 +230,7 @@ __global__ void __launch_bounds__(kChunk) lb1_kernel(KArgs a) {
     const float4 ce = a.cends[c];
     float b = bound1<MEAS>(a, qb, qe, n, a.cbox[c], ce, a.clen[c]);
     a.lb1[(size_t)q * a.C + c] = b;
-    key = pack_key(seed_score<MEAS>(b, qe, ce), threadIdx.x);
+    key = pack_key(seed_score<MEAS>(b, qe, ce, ends_align(n, a.clen[c], a.delta)), threadIdx.x);
   }
   keys[threadIdx.x] = key;
   __syncthreads();
@@ -250,7 +258,8 @@ __global__ void __launch_bounds__(kSelThreads) seed_kernel(KArgs a) {
     unsigned long long key = ~0ull;
     if (c >= 0) {
       float b = a.lb1[(size_t)q * a.C + c];
-      key = pack_key(seed_score<MEAS>(b, a.qends[q], a.cends[c]), c);
+      key = pack_key(seed_score<MEAS>(b, a.qends[q], a.cends[c],
+                                      ends_align(a.qlen[q], a.clen[c], a.delta)), c);
     }
     keys[i] = key;
   }
@@ -666,6 +675,37 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
   QTable T;
   if (kTable && use_table) qtable_build(T, A, n, reinterpret_cast<float4*>(smem_raw));
   const float e2 = __fmul_ru(a.eps, 1.0f + 1.0f / 1048576.0f);
+  // LCSS: an occupancy grid of the query in shared memory, cells of side
+  // gs >= 1.01 eps, each query point marking its cell and the 8 around it.
+  // A candidate point within eps (per coordinate) of any query point then
+  // lies in a marked cell: its cell index differs from that query point's
+  // by at most 1 per axis, the index arithmetic's rounding (< 1e-3 cell)
+  // being covered by the 1 % margin.  Points outside the grid match nothing.
+  uint32_t* grid = reinterpret_cast<uint32_t*>(smem_raw + (size_t)a.tstride * sizeof(float4));
+  float gx0 = 0.0f, gy0 = 0.0f, ginv = 0.0f;
+  int gnx = 0, gny = 0;
+  if (MEAS == M_LCSS && a.eps > 0.0f) {
+    float gs = __fmul_ru(a.eps, 1.01f);
+    const float W = qb.z - qb.x, H = qb.w - qb.y;
+    while ((W / gs + 3.0f) * (H / gs + 3.0f) > 32.0f * kGridWords) gs *= 1.25f;
+    gnx = (int)(W / gs) + 3;
+    gny = (int)(H / gs) + 3;
+    gx0 = qb.x - gs;
+    gy0 = qb.y - gs;
+    ginv = 1.0f / gs;
+    for (int w = threadIdx.x; w < kGridWords; w += blockDim.x) grid[w] = 0u;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int cx = min(max((int)((A[i].x - gx0) * ginv), 1), gnx - 2);
+      const int cy = min(max((int)((A[i].y - gy0) * ginv), 1), gny - 2);
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int cell = (cy + dy) * gnx + cx + dx;
+          atomicOr(grid + (cell >> 5), 1u << (cell & 31));
+        }
+    }
+    __syncthreads();
+  }
   for (int e = blockIdx.x * kLb2Warps + warp; e < cnt; e += gridDim.x * kLb2Warps) {
     const int c = a.list1[(size_t)q * a.C + e];
     const float2* B = a.cpts + a.coff[c];
@@ -767,8 +807,13 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
         const float4 bx = qtable_box(T, lo, hi);
         const float2 p = B[j];
         if (p.x >= __fsub_rd(bx.x, e2) && p.x <= __fadd_ru(bx.z, e2) &&
-            p.y >= __fsub_rd(bx.y, e2) && p.y <= __fadd_ru(bx.w, e2))
-          ++count;
+            p.y >= __fsub_rd(bx.y, e2) && p.y <= __fadd_ru(bx.w, e2)) {
+          const float fx = (p.x - gx0) * ginv, fy = (p.y - gy0) * ginv;
+          if (fx >= 0.0f && fy >= 0.0f && fx < (float)gnx && fy < (float)gny) {
+            const int cell = (int)fy * gnx + (int)fx;
+            if ((grid[cell >> 5] >> (cell & 31)) & 1u) ++count;
+          }
+        }
       }
       for (int o = 16; o; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
       lbv = fminf((float)min(count, min(n, m)), sbnd);  // an upper bound on the count
@@ -1413,6 +1458,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   // whole request, so a single query against a large database fills the GPU
   const int ch = std::max(1, std::min(65535, (8 * ctx->num_sms + nq - 1) / nq));
   size_t lb2_smem = (MEAS == M_DTW || MEAS == M_LCSS) ? qtable_bytes(max_qlen) : 0;
+  if (MEAS == M_LCSS) lb2_smem = (size_t)a.tstride * sizeof(float4) + sizeof(uint32_t) * kGridWords;
   if (lb2_smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(lb2_kernel<MEAS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)lb2_smem));
