@@ -1250,16 +1250,18 @@ __global__ void stats_kernel(KArgs a, unsigned long long* counters, int with_res
 // latency: a round of few pairs (seeds, round 1, re-score), whose launch
 // lasts as long as its longest pair.  A step of a warp per pair costs R rows
 // of instructions on one warp; a CTA per pair spreads the rows over 8 warps
-// for a barrier per step, which pays off only once a warp would need 8 or
-// more rows per lane (long full rows; measured: at R = 2 and 4 the barrier
-// made the compensated re-score of the batched DTW workload 0.43 -> 0.58 ms).
+// for a barrier per step, which pays off once a warp would need 8 or more
+// FP32 rows per lane, or 4 or more compensated (two-float) ones (measured: at
+// R = 2 the barrier made the compensated re-score of the batched DTW workload
+// 0.43 -> 0.58 ms).
 int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& d,
            bool latency = false) {
   const bool diag_kind = kind == DP_DTW_SQ || kind == DP_DTW_EU || kind == DP_LCSS ||
                          kind == DP_FRECHET_SQ || kind == DP_DTW_SQC || kind == DP_DTW_EUC ||
                          kind == DP_FRECHET_SQC;
   if (!diag_kind || a.rdiag == 0) return launch_dp(ctx, kind, G, R, d, a.max_clen);
-  if (latency && a.rdiag_cta > 0 && a.rdiag >= 8) {
+  const bool twofloat = kind == DP_DTW_SQC || kind == DP_DTW_EUC || kind == DP_FRECHET_SQC;
+  if (latency && a.rdiag_cta > 0 && a.rdiag >= (twofloat ? 4 : 8)) {
     TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag_cta, d, a.max_clen, a.spill, a.nspill, a.spill2,
                             a.nspill2, 8));
   } else {
