@@ -386,10 +386,13 @@ __device__ __forceinline__ float4 qtable_box(const QTable& T, int lo, int hi) {
   return make_float4(fminf(u.x, v.x), fminf(u.y, v.y), fmaxf(u.z, v.z), fmaxf(u.w, v.w));
 }
 
+// Bytes of the largest table of any query of up to max_n rows.  The size is
+// not monotone in n (a 512-row query keeps 512 blocks, a 600-row one 300
+// blocks of 2 rows), so a buffer shared by queries of different lengths is
+// sized for the worst case: min(max_n, kMaxTable) blocks, whose level count
+// no shorter query exceeds.
 size_t qtable_bytes(int max_n) {
-  int f_log = 0;
-  while ((max_n + (1 << f_log) - 1) >> f_log > kMaxTable) ++f_log;
-  int nb = (max_n + (1 << f_log) - 1) >> f_log;
+  const int nb = std::max(1, std::min(max_n, kMaxTable));
   int levels = 1;
   while ((1 << levels) <= nb) ++levels;
   return (size_t)levels * nb * sizeof(float4);

@@ -13,10 +13,14 @@
 //     (knn_scratch_bytes), lent to the slot context, which never grows it;
 //   * a FIFO admission queue and one worker thread.  The worker admits the
 //     head request as soon as a slot is free and its block fits the pool,
-//     and polls the slots' completion events; a request that arrives while
-//     others run starts as soon as a slot and memory free up.
-// A request's kernels read only its own block and the read-only database, so
-// its results are the same alone and in any mix.
+//     together with up to 15 queued requests of the same parameters (found
+//     among the next 64): their queries run as one pipeline call, which
+//     fills the GPU far better than single-query calls.  It polls the slots'
+//     completion events; a request that arrives while others run starts as
+//     soon as a slot and memory free up.
+// A query's top-k depends only on that query and the read-only database (no
+// stage couples the queries of a call), so results are the same alone, in
+// a batch and in any mix.
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -94,14 +98,28 @@ class Pool {
   std::map<size_t, size_t> free_;
 };
 
+// Requests admitted together into one slot: the same parameters, their
+// queries concatenated into one pipeline call (continuous batching).  A
+// query's top-k never depends on the other queries of its call.
+constexpr int kMaxBatch = 16;     // requests per batch
+constexpr int kLookahead = 64;    // queue entries scanned for batch mates
+
 struct Slot {
   tsim_ctx* ctx = nullptr;
   cudaEvent_t t0 = nullptr, t1 = nullptr, done = nullptr;
   char* pinned = nullptr;
   size_t pinned_cap = 0;
-  Request* req = nullptr;
+  std::vector<Request*> batch;  // empty: the slot is free
+  std::vector<int> first_q;     // each request's first query in the batch
+  int nq = 0, max_qlen = 0, qb = 0;
+  size_t o_off = 0, o_ids = 0, o_dists = 0, staging = 0, scratch = 0;
   size_t off = 0, bytes = 0;
 };
+
+bool same_params(const tsim_params& a, const tsim_params& b) {
+  return a.measure == b.measure && a.k == b.k && a.cost == b.cost && a.band_pct == b.band_pct &&
+         a.epsilon == b.epsilon && a.delta == b.delta && a.flags == b.flags;
+}
 
 }  // namespace
 }  // namespace tsim
@@ -130,65 +148,103 @@ struct tsim_server {
 namespace tsim {
 namespace {
 
-// Enqueue the request's work on its slot's stream (no lock held).
+// Lay out a batch's staging (queries, offsets, ids, distances) and size its
+// pipeline scratch.
+void plan_batch(tsim_server* s, Slot& sl) {
+  const tsim_params& p = sl.batch[0]->p;
+  sl.first_q.clear();
+  sl.nq = 0;
+  sl.max_qlen = 0;
+  size_t npts = 0;
+  for (Request* r : sl.batch) {
+    sl.first_q.push_back(sl.nq);
+    sl.nq += r->nq;
+    sl.max_qlen = std::max(sl.max_qlen, r->max_qlen);
+    npts += r->pts.size();
+  }
+  const int64_t kMaxPairs = int64_t(1) << 24;
+  sl.qb = (int)std::max<int64_t>(1, std::min<int64_t>(sl.nq, kMaxPairs / std::max(s->db->count, 1)));
+  sl.scratch = align256(knn_scratch_bytes(&p, sl.qb, sl.max_qlen, s->db));
+  sl.o_off = align256(sizeof(tsim_point) * npts);
+  sl.o_ids = sl.o_off + align256(sizeof(int64_t) * (sl.nq + 1));
+  sl.o_dists = sl.o_ids + align256(sizeof(int) * (size_t)sl.nq * p.k);
+  sl.staging = sl.o_dists + align256(sizeof(float) * (size_t)sl.nq * p.k);
+  sl.bytes = sl.staging + sl.scratch;
+}
+
+// Enqueue the batch's work on its slot's stream (no lock held).
 int launch(tsim_server* s, Slot& sl) {
-  Request& r = *sl.req;
   tsim_ctx* c = sl.ctx;
   char* base = s->pool_base + sl.off;
-  if (sl.pinned_cap < r.staging) {  // the slot is idle: nothing reads the old buffer
+  if (sl.pinned_cap < sl.staging) {  // the slot is idle: nothing reads the old buffer
     if (sl.pinned) TSIM_CUDA(cudaFreeHost(sl.pinned));
     sl.pinned = nullptr;
     sl.pinned_cap = 0;
-    const size_t cap = std::max<size_t>(r.staging, size_t(1) << 20);
+    const size_t cap = std::max<size_t>(sl.staging, size_t(1) << 20);
     TSIM_CUDA(cudaHostAlloc((void**)&sl.pinned, cap, cudaHostAllocDefault));
     sl.pinned_cap = cap;
   }
-  memcpy(sl.pinned, r.pts.data(), sizeof(tsim_point) * r.pts.size());
-  memcpy(sl.pinned + r.o_off, r.off.data(), sizeof(int64_t) * r.off.size());
-  TSIM_CUDA(cudaMemcpyAsync(base, sl.pinned, r.o_ids, cudaMemcpyHostToDevice, c->stream));
-  c->arena = base + r.staging;
-  c->arena_cap = r.scratch;
+  // concatenate the queries and rebase their offsets
+  int64_t* hoff = reinterpret_cast<int64_t*>(sl.pinned + sl.o_off);
+  size_t pt = 0;
+  int qi = 0;
+  hoff[0] = 0;
+  for (Request* r : sl.batch) {
+    memcpy(sl.pinned + sizeof(tsim_point) * pt, r->pts.data(), sizeof(tsim_point) * r->pts.size());
+    for (int i = 0; i < r->nq; ++i) hoff[qi + i + 1] = (int64_t)pt + r->off[i + 1];
+    pt += r->pts.size();
+    qi += r->nq;
+  }
+  TSIM_CUDA(cudaMemcpyAsync(base, sl.pinned, sl.o_ids, cudaMemcpyHostToDevice, c->stream));
+  c->arena = base + sl.staging;
+  c->arena_cap = sl.scratch;
   c->arena_used = 0;
   TSIM_CUDA(cudaEventRecord(sl.t0, c->stream));
+  const tsim_params& p = sl.batch[0]->p;
   const float2* qpts = reinterpret_cast<const float2*>(base);
-  const int64_t* qoff = reinterpret_cast<const int64_t*>(base + r.o_off);
-  int* ids = reinterpret_cast<int*>(base + r.o_ids);
-  float* dists = reinterpret_cast<float*>(base + r.o_dists);
-  const int k = r.p.k;
-  for (int q0 = 0; q0 < r.nq; q0 += r.qb) {
-    const int nb = std::min(r.qb, r.nq - q0);
-    TSIM_TRY(knn(c, &r.p, qpts, qoff + q0, nb, r.max_qlen, s->db, ids + (size_t)q0 * k,
+  const int64_t* qoff = reinterpret_cast<const int64_t*>(base + sl.o_off);
+  int* ids = reinterpret_cast<int*>(base + sl.o_ids);
+  float* dists = reinterpret_cast<float*>(base + sl.o_dists);
+  const int k = p.k;
+  for (int q0 = 0; q0 < sl.nq; q0 += sl.qb) {
+    const int nb = std::min(sl.qb, sl.nq - q0);
+    TSIM_TRY(knn(c, &p, qpts, qoff + q0, nb, sl.max_qlen, s->db, ids + (size_t)q0 * k,
                  dists + (size_t)q0 * k, nullptr, nullptr));
   }
   TSIM_CUDA(cudaEventRecord(sl.t1, c->stream));
-  TSIM_CUDA(cudaMemcpyAsync(sl.pinned + r.o_ids, base + r.o_ids, r.staging - r.o_ids,
+  TSIM_CUDA(cudaMemcpyAsync(sl.pinned + sl.o_ids, base + sl.o_ids, sl.staging - sl.o_ids,
                             cudaMemcpyDeviceToHost, c->stream));
   TSIM_CUDA(cudaEventRecord(sl.done, c->stream));
   return TSIM_OK;
 }
 
-// Retire the slot's request (lock held; its stream work has ended).
+// Retire the slot's batch (lock held; its stream work has ended).
 void finish(tsim_server* s, Slot& sl, int status, const std::string& err) {
-  Request* r = sl.req;
-  if (status == TSIM_OK) {
-    const size_t nk = (size_t)r->nq * r->p.k;
-    r->ids.resize(nk);
-    r->dists.resize(nk);
-    memcpy(r->ids.data(), sl.pinned + r->o_ids, sizeof(int) * nk);
-    memcpy(r->dists.data(), sl.pinned + r->o_dists, sizeof(float) * nk);
-    if (cudaEventElapsedTime(&r->device_ms, sl.t0, sl.t1) != cudaSuccess) r->device_ms = 0.0f;
-    ++s->completed;
-  } else {
-    r->error = err;
-    ++s->failed;
+  float dms = 0.0f;
+  if (status == TSIM_OK && cudaEventElapsedTime(&dms, sl.t0, sl.t1) != cudaSuccess) dms = 0.0f;
+  const Clock::time_point now = Clock::now();
+  for (size_t b = 0; b < sl.batch.size(); ++b) {
+    Request* r = sl.batch[b];
+    if (status == TSIM_OK) {
+      const size_t nk = (size_t)r->nq * r->p.k, at = (size_t)sl.first_q[b] * r->p.k;
+      r->ids.resize(nk);
+      r->dists.resize(nk);
+      memcpy(r->ids.data(), sl.pinned + sl.o_ids + sizeof(int) * at, sizeof(int) * nk);
+      memcpy(r->dists.data(), sl.pinned + sl.o_dists + sizeof(float) * at, sizeof(float) * nk);
+      r->device_ms = dms;
+      ++s->completed;
+    } else {
+      r->error = err;
+      ++s->failed;
+    }
+    r->status = status;
+    r->t_done = now;
+    r->done = true;
   }
-  r->status = status;
-  r->t_done = Clock::now();
-  r->done = true;
   s->pool.release(sl.off, sl.bytes);
   s->in_use -= sl.bytes;
-  --s->in_flight;
-  sl.req = nullptr;
+  s->in_flight -= (int)sl.batch.size();
+  sl.batch.clear();
   sl.ctx->arena = nullptr;
   sl.ctx->arena_cap = 0;
   s->cv_done.notify_all();
@@ -201,7 +257,7 @@ void worker_loop(tsim_server* s) {
     const Clock::time_point t_round = Clock::now();
     bool progressed = false;
     for (Slot& sl : s->slots) {  // completions
-      if (!sl.req) continue;
+      if (sl.batch.empty()) continue;
       const cudaError_t e = cudaEventQuery(sl.done);
       if (e == cudaErrorNotReady) continue;
       if (e == cudaSuccess)
@@ -211,27 +267,47 @@ void worker_loop(tsim_server* s) {
                                          cudaGetErrorString(e));
       progressed = true;
     }
-    while (!s->queue.empty()) {  // admissions, first come first served
+    while (!s->queue.empty()) {  // admissions: the head request and its batch mates
       Slot* sl = nullptr;
       for (Slot& x : s->slots)
-        if (!x.req) {
+        if (x.batch.empty()) {
           sl = &x;
           break;
         }
       if (!sl) break;
-      Request* r = s->queue.front();
-      const size_t bytes = r->staging + r->scratch;
+      Request* r0 = s->queue.front();
+      std::vector<size_t> picked{0};  // queue positions of the batch
+      sl->batch.assign(1, r0);
+      for (size_t qi = 1; qi < s->queue.size() && qi < (size_t)kLookahead &&
+                          sl->batch.size() < (size_t)kMaxBatch;
+           ++qi)
+        if (same_params(s->queue[qi]->p, r0->p)) {
+          picked.push_back(qi);
+          sl->batch.push_back(s->queue[qi]);
+        }
+      plan_batch(s, *sl);
       size_t off = 0;
-      if (!s->pool.alloc(bytes, off)) break;  // waits for memory to free up
-      s->queue.pop_front();
-      sl->req = r;
+      bool fits = s->pool.alloc(sl->bytes, off);
+      if (!fits && sl->batch.size() > 1) {
+        picked.resize(1);  // the batch does not fit: the head request alone
+        sl->batch.resize(1);
+        plan_batch(s, *sl);
+        fits = s->pool.alloc(sl->bytes, off);
+      }
+      if (!fits) {
+        sl->batch.clear();
+        break;  // waits for memory to free up
+      }
+      for (size_t i = picked.size(); i-- > 0;) s->queue.erase(s->queue.begin() + picked[i]);
       sl->off = off;
-      sl->bytes = bytes;
-      r->t_admit = Clock::now();
-      r->inflight_at_admit = s->in_flight;
-      ++s->in_flight;
+      const Clock::time_point now = Clock::now();
+      for (Request* r : sl->batch) {
+        r->t_admit = now;
+        r->inflight_at_admit = s->in_flight;
+      }
+      s->in_flight += (int)sl->batch.size();
       s->peak_in_flight = std::max(s->peak_in_flight, s->in_flight);
-      s->in_use += bytes;
+      s->in_use += sl->bytes;
       s->peak_in_use = std::max(s->peak_in_use, s->in_use);
       lk.unlock();
       const Clock::time_point t0 = Clock::now();

@@ -245,3 +245,21 @@ def test_knn_full_rows_long_candidates(tsim, cuda_ctx, oracle, measure, kw):
     rel = np.abs(d.astype(np.float64) - want_d) / np.maximum(want_d, 1e-30)
     assert rel.max() <= REL_TOL
     db.close()
+
+
+@pytest.mark.parametrize("measure,kw", [("dtw", dict(band_pct=10)), ("lcss", dict(epsilon=0.5, delta=20))])
+def test_knn_mixed_query_lengths_one_call(tsim, cuda_ctx, oracle, measure, kw):
+    """Queries of 512, 600 and 1,100 points in one call: their sparse tables
+    share a stride sized for the longest, although a 512-row table is larger
+    than a 600-row one (rows are grouped in blocks beyond 512)."""
+    cp, co = _db(1500, 40, 200, 400)
+    qp, qo = G.random_walks(4, [512, 600, 300, 1100], 401)
+    db = tsim.Database(cuda_ctx, cp, co)
+    okw = dict(kw)
+    if "epsilon" in okw:
+        okw["eps"] = okw.pop("epsilon")
+    want_ids, want_d = oracle.knn(measure, qp, qo, cp, co, 10, **okw)
+    ids, d, _, _ = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 10,
+                               flags=tsim.api.FLAG_ALWAYS_PRUNE, **kw)
+    assert np.array_equal(ids, want_ids)
+    db.close()
