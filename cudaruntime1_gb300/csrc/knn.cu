@@ -44,7 +44,8 @@ constexpr int kChunk = 256;     // candidates per stage-A CTA
 constexpr int kSelThreads = 256;
 constexpr int kSeg = 2048;       // list entries per CTA of the two-level selections
 constexpr int kLb2Warps = 8;
-constexpr int kGridWords = 4096;  // LCSS occupancy grid of a query: 131,072 cells (16 KiB)
+constexpr int kGridWords = 4096;
+constexpr int kQBlocks = 8;       // row blocks of a query in the O(1) bound  // LCSS occupancy grid of a query: 131,072 cells (16 KiB)
 constexpr int kMaxTable = 512;  // sparse-table columns (query rows, downsampled beyond)
 
 enum Meas { M_DTW = 0, M_LCSS = 1, M_FRECHET = 2, M_HAUSDORFF = 3, M_EUCLID = 4 };
@@ -105,6 +106,7 @@ struct KArgs {
   const float4* csegbox;    // [C*kSegs] candidate segment boxes
   const float2* csegsum;    // [C*kSegs] sums of the candidate segments' points
   double2* qpre;            // [nq*(max_qlen+1)] query prefix sums (FP64)
+  float4* qblk;             // [nq*kQBlocks] boxes of the query's row blocks
   int* spill;               // pairs the anti-diagonal kernel leaves to the striped one
   int* nspill;
   int* spill2;              // the list between passes of the anti-diagonal kernel
@@ -156,6 +158,62 @@ __device__ __forceinline__ float widen(float t, double g) {
 // ---------------------------------------------------------------------------
 // stage A: O(1) bounds from summaries + chunk-local best candidates
 // ---------------------------------------------------------------------------
+// The query's rows in kQBlocks blocks (block b: rows [b n / kQBlocks,
+// (b+1) n / kQBlocks)), each with its bounding box.  Every query row is
+// coupled to (DTW, Frechet, Euclidean) or has a nearest point in (Hausdorff)
+// the candidate, whose points lie in its box, so a block costs at least its
+// box's distance to the candidate's box per row; LCSS: a row can only match
+// when its block's eps-inflated box meets the candidate's box.
+template <int MEAS>
+__device__ __forceinline__ float block_bound(const KArgs& a, const float4* qblk, int n, float4 cb,
+                                             int m) {
+  const int rows_max = MEAS == M_EUCLID ? m : n;  // lock-step: rows 0 .. m-1 only
+  float acc = 0.0f;
+  int cnt = 0;
+  const float e2 = __fmul_ru(a.eps, 1.0f + 1.0f / 1048576.0f);
+#pragma unroll
+  for (int b = 0; b < kQBlocks; ++b) {
+    const int r0 = (int)((long long)b * n / kQBlocks);
+    const int r1 = min((int)((long long)(b + 1) * n / kQBlocks), rows_max);
+    if (r1 <= r0) continue;
+    const float4 bx = qblk[b];
+    if (MEAS == M_LCSS) {
+      if (cb.z >= __fsub_rd(bx.x, e2) && cb.x <= __fadd_ru(bx.z, e2) &&
+          cb.w >= __fsub_rd(bx.y, e2) && cb.y <= __fadd_ru(bx.w, e2))
+        cnt += r1 - r0;
+      continue;
+    }
+    const float d = box_box_d2_rd(bx, cb);
+    if (MEAS == M_FRECHET || MEAS == M_HAUSDORFF) {
+      acc = fmaxf(acc, d);
+    } else {
+      const float c = (MEAS == M_DTW && a.cost) ? __fsqrt_rd(d) : d;
+      acc = __fadd_rd(acc, __fmul_rd((float)(r1 - r0), c));
+    }
+  }
+  return MEAS == M_LCSS ? (float)cnt : acc;
+}
+
+// one warp per query: lane b < kQBlocks reduces block b's box
+__global__ void qblocks_kernel(const float2* __restrict__ pts, const int64_t* __restrict__ off,
+                               int nq, float4* __restrict__ qblk) {
+  const int lane = threadIdx.x & 31;
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= nq || lane >= kQBlocks) return;
+  const int64_t o = off[q];
+  const int n = (int)(off[q + 1] - o);
+  const int r0 = (int)((long long)lane * n / kQBlocks), r1 = (int)((long long)(lane + 1) * n / kQBlocks);
+  float x0 = TSIM_INF, y0 = TSIM_INF, x1 = -TSIM_INF, y1 = -TSIM_INF;
+  for (int r = r0; r < r1; ++r) {
+    const float2 p = pts[o + r];
+    x0 = fminf(x0, p.x);
+    y0 = fminf(y0, p.y);
+    x1 = fmaxf(x1, p.x);
+    y1 = fmaxf(y1, p.y);
+  }
+  qblk[(size_t)q * kQBlocks + lane] = make_float4(x0, y0, x1, y1);
+}
+
 template <int MEAS>
 __device__ __forceinline__ float bound1(const KArgs& a, float4 qb, float4 qe, int n, float4 cb,
                                         float4 ce, int m) {
@@ -223,12 +281,20 @@ __global__ void __launch_bounds__(kChunk) lb1_kernel(KArgs a) {
   __shared__ unsigned long long sel[64];
   const int q = blockIdx.y, chunk = blockIdx.x;
   const int c = chunk * kChunk + threadIdx.x;
+  __shared__ float4 qblk[kQBlocks];
   const float4 qb = a.qbox[q], qe = a.qends[q];
   const int n = a.qlen[q];
+  if (threadIdx.x < kQBlocks) qblk[threadIdx.x] = a.qblk[(size_t)q * kQBlocks + threadIdx.x];
+  __syncthreads();
   unsigned long long key = ~0ull;
   if (c < a.C) {
-    const float4 ce = a.cends[c];
-    float b = bound1<MEAS>(a, qb, qe, n, a.cbox[c], ce, a.clen[c]);
+    const float4 ce = a.cends[c], cb = a.cbox[c];
+    const int m = a.clen[c];
+    float b = bound1<MEAS>(a, qb, qe, n, cb, ce, m);
+    if (n > 0 && m > 0 && (MEAS != M_EUCLID || n >= m)) {
+      const float bb = block_bound<MEAS>(a, qblk, n, cb, m);
+      b = MEAS == M_LCSS ? fminf(b, fminf(bb, (float)min(n, m))) : fmaxf(b, bb);
+    }
     a.lb1[(size_t)q * a.C + c] = b;
     key = pack_key(seed_score<MEAS>(b, qe, ce, ends_align(n, a.clen[c], a.delta)), threadIdx.x);
   }
@@ -1670,6 +1736,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
                 align256(sizeof(float) * nq * a.M) + 2 * align256(sizeof(float) * (nq + 1)) +
                 align256(sizeof(float4) * (size_t)nq * a.tstride) +
                 align256(sizeof(double2) * (size_t)nq * (max_qlen + 1)) +
+                align256(sizeof(float4) * (size_t)nq * kQBlocks) +
                 2 * align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 2 * 256;
   return need;
 }
@@ -1738,6 +1805,7 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.fcnt = arena_take<int>(ctx, nq + 1);
   a.qtab = arena_take<float4>(ctx, (size_t)nq * a.tstride);
   a.qpre = arena_take<double2>(ctx, (size_t)nq * (max_qlen + 1));
+  a.qblk = arena_take<float4>(ctx, (size_t)nq * kQBlocks);
   a.spill = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
   a.nspill = arena_take<int>(ctx, 4);
   a.spill2 = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
@@ -1750,6 +1818,9 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
 
   stage_begin(ctx, TSIM_STAGE_SUMMARY);
   TSIM_TRY(summarize(ctx, qpts, qoff, nq, qbox, qends, qlen));
+  qblocks_kernel<<<(nq + 3) / 4, 128, 0, ctx->stream>>>(qpts, qoff, nq, a.qblk);
+  TSIM_CUDA(cudaGetLastError());
+  launched(ctx);
   stage_end(ctx);
   switch (p->measure) {
     case TSIM_DTW:
