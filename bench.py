@@ -147,6 +147,17 @@ def dist_init():
     return rank, ws, local
 
 
+def max_over_ranks(x: float) -> float:
+    """The largest of the ranks' values (the replicas' timed regions): one
+    all-reduce, on the device for NCCL, on the host for gloo."""
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     rank, ws, _ = dist_init()
     if rank != 0:
@@ -457,9 +468,7 @@ def main():
     cnt = ctx.counters(reset=True)
     launches = cnt["launches"]
     if ws > 1:
-        t = torch.tensor([total_ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms)
     value = ws * nq * args.steps / (total_ms / 1e3)
     res_ids = ids.cpu().numpy().reshape(nq, k)
     res_d64 = d64.cpu().numpy().reshape(nq, k)
