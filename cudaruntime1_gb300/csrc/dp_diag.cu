@@ -378,8 +378,8 @@ int launch_chain(tsim_ctx* ctx, int R0, int warps, const DpArgs& a, int max_m, i
   // R0, 2 R0, .. Rmax: each pass takes the pairs the previous one spilled, so
   // every pair runs with the fewest rows per lane-group its shape admits
   // (fewer rows in flight, fewer masked cells); the last pass writes `spill`.
-  // A warp per pair goes to R = 16 (full rows of up to 497 columns), a CTA
-  // per pair to R = 4 (1021 columns).
+  // A warp per pair goes to R = 16 (full rows of up to 497 columns), two or
+  // eight warps per pair to R = 4 (253 or 1021 columns).
   const int rmax = warps == 1 ? 16 : 4;
   std::vector<int> rs;
   for (int R = std::max(1, std::min(R0, rmax)); R <= rmax; R *= 2) rs.push_back(R);
@@ -392,6 +392,8 @@ int launch_chain(tsim_ctx* ctx, int R0, int warps, const DpArgs& a, int max_m, i
     TSIM_CUDA(cudaMemsetAsync(nout, 0, sizeof(int), ctx->stream));
     if (warps == 1)
       TSIM_TRY((launch_diag_r<P, 1>(ctx, rs[p], in, max_m, out, nout)));
+    else if (warps == 2)
+      TSIM_TRY((launch_diag_r<P, 2>(ctx, rs[p], in, max_m, out, nout)));
     else
       TSIM_TRY((launch_diag_r<P, kCtaWarps>(ctx, rs[p], in, max_m, out, nout)));
     in.order = out;
@@ -404,7 +406,7 @@ int launch_chain(tsim_ctx* ctx, int R0, int warps, const DpArgs& a, int max_m, i
 
 int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, int* spill,
                    int* nspill, int* tmp, int* ntmp, int warps) {
-  const int W = warps > 1 ? kCtaWarps : 1;
+  const int W = warps > 2 ? kCtaWarps : warps;
   switch (kind) {
     case DP_DTW_SQ: return launch_chain<PolDtwSq>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
     case DP_DTW_EU: return launch_chain<PolDtwEu>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);

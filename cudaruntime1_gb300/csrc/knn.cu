@@ -113,6 +113,7 @@ struct KArgs {
   int* nspill2;
   int rdiag;                // rows per lane-group of the anti-diagonal kernel (0: off)
   int rdiag_cta;            // the same for a CTA per pair (0: no R fits the longest pair)
+  int rdiag_w2;             // the same for two warps per pair
   float4* qtab;             // [nq*tstride] query sparse tables (global memory)
   int tstride;
   int* off2;                // [nq+1]
@@ -1333,6 +1334,11 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
   if (latency && a.rdiag_cta > 0 && a.rdiag >= (twofloat ? 4 : 8)) {
     TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag_cta, d, a.max_clen, a.spill, a.nspill, a.spill2,
                             a.nspill2, 8));
+  } else if (latency && twofloat && a.rdiag >= 2 && a.rdiag_w2 > 0) {
+    // two warps per pair: a compensated row per lane and step, for a barrier
+    // of two warps
+    TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag_w2, d, a.max_clen, a.spill, a.nspill, a.spill2,
+                            a.nspill2, 2));
   } else {
     TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag, d, a.max_clen, a.spill, a.nspill, a.spill2,
                             a.nspill2));
@@ -1708,6 +1714,12 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
     for (int R : {1, 2, 4})
       if (diag_ok(p->measure == TSIM_LCSS, n, m, wd, R, 256)) {
         a.rdiag_cta = R;
+        break;
+      }
+    a.rdiag_w2 = 0;
+    for (int R : {1, 2, 4})
+      if (diag_ok(p->measure == TSIM_LCSS, n, m, wd, R, 64)) {
+        a.rdiag_w2 = R;
         break;
       }
     if (a.plain || (p->flags & TSIM_FLAG_NO_PRUNE)) a.rdiag = 0;
@@ -2118,7 +2130,7 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   using namespace tsim;
   TSIM_CHECK_ARG(ctx && p && d_qpts && d_qoff && d_cpts && d_coff && d_pairs, "NULL argument");
   TSIM_CHECK_ARG(npairs >= 0 && max_qlen >= 1 && max_clen >= 1, "bad sizes");
-  TSIM_CHECK_ARG(precision >= 0 && precision <= 2 && kernel >= 0 && kernel <= 3, "bad mode");
+  TSIM_CHECK_ARG(precision >= 0 && precision <= 2 && kernel >= 0 && kernel <= 4, "bad mode");
   TSIM_CHECK_ARG(precision == 0 ? d_out32 != nullptr : d_out64 != nullptr, "NULL output");
   int kinds[3];
   if (p->measure == TSIM_DTW) {
@@ -2163,16 +2175,18 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   if (kernel == 1 || (kernel == 0 && (!diag_kind || Rd == 0)) || !diag_kind)
     return launch_dp(ctx, kind, G, R, d, max_clen);
   if (Rd == 0) Rd = 16;  // none fits the longest pair: the widest takes the rest
-  int Rc = 4;  // a CTA per pair: the smallest R that fits the longest pair
+  const int lanes = kernel == 3 ? 256 : 64;  // a CTA of 8 warps, or 2 warps, per pair
+  int Rc = 4;  // the smallest R that fits the longest pair
   for (int R2 : {4, 2, 1})
-    if (diag_ok(p->measure == TSIM_LCSS, max_qlen, max_clen, wd, R2, 256)) Rc = R2;
+    if (diag_ok(p->measure == TSIM_LCSS, max_qlen, max_clen, wd, R2, lanes)) Rc = R2;
   TSIM_TRY(arena_reserve(ctx, 2 * align256(sizeof(int) * (size_t)npairs) + 512));
   int* spill = arena_take<int>(ctx, npairs);
   int* nspill = arena_take<int>(ctx, 4);
   int* tmp = arena_take<int>(ctx, npairs);
   int* ntmp = arena_take<int>(ctx, 4);
-  if (kernel == 3)
-    TSIM_TRY(launch_dp_diag(ctx, kind, Rc, d, max_clen, spill, nspill, tmp, ntmp, 8));
+  if (kernel >= 3)
+    TSIM_TRY(launch_dp_diag(ctx, kind, Rc, d, max_clen, spill, nspill, tmp, ntmp,
+                            kernel == 3 ? 8 : 2));
   else
     TSIM_TRY(launch_dp_diag(ctx, kind, Rd, d, max_clen, spill, nspill, tmp, ntmp));
   d.order = spill;

@@ -272,8 +272,8 @@ TSIM_API int tsim_server_destroy(tsim_server* s);
  * d_pairs[2*i+1] = candidate index -- for DTW, LCSS or Frechet under p's
  * band / window / cost.  precision: 0 = FP32 (d_out32), 1 = compensated FP32
  * (d_out64), 2 = FP64 (d_out64).  kernel: 0 = automatic, 1 = round-striped
- * DP, 2 = anti-diagonal DP with a warp per pair, 3 = anti-diagonal DP with a
- * CTA per pair (pairs either cannot take fall back to 1).  Frechet
+ * DP, 2 = anti-diagonal DP with a warp per pair, 3 = with a CTA of 8 warps
+ * per pair, 4 = with 2 warps per pair (pairs they cannot take fall back to 1).  Frechet
  * values are squared distances; LCSS values are match counts. */
 TSIM_API int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision, int kernel,
                            const tsim_point* d_qpts, const int64_t* d_qoff, int max_qlen,

@@ -58,7 +58,7 @@ def test_dp_pairs_all_kernels(tsim, cuda_ctx, oracle, measure, kw, lo, hi):
                      for a, b in pairs])
     n_ = np.diff(qo)[pairs[:, 0]]
     m_ = np.diff(co)[pairs[:, 1]]
-    for kernel in (1, 2, 3):
+    for kernel in (1, 2, 3, 4):
         for precision in ((0,) if measure == "lcss" else (0, 1, 2)):
             o32 = torch.full((len(pairs),), float("nan"), dtype=torch.float32, device="cuda")
             o64 = torch.full((len(pairs),), float("nan"), dtype=torch.float64, device="cuda")
