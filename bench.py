@@ -36,6 +36,10 @@ UNIT = "queries/s"
 WORKLOAD = dict(workload="dtw_knn_batched_uneven", queries=64, candidates=16384, len_lo=64,
                 len_hi=512, band_pct=10, cost="squared_euclidean", k=10, seed=2024)
 DP_FLOPS_PER_CELL = 8  # 2 sub, mul, fma (2), 2 min, add
+# dram__bytes_read.sum + dram__bytes_write.sum of the survivor-round DP launch
+# of this workload (single stream, planner's R), one ncu capture of
+# `python -m cudaruntime1_gb300.profile_pass 1` on a GB300
+SURVIVOR_DP_DRAM_BYTES = 11230208
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -573,7 +577,8 @@ def main():
             "roofline": {
                 "kernel": "dp_diag_kernel<PolDtwSq,R>, survivor round (FP32 anti-diagonal DTW)",
                 "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                "frac": achieved / fp32_peak if fp32_peak else None,
+                "traffic": SURVIVOR_DP_DRAM_BYTES, "traffic_unit": "bytes per launch (ncu)",
                 "peak_source": "measured FP32 FMA probe kernel on this GPU (tsim_probe_fp32_tflops)",
                 "flops_per_cell": DP_FLOPS_PER_CELL, "cells_per_launch": surv_cells_launch,
                 "launch_ms": surv_ms,
