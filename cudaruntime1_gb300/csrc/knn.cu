@@ -93,6 +93,7 @@ struct KArgs {
   int Cw;
   float* seed_vals;         // [nq*S]
   float* thr;               // [nq]  pruning / abandon threshold
+  int* cnt0;                // [nq]  pairs the O(1) bound keeps (stage A, first half)
   int* cnt1;                // [nq]
   int* list1;               // [nq*C]
   int* cnt2;                // [nq]
@@ -393,6 +394,7 @@ __global__ void thresh_kernel(KArgs a) {
     }
     if (a.noprune) t = MEAS == M_LCSS ? -TSIM_INF : TSIM_INF;
     a.thr[q] = t;
+    a.cnt0[q] = 0;
     a.cnt1[q] = 0;
     a.cnt2[q] = 0;
     a.rcnt[q] = 0;
@@ -698,6 +700,20 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
   return fmaxf(fmaxf(acc, accr), lb1);
 }
 
+// append the pair to a per-query list (warp-aggregated)
+__device__ __forceinline__ void warp_append(bool take, int* count, int* list, int value) {
+  const unsigned ball = __ballot_sync(0xffffffffu, take);
+  if (!ball) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(ball) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(ball));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (take) list[base + __popc(ball & ((1u << lane) - 1))] = value;
+}
+
+// Stage A, first half: the pairs the O(1) bound keeps (seeds excluded) are
+// listed (in list2, free until the O(length) stage) ...
 template <int MEAS>
 __global__ void __launch_bounds__(kChunk) compact_kernel(KArgs a) {
   const int q = blockIdx.y;
@@ -708,22 +724,34 @@ __global__ void __launch_bounds__(kChunk) compact_kernel(KArgs a) {
     const bool seeded = (a.seedmap[(size_t)q * a.Cw + (c >> 5)] >> (c & 31)) & 1u;
     const float b = a.lb1[(size_t)q * a.C + c];
     pass = !seeded && (MEAS == M_LCSS ? (b >= t) : (b <= t));
-    if (pass) {  // the segment bound, only for pairs the O(1) bound keeps
-      const float sbnd = seg_bound<MEAS>(a, q, c, a.qlen[q], a.clen[c], b, t);
+  }
+  warp_append(pass, a.cnt0 + q, a.list2 + (size_t)q * a.C, c);
+}
+
+// ... and their segment bounds are computed with every lane of a warp busy
+// (the O(1) bound keeps few pairs of a chunk).  The bound is kept in place of
+// the O(1) bound: the O(length) stage and the round-1 order use the tighter
+// of it and their own.
+template <int MEAS>
+__global__ void __launch_bounds__(256) segfilter_kernel(KArgs a) {
+  const int q = blockIdx.y;
+  const int cnt = a.cnt0[q];
+  const float t = a.thr[q];
+  const int n = a.qlen[q];
+  const int start = blockIdx.x * blockDim.x;
+  const int stride = gridDim.x * blockDim.x;
+  for (int e0 = start; e0 < cnt; e0 += stride) {  // uniform per warp: whole warps iterate
+    const int e = e0 + threadIdx.x;
+    bool pass = false;
+    int c = 0;
+    if (e < cnt) {
+      c = a.list2[(size_t)q * a.C + e];
+      const float b = a.lb1[(size_t)q * a.C + c];
+      const float sbnd = seg_bound<MEAS>(a, q, c, n, a.clen[c], b, t);
       pass = MEAS == M_LCSS ? (sbnd >= t) : (sbnd <= t);
-      // kept in place of the O(1) bound: the O(length) stage and the round-1
-      // order use the tighter of it and their own bound
       if (pass) a.lb1[(size_t)q * a.C + c] = sbnd;
     }
-  }
-  const unsigned ball = __ballot_sync(0xffffffffu, pass);
-  if (ball) {
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(ball) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(a.cnt1 + q, __popc(ball));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (pass) a.list1[(size_t)q * a.C + base + __popc(ball & ((1u << lane) - 1))] = c;
+    warp_append(pass, a.cnt1 + q, a.list1 + (size_t)q * a.C, c);
   }
 }
 
@@ -1530,6 +1558,9 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   qtable_global_kernel<<<nq, 256, 0, s>>>(a, MEAS == M_EUCLID);  // segment bounds
   launched(ctx);
   compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
+  segfilter_kernel<MEAS><<<dim3(std::max(1, std::min(1024, (8 * ctx->num_sms + nq - 1) / nq)), nq),
+                           256, 0, s>>>(a);
+  launched(ctx);
   launched(ctx, 2);
   // CTAs per query of the grid-stride filter kernels: about 8 per SM over the
   // whole request, so a single query against a large database fills the GPU
@@ -1737,7 +1768,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
                 align256(sizeof(float) * nqC) + align256(sizeof(int) * nq * a.nch * a.T) +
                 align256(sizeof(int2) * nq * a.S) + align256(sizeof(unsigned) * nq * a.Cw) +
                 align256(sizeof(float) * nq * a.S) + align256(sizeof(float) * nq) +
-                4 * align256(sizeof(int) * (nq + 1)) + 2 * align256(sizeof(int) * nqC) +
+                5 * align256(sizeof(int) * (nq + 1)) + 2 * align256(sizeof(int) * nqC) +
                 align256(sizeof(int) * 4) + align256(sizeof(int2) * nqC) +
                 align256(sizeof(float) * nqC) +
                 align256(sizeof(unsigned long long) * nq * (size_t)a.nseg * 64) +
@@ -1793,6 +1824,7 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.seedmap = arena_take<unsigned>(ctx, (size_t)nq * a.Cw);
   a.seed_vals = arena_take<float>(ctx, (size_t)nq * a.S);
   a.thr = arena_take<float>(ctx, nq);
+  a.cnt0 = arena_take<int>(ctx, nq + 1);
   a.cnt1 = arena_take<int>(ctx, nq + 1);
   a.cnt2 = arena_take<int>(ctx, nq + 1);
   a.off2 = arena_take<int>(ctx, nq + 1);
