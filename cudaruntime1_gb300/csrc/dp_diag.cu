@@ -17,10 +17,11 @@
 // an LCSS window |i - j| <= delta when delta <= 31 R.  Pairs that fail the
 // condition are listed for the round-striped kernel instead (dp_kernels.cu).
 //
-// No shared memory: a lane's band columns come from integer ramps stepped
+// No row buffer in shared memory: a lane's band columns come from integer ramps stepped
 // by additions, the query points of its next group are prefetched into
 // registers one group ahead, and the candidate point of the next step is
-// loaded (through L1) one step ahead.  Occupancy is set by registers alone.
+// loaded one step ahead from the pair's copy in shared memory (through L1
+// for candidates too long to stage).
 //
 // Early abandon: every warping path crosses one of any two consecutive
 // anti-diagonals and DP values never decrease along a path, so the minimum
@@ -157,57 +158,6 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
     const int rrow = result_row<P>(n, m, a.delta);
     if (pl == 0) store_result(a, pid, P::border());
 
-    const Ramps rp = make_ramps(n, m, wd, kLcss);
-    const int row_q = (int)(rp.a / rp.d), row_r = (int)(rp.a % rp.d);
-    const int rnd_q = (int)(kRound * rp.a / rp.d), rnd_r = (int)(kRound * rp.a % rp.d);
-
-    // the lane's next group (first row i1, its band ramps, prefetched points)
-    int i1 = R * pl;
-    Ramp L1 = rp.lo_at(i1), H1 = rp.hi_at(i1);
-    float nqx[R], nqy[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const float2 p = i1 + r < n ? __ldg(A + i1 + r) : make_float2(0.f, 0.f);
-      nqx[r] = p.x;
-      nqy[r] = p.y;
-    }
-    int i0 = 0;
-    float qx[R], qy[R];
-    int base[R];      // step at which row r's band starts: t - base = column - lo
-    unsigned wdt[R];  // band width - 1 (empty rows: never in band)
-    V left[R], left2[R];  // each row's values one and two columns back
-    // switch to the next group: rows from the ramps, points from the prefetch
-    auto take_next = [&]() -> int {
-      i0 = i1;
-      Ramp L = L1, H = H1;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int lo = rp.lo(L), hi = rp.hi(H);
-        const bool ok = i0 + r < n && hi >= lo;
-        base[r] = ok ? i0 + r + lo : 0x3fffffff;
-        wdt[r] = ok ? (unsigned)(hi - lo) : 0u;
-        qx[r] = nqx[r];
-        qy[r] = nqy[r];
-        left[r] = left2[r] = P::border();
-        if (r + 1 < R) {
-          rp.step(L, row_q, row_r);
-          rp.step(H, row_q, row_r);
-        }
-      }
-      i1 += kRound;
-      rp.step(L1, rnd_q, rnd_r);
-      rp.step(H1, rnd_q, rnd_r);
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const float2 p = i1 + r < n ? __ldg(A + i1 + r) : make_float2(0.f, 0.f);
-        nqx[r] = p.x;
-        nqy[r] = p.y;
-      }
-      if (i1 >= n) return 0x7fffffff;  // step at which the following group starts
-      const int lo = rp.lo(L1), hi = rp.hi(H1);
-      return hi >= lo ? i1 + lo : 0x7fffffff;
-    };
-    int ns = take_next();
     if (W == 1) {
       __syncwarp();
       if (staged)
@@ -221,46 +171,124 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
       __syncthreads();
     }
     const float2* C = staged ? cs : B;
+    // candidate point of column j; columns outside 0 .. m-1 (cells outside
+    // the band, whose values are masked) read point m-1
+    auto cand = [&](int j) -> float2 { return C[min((unsigned)j, (unsigned)(m - 1))]; };
+
+    const Ramps rp = make_ramps(n, m, wd, kLcss);
+    const int row_q = (int)(rp.a / rp.d), row_r = (int)(rp.a % rp.d);
+    const int rnd_q = (int)(kRound * rp.a / rp.d), rnd_r = (int)(kRound * rp.a % rp.d);
+
+    // The lane's current group (first row i0) and its next one (first row
+    // i1, starting at step ns), prepared ahead: a switch is register moves
+    // only.  Lanes switch at different steps, so whatever a switch executes
+    // the warp issues once per lane; the preparation (band ramps, point
+    // loads) instead runs for every lane that needs it at once, on every
+    // 16th step -- a lane's switches are at least 32 R W steps apart.
+    int i1 = R * pl;
+    Ramp L1 = rp.lo_at(i1), H1 = rp.hi_at(i1);  // band ramps at row i1
+    float nqx[R], nqy[R];
+    int nbase[R];
+    unsigned nwdt[R];
+    int ns;  // step of the next group's first cell (-1: not prepared yet)
+    float2 ncand;
+    auto prepare = [&]() {
+      Ramp L = L1, H = H1;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int lo = rp.lo(L), hi = rp.hi(H);
+        const bool ok = i1 + r < n && hi >= lo;
+        nbase[r] = ok ? i1 + r + lo : 0x3fffffff;
+        nwdt[r] = ok ? (unsigned)(hi - lo) : 0u;
+        const float2 p = i1 + r < n ? __ldg(A + i1 + r) : make_float2(0.f, 0.f);
+        nqx[r] = p.x;
+        nqy[r] = p.y;
+        if (r + 1 < R) {
+          rp.step(L, row_q, row_r);
+          rp.step(H, row_q, row_r);
+        }
+      }
+      const int lo = rp.lo(L1), hi = rp.hi(H1);
+      ns = i1 < n && hi >= lo ? i1 + lo : 0x7fffffff;  // its first cell's step
+      ncand = cand(lo);                                 // and column
+    };
+    int i0 = 0;
+    float qx[R], qy[R];
+    int base[R];      // step at which row r's band starts: t - base = column - lo
+    unsigned wdt[R];  // band width - 1 (empty rows: never in band)
+    V left[R], left2[R];  // each row's values one and two columns back
+    auto take_next = [&]() {
+      i0 = i1;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        base[r] = nbase[r];
+        wdt[r] = nwdt[r];
+        qx[r] = nqx[r];
+        qy[r] = nqy[r];
+        left[r] = left2[r] = P::border();
+      }
+      ns = -1;  // until the next preparation
+    };
+    auto advance = [&]() {
+      i1 += kRound;
+      rp.step(L1, rnd_q, rnd_r);
+      rp.step(H1, rnd_q, rnd_r);
+      prepare();
+    };
+    prepare();
+    take_next();
+    advance();
+    // lane 0's first group holds row 0, whose row above is the virtual row -1
+    // (+inf, with D(-1,-1) = origin)
+    bool first = pl == 0;
     V out = P::border();
     V prev_raw = P::border();  // the shuffled value of the previous step
+    V dg0 = P::origin();       // D(-1,-1), read once
     float2 cw[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) cw[r] = make_float2(0.f, 0.f);
-    // candidate point of the next step, loaded one step ahead
-    float2 cnext = C[min(max(-i0, 0), m - 1)];
+    // candidate point of the next step, loaded one step ahead (at a switch,
+    // the prepared group's first column)
+    float2 cnext = cand(-i0);
     V result = P::border();
     bool holds = false;
     bool alive = true;
     float mprev = TSIM_INF;
+    const bool check = P::kMin && a.thr != nullptr;
     const int t_end = n + m - 2;
     int t_ab = t_end;
 
+    // two steps per loop iteration: the registers of the rows' values one and
+    // two columns back and of the candidate points alternate between the two
+    // halves instead of being copied every step
+#pragma unroll 2
     for (int t = 0; t <= t_end; ++t) {
       if (t == ns) {  // this lane's next group starts now
+        if ((unsigned)(rrow - i0) < (unsigned)R) {  // it holds the result row
 #pragma unroll
-        for (int r = 0; r < R; ++r)
-          if (i0 + r == rrow) {
-            result = left[r];
-            holds = true;
-          }
-        ns = take_next();
+          for (int r = 0; r < R; ++r)
+            if (i0 + r == rrow) {
+              result = left[r];
+              holds = true;
+            }
+        }
+        take_next();
+        first = false;
+        cnext = ncand;
       }
+      if ((t & 15) == 0 && ns < 0) advance();
       // the last row of the previous lane's group, one column back: the row
-      // above this lane's first row (lane 0's first group reads the virtual
-      // row -1 instead, whose only finite cell is D(-1,-1) = origin)
+      // above this lane's first row
       V raw = shfl_lane(out, (lane + 31) & 31);
       if (W > 1 && lane == 0) raw = xbuf[(t + 1) & 1][(warp + W - 1) % W];  // the previous warp's
-      const bool first = pl == 0 && i0 == 0;
       const V up_in = first ? P::border() : raw;
-      const V dg_in = first ? (t == 0 ? P::origin() : P::border()) : prev_raw;
+      const V dg_in = first ? dg0 : prev_raw;
+      dg0 = P::border();
       prev_raw = raw;
 #pragma unroll
       for (int r = R - 1; r > 0; --r) cw[r] = cw[r - 1];
       cw[0] = cnext;
-      {
-        const int inext = t + 1 == ns ? i1 : i0;
-        cnext = C[min(max(t + 1 - inext, 0), m - 1)];
-      }
+      cnext = cand(t + 1 - i0);
       // row r computes column t - i0 - r: its up neighbour is row r-1 one step
       // ago and its diagonal neighbour row r-1 two steps ago, so rows are
       // visited last to first before row r-1 is overwritten
@@ -276,9 +304,10 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
         left[r] = v;
       }
       out = left[R - 1];
-      if (P::kMin && a.thr) {
+      if (check && (t & 15) >= 14) {
         // minimum of this anti-diagonal's cells, all R rows (masked cells are
-        // +inf): three-operand mins, then a last two-operand one if needed
+        // +inf): three-operand mins, then a last two-operand one if needed;
+        // taken on the last two steps of every 16
         float mstep = vf(left[0]);
         int r = 1;
 #pragma unroll

@@ -113,6 +113,7 @@ struct KArgs {
   int* spill2;              // the list between passes of the anti-diagonal kernel
   int* nspill2;
   int rdiag;                // rows per lane-group of the anti-diagonal kernel (0: off)
+  int rdiag_shape;          // the smallest R a warp per pair admits for the longest pair
   int rdiag_cta;            // the same for a CTA per pair (0: no R fits the longest pair)
   int rdiag_w2;             // the same for two warps per pair
   float4* qtab;             // [nq*tstride] query sparse tables (global memory)
@@ -1359,10 +1360,16 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
                          kind == DP_FRECHET_SQC;
   if (!diag_kind || a.rdiag == 0) return launch_dp(ctx, kind, G, R, d, a.max_clen);
   const bool twofloat = kind == DP_DTW_SQC || kind == DP_DTW_EUC || kind == DP_FRECHET_SQC;
-  if (latency && a.rdiag_cta > 0 && a.rdiag >= (twofloat ? 4 : 8)) {
+  // Latency rounds (few pairs, one wave) pick the kernel by the pair shape
+  // (not by the throughput-tuned R): compensated pairs take two warps per
+  // pair while 64 lanes need at most 2 rows each (lone 512-point pair: 188 us
+  // against 212 us on a warp and 196 us on a CTA; 640 pairs: 207, 234 and
+  // 432 us), longer shapes a CTA per pair.
+  const bool w2 = latency && twofloat && a.rdiag_w2 > 0 && a.rdiag_w2 <= 2;
+  if (!w2 && latency && a.rdiag_cta > 0 && a.rdiag_shape >= (twofloat ? 4 : 8)) {
     TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag_cta, d, a.max_clen, a.spill, a.nspill, a.spill2,
                             a.nspill2, 8));
-  } else if (latency && twofloat && a.rdiag >= 2 && a.rdiag_w2 > 0) {
+  } else if (w2 || (latency && twofloat && a.rdiag_shape >= 2 && a.rdiag_w2 > 0)) {
     // two warps per pair: a compensated row per lane and step, for a barrier
     // of two warps
     TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag_w2, d, a.max_clen, a.spill, a.nspill, a.spill2,
@@ -1753,6 +1760,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
         a.rdiag_w2 = R;
         break;
       }
+    a.rdiag_shape = a.rdiag;
     if (a.plain || (p->flags & TSIM_FLAG_NO_PRUNE)) a.rdiag = 0;
   }
   a.cost = p->cost;
