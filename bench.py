@@ -399,6 +399,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--kernels-only", action="store_true",
                     help="only the warm-up and timed steps (for profiler launch lists)")
+    ap.add_argument("--save-tuning", default=None,
+                    help="write the autotuner's choices to this file")
+    ap.add_argument("--load-tuning", default=None,
+                    help="take the launch choices from this file instead of autotuning "
+                         "(profiled runs: the autotuner would time the profiler's serialised launches)")
     ap.add_argument("--workload", default="dtw_knn_batched_uneven",
                     choices=["dtw_knn_batched_uneven", "serving"] + list(KNN_WORKLOADS))
     ap.add_argument("--serve-seconds", type=float, default=5.0)
@@ -446,7 +451,13 @@ def main():
 
     # launch choices (rows per lane-group, concurrent query chunks) picked by
     # the autotuner on this request before anything is timed
-    tune = ctx.autotune(db, qpt.data_ptr(), qot.data_ptr(), nq, maxq, "dtw", k, reps=5, **kw)
+    if args.load_tuning:
+        ctx.load_tuning(args.load_tuning)
+        tune = {"loaded": args.load_tuning}
+    else:
+        tune = ctx.autotune(db, qpt.data_ptr(), qot.data_ptr(), nq, maxq, "dtw", k, reps=5, **kw)
+    if args.save_tuning:
+        ctx.save_tuning(args.save_tuning)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()

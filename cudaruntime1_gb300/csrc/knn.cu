@@ -280,7 +280,7 @@ __device__ __forceinline__ bool ends_align(int n, int m, int delta) {
 template <int MEAS>
 __global__ void __launch_bounds__(kChunk) lb1_kernel(KArgs a) {
   __shared__ unsigned long long keys[kChunk];
-  __shared__ unsigned long long red[33];
+  __shared__ SelScratch red;
   __shared__ unsigned long long sel[64];
   const int q = blockIdx.y, chunk = blockIdx.x;
   const int c = chunk * kChunk + threadIdx.x;
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(kChunk) lb1_kernel(KArgs a) {
 template <int MEAS>
 __global__ void __launch_bounds__(kSelThreads) seed_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ unsigned long long red[33];
+  __shared__ SelScratch red;
   __shared__ unsigned long long sel[64];
   const int q = blockIdx.x;
   const int N = a.nch * a.T;
@@ -931,7 +931,7 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
 // tighten the threshold for the rest.  Taken entries are consumed (-1).
 template <int MEAS>
 __global__ void __launch_bounds__(kSelThreads) r1_select_kernel(KArgs a) {
-  __shared__ unsigned long long red[33];
+  __shared__ SelScratch red;
   __shared__ unsigned long long sel[64];
   const int q = blockIdx.x;
   const int ns = (a.cnt2[q] + kSeg - 1) / kSeg;
@@ -1057,27 +1057,52 @@ __global__ void shape_hist_kernel(KArgs a) {
   }
 }
 
-// exclusive scan of the shape histogram in place (one CTA of 1024 threads)
+// exclusive scan of the shape histogram in place (one CTA of 1024 threads,
+// 16 consecutive buckets per thread read as four int4): warp scans by
+// shuffles, then a scan of the 32 warp totals
 __global__ void __launch_bounds__(1024) shape_scan_kernel(KArgs a) {
-  __shared__ int part[1024];
-  constexpr int per = kNumShapes / 1024;
-  int loc[per], s = 0;
-  for (int i = 0; i < per; ++i) {
-    loc[i] = a.shape_cnt[threadIdx.x * per + i];
-    s += loc[i];
+  static_assert(kNumShapes == 1024 * 16, "16 buckets per thread");
+  __shared__ int wsum[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int4* h = reinterpret_cast<int4*>(a.shape_cnt) + threadIdx.x * 4;
+  int4 v[4];
+  int s = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    v[i] = h[i];
+    s += v[i].x + v[i].y + v[i].z + v[i].w;
   }
-  part[threadIdx.x] = s;
+  int inc = s;  // inclusive scan over the warp
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) wsum[warp] = inc;
   __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
-    __syncthreads();
-    part[threadIdx.x] += v;
-    __syncthreads();
+  if (warp == 0) {
+    int w = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += u;
+    }
+    wsum[lane] = w;  // inclusive over warps
   }
-  int run = part[threadIdx.x] - s;
-  for (int i = 0; i < per; ++i) {
-    a.shape_cnt[threadIdx.x * per + i] = run;
-    run += loc[i];
+  __syncthreads();
+  int run = inc - s + (warp > 0 ? wsum[warp - 1] : 0);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int4 o;
+    o.x = run;
+    run += v[i].x;
+    o.y = run;
+    run += v[i].y;
+    o.z = run;
+    run += v[i].z;
+    o.w = run;
+    run += v[i].w;
+    h[i] = o;
   }
 }
 
@@ -1114,7 +1139,7 @@ __device__ __forceinline__ void entry(const KArgs& a, int q, int i, int base, in
 template <int MEAS, int MODE>
 __global__ void __launch_bounds__(kSelThreads) seg_select_kernel(KArgs a, int K) {
   __shared__ unsigned long long keys[kSeg];
-  __shared__ unsigned long long red[33];
+  __shared__ SelScratch red;
   __shared__ unsigned long long sel[64];
   const int q = blockIdx.y, seg = blockIdx.x;
   const int N = MODE == 0 ? a.cnt2[q] : a.S + a.M + a.fcnt[q];
@@ -1144,7 +1169,7 @@ __global__ void __launch_bounds__(kSelThreads) seg_select_kernel(KArgs a, int K)
 
 template <int MEAS>
 __global__ void __launch_bounds__(kSelThreads) final_select_kernel(KArgs a) {
-  __shared__ unsigned long long red[33];
+  __shared__ SelScratch red;
   __shared__ unsigned long long sel[64];
   const int q = blockIdx.x;
   const int ns = (a.S + a.M + a.fcnt[q] + kSeg - 1) / kSeg;
@@ -1217,97 +1242,111 @@ __device__ __forceinline__ double gamma_c(int meas, int P) {
   return (cost + (4.0 * P + 32.0) * u2 + (P + 8.0) * e53) * 1.25;
 }
 
-// Sort the re-score set by compensated value; pairs whose values are within
+// Rank of each re-score entry in (value, candidate) order: a warp per query,
+// the entries staged in shared memory, each lane counting the entries before
+// its own (ties by entry index, so ranks are distinct).  kRankWarps queries
+// per CTA, at most kMaxRC entries each.
+constexpr int kRankWarps = 4;
+constexpr int kMaxRC = 256;
+struct RankSlot {
+  double v[kMaxRC];
+  int c[kMaxRC];
+  unsigned char ord[kMaxRC];  // entry index by rank
+};
+__device__ __forceinline__ bool before(double dv, int dc, int di, double v, int c, int i) {
+  return dv < v || (dv == v && (dc < c || (dc == c && di < i)));
+}
+__device__ __forceinline__ int rank_of(const RankSlot& S, int n, int i) {
+  int r = 0;
+  for (int j = 0; j < n; ++j) r += before(S.v[j], S.c[j], j, S.v[i], S.c[i], i) ? 1 : 0;
+  return r;
+}
+
+// Order the re-score set by compensated value; pairs whose values are within
 // the error bound of a neighbour in that order (chains of them) cannot be
-// ordered without FP64 and are sent to the FP64 re-score.  One thread/query.
+// ordered without FP64 and are sent to the FP64 re-score.
 template <int MEAS>
-__global__ void cluster_kernel(KArgs a) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32 * kRankWarps) cluster_kernel(KArgs a) {
+  __shared__ RankSlot slots[kRankWarps];
+  const int lane = threadIdx.x & 31;
+  RankSlot& S = slots[threadIdx.x >> 5];
+  const int q = blockIdx.x * kRankWarps + (threadIdx.x >> 5);
   if (q >= a.nq) return;
-  const int cnt = a.rcnt[q];
+  const int n = min(a.rcnt[q], kMaxRC);
   const int2* rp = a.rpairs + (size_t)q * a.RC;
   const double* rv = a.rdc + (size_t)q * a.RC;
   int2* r64p = a.r64pairs + (size_t)q * a.RC;
   // compensated DTW values: gamma_c; FP32 values: twice their bound
   const double g = compensated_rescore(MEAS) ? gamma_c(MEAS, a.qlen[q] + a.max_clen)
                                              : 2.0 * gamma_dp(MEAS, a.qlen[q], a.max_clen);
-  unsigned char ord[256];
-  int n = 0;
-  for (int i = 0; i < cnt && i < 256; ++i) {
-    int p = n++;
-    while (p > 0) {
-      const int j = ord[p - 1];
-      if (rv[j] < rv[i] || (rv[j] == rv[i] && rp[j].y < rp[i].y)) break;
-      ord[p] = ord[p - 1];
-      --p;
-    }
-    ord[p] = (unsigned char)i;
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
+  for (int i = lane; i < n; i += 32) {
+    S.v[i] = rv[i];
+    S.c[i] = rp[i].y;
   }
-  for (int i = 0; i < a.RC; ++i) r64p[i] = make_int2(q, -1);
+  for (int i = lane; i < a.RC; i += 32) r64p[i] = make_int2(q, -1);
+  __syncwarp();
+  for (int i = lane; i < n; i += 32) S.ord[rank_of(S, n, i)] = (unsigned char)i;
+  __syncwarp();
   int sent = 0;
-  for (int p = 0; p < n; ++p) {
-    const int i = ord[p];
-    const double v = rv[i];
-    if (!(v < __longlong_as_double(0x7ff0000000000000ll))) continue;  // infeasible: exact
+  for (int p = lane; p < n; p += 32) {
+    const int i = S.ord[p];
+    const double v = S.v[i];
+    if (!(v < inf)) continue;  // infeasible: exact
     bool amb = a.force64 != 0;
     if (p > 0) {
-      const double u = rv[ord[p - 1]];
+      const double u = S.v[S.ord[p - 1]];
       if (v - u <= g * (u + v)) amb = true;
     }
     if (p + 1 < n) {
-      const double w = rv[ord[p + 1]];
-      if (w < __longlong_as_double(0x7ff0000000000000ll) && w - v <= g * (v + w)) amb = true;
+      const double w = S.v[S.ord[p + 1]];
+      if (w < inf && w - v <= g * (v + w)) amb = true;
     }
     if (amb) {
       r64p[i] = rp[i];
       ++sent;
     }
   }
-  if (sent) atomicAdd(a.n64, sent);
+  for (int o = 16; o; o >>= 1) sent += __shfl_xor_sync(0xffffffffu, sent, o);
+  if (lane == 0 && sent) atomicAdd(a.n64, sent);
 }
 
 // final order: FP64 value for cluster members, compensated value otherwise
-// (the two agree in order across clusters); ties by candidate index
+// (the two agree in order across clusters); ties by candidate index.  The
+// first k entries by rank are the result; a warp per query.
 template <int MEAS>
-__global__ void final_sort_kernel(KArgs a) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32 * kRankWarps) final_sort_kernel(KArgs a) {
+  __shared__ RankSlot slots[kRankWarps];
+  const int lane = threadIdx.x & 31;
+  RankSlot& S = slots[threadIdx.x >> 5];
+  const int q = blockIdx.x * kRankWarps + (threadIdx.x >> 5);
   if (q >= a.nq) return;
-  const int cnt = a.rcnt[q];
+  const int n = min(a.rcnt[q], kMaxRC);
   const int2* rp = a.rpairs + (size_t)q * a.RC;
   const double* rc = a.rdc + (size_t)q * a.RC;
   const double* r64 = a.r64 + (size_t)q * a.RC;
   const int2* r64p = a.r64pairs + (size_t)q * a.RC;
-  double last_d = -1.0;
-  int last_c = -1;
-  for (int e = 0; e < a.k; ++e) {
-    // selection of the next (d, c) after (last_d, last_c)
-    double bd = __longlong_as_double(0x7ff0000000000000ll);
-    int bc = -1;
-    bool found = false;
-    for (int i = 0; i < cnt; ++i) {
-      double d = r64p[i].y >= 0 ? r64[i] : rc[i];
-      if (is_squared(MEAS)) d = __dsqrt_rn(d);
-      const int c = rp[i].y;
-      const bool after = d > last_d || (d == last_d && c > last_c);
-      if (!after) continue;
-      if (!found || d < bd || (d == bd && c < bc)) {
-        bd = d;
-        bc = c;
-        found = true;
-      }
+  for (int i = lane; i < n; i += 32) {
+    double d = r64p[i].y >= 0 ? r64[i] : rc[i];
+    if (is_squared(MEAS)) d = __dsqrt_rn(d);
+    S.v[i] = d;
+    S.c[i] = rp[i].y;
+  }
+  __syncwarp();
+  for (int i = lane; i < n; i += 32) {
+    const int r = rank_of(S, n, i);
+    if (r < a.k) {
+      const size_t o = (size_t)q * a.k + r;
+      a.ids[o] = S.c[i];
+      a.dists[o] = __double2float_rn(S.v[i]);
+      if (a.dists64) a.dists64[o] = S.v[i];
     }
+  }
+  for (int e = n + lane; e < a.k; e += 32) {
     const size_t o = (size_t)q * a.k + e;
-    if (found) {
-      a.ids[o] = bc;
-      a.dists[o] = __double2float_rn(bd);
-      if (a.dists64) a.dists64[o] = bd;
-      last_d = bd;
-      last_c = bc;
-    } else {
-      a.ids[o] = -1;
-      a.dists[o] = TSIM_INF;
-      if (a.dists64) a.dists64[o] = __longlong_as_double(0x7ff0000000000000ll);
-    }
+    a.ids[o] = -1;
+    a.dists[o] = TSIM_INF;
+    if (a.dists64) a.dists64[o] = __longlong_as_double(0x7ff0000000000000ll);
   }
 }
 
@@ -1428,7 +1467,7 @@ int finish_knn(tsim_ctx* ctx, KArgs& a, int dpc, int dp64) {
     // compensated FP32 re-score of the set, then FP64 only for the pairs it
     // cannot order (near-ties within the compensated error bound)
     if (compensated_rescore(MEAS)) TSIM_TRY(run_dp(ctx, a, dpc, 32, 1, r, true));
-    cluster_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+    cluster_kernel<MEAS><<<(nq + kRankWarps - 1) / kRankWarps, 32 * kRankWarps, 0, s>>>(a);
     r.pairs = a.r64pairs;
     r.out64 = a.r64;
     if (is_dp(MEAS)) {
@@ -1438,7 +1477,7 @@ int finish_knn(tsim_ctx* ctx, KArgs& a, int dpc, int dp64) {
                a.r64, nullptr};
       TSIM_TRY(launch_pairwise64(ctx, MEAS == M_HAUSDORFF ? TSIM_HAUSDORFF : TSIM_EUCLIDEAN, p));
     }
-    final_sort_kernel<MEAS><<<(nq + 127) / 128, 128, 0, s>>>(a);
+    final_sort_kernel<MEAS><<<(nq + kRankWarps - 1) / kRankWarps, 32 * kRankWarps, 0, s>>>(a);
     TSIM_CUDA(cudaGetLastError());
     launched(ctx, 2);
     stage_end(ctx);

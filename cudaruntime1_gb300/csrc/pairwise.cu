@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(kSelThreads)
     mbr_knn_kernel(const float4* __restrict__ qbox, const float4* __restrict__ cbox, int num_t2,
                    int k, unsigned long long* __restrict__ gkeys, int* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ unsigned long long red[33];
+  __shared__ SelScratch red;
   const int q = blockIdx.x;
   unsigned long long* keys =
       gkeys ? gkeys + (size_t)q * num_t2 : reinterpret_cast<unsigned long long*>(smem_raw);

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kFilterThreads)
                       int n, int m, float eps, int K, unsigned long long* __restrict__ gkeys,
                       int2* __restrict__ pairs) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ unsigned long long red[33];
+  __shared__ SelScratch red;
   const int q = blockIdx.x;
   // envelope of query point v*n/m for each candidate position v, m entries
   float4* envv = reinterpret_cast<float4*>(smem_raw);

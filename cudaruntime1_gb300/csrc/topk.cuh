@@ -42,26 +42,110 @@ __device__ __forceinline__ unsigned long long block_min_u64(unsigned long long v
   return r;
 }
 
-// Extract the K smallest packed keys of keys[0..N) in ascending order into
-// out[0..K) (~0 when fewer than K remain).  Keys must be unique; each
-// extracted key is overwritten with ~0 by the thread that owns its slot.
-__device__ inline void block_select_k(unsigned long long* keys, int N, int K,
-                                      unsigned long long* out, unsigned long long* red) {
-  for (int k = 0; k < K; ++k) {
-    unsigned long long best = ~0ull;
-    int bpos = -1;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-      unsigned long long x = keys[i];
-      if (x < best) {
-        best = x;
-        bpos = i;
+// Shared scratch of block_select_k.
+struct SelScratch {
+  int hist[256];
+  unsigned long long cand[64];
+  unsigned long long pfx;  // digits of the K-th smallest key fixed so far
+  int need;                // keys still to take at and above the current digit
+  int shift;               // bit position of the last digit fixed
+  int cnt;
+  int stop;                // 1: the keys up to pfx at `shift` are the K; 2: all keys
+};
+
+// The K (<= 64) smallest packed keys of keys[0..N) (unique; ~0 = absent) in
+// ascending order into out[0..K) (~0 when fewer than K are present).  All
+// threads of the block must call it; out is visible to all on return.
+// Radix selection from the top 8-bit digit down: a histogram of the keys
+// that share the digits fixed so far locates the digit of the K-th smallest
+// key; it stops when that digit's bin holds exactly the keys still needed
+// (unique keys: at the last digit at the latest), then the at most K keys
+// at or below that prefix are collected and ranked.
+__device__ inline void block_select_k(const unsigned long long* keys, int N, int K,
+                                      unsigned long long* out, SelScratch& S) {
+  if (K <= 0) return;
+  if (threadIdx.x == 0) {
+    S.pfx = 0;
+    S.need = K;
+    S.stop = 0;
+    S.shift = 64;
+  }
+  for (int shift = 56; shift >= 0; shift -= 8) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) S.hist[i] = 0;
+    __syncthreads();  // also publishes the previous pass's prefix
+    const unsigned long long pfx = S.pfx;
+    const int hs = shift + 8;
+    // warp-aggregated counts: most keys share a few bins of the top digits
+    for (int b = 0; b < N; b += blockDim.x) {
+      const int i = b + threadIdx.x;
+      const unsigned long long x = i < N ? keys[i] : ~0ull;
+      const bool in = x != ~0ull && (hs >= 64 || (x >> hs) == (pfx >> hs));
+      const unsigned bin = in ? (unsigned)(x >> shift) & 255u : 256u;
+      const unsigned same = __match_any_sync(0xffffffffu, bin);
+      if (in && (threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&S.hist[bin], __popc(same));
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      const int lane = threadIdx.x;
+      int c[8], sum = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        c[j] = S.hist[lane * 8 + j];
+        sum += c[j];
+      }
+      int inc = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += u;
+      }
+      const int total = __shfl_sync(0xffffffffu, inc, 31);
+      const int need = S.need;
+      if (total < need) {  // fewer keys than K at all (first pass only)
+        if (lane == 0) S.stop = 2;
+      } else if (inc - sum < need && need <= inc) {  // the lane holding the need-th key
+        int run = inc - sum, d = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (run + c[j] >= need) {
+            d = j;
+            break;
+          }
+          run += c[j];
+        }
+        const int bin = c[d];
+        S.pfx = pfx | ((unsigned long long)(lane * 8 + d) << shift);
+        S.need = need - run;
+        S.shift = shift;
+        if (bin == need - run) S.stop = 1;
       }
     }
-    const unsigned long long g = block_min_u64(best, red);
-    if (g != ~0ull && best == g) keys[bpos] = ~0ull;
-    if (threadIdx.x == 0) out[k] = g;
     __syncthreads();
+    if (S.stop) break;
   }
+  const int stop = S.stop, sh = S.shift;
+  const unsigned long long lim = sh < 64 ? S.pfx >> sh : 0ull;
+  if (threadIdx.x == 0) S.cnt = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const unsigned long long x = keys[i];
+    if (x == ~0ull || (stop != 2 && (x >> sh) > lim)) continue;
+    const int p = atomicAdd(&S.cnt, 1);
+    if (p < 64) S.cand[p] = x;
+  }
+  __syncthreads();
+  const int cnt = min(min(S.cnt, K), 64);
+  for (int t = threadIdx.x; t < K; t += blockDim.x) {
+    if (t < cnt) {
+      const unsigned long long x = S.cand[t];
+      int r = 0;
+      for (int j = 0; j < cnt; ++j) r += S.cand[j] < x ? 1 : 0;
+      out[r] = x;
+    } else {
+      out[t] = ~0ull;
+    }
+  }
+  __syncthreads();
 }
 
 __device__ __forceinline__ int key_index(unsigned long long key) {
