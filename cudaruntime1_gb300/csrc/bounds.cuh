@@ -33,11 +33,20 @@ __device__ __forceinline__ float box_box_d2_rd(float4 a, float4 b) {
   return __fadd_rd(__fmul_rd(dx, dx), __fmul_rd(dy, dy));
 }
 
-// Floor division with a non-negative remainder, for incremental stepping.
-struct FloorDiv {
-  int q, r, d;
-  __device__ __forceinline__ void init(long long num, int den) {
-    d = den;
+// q = floor(num / den), r = num - q den (0 <= r < den) for den > 0 and a
+// quotient that fits an int.  32-bit arithmetic when the numerator fits (a
+// 64-bit division is a long software sequence), 64-bit otherwise.
+__device__ __forceinline__ void divmod_floor(long long num, int den, int& q, int& r) {
+  if (num >= -2147483647ll && num <= 2147483647ll) {
+    const int n32 = (int)num;
+    int qq = n32 / den, rr = n32 - qq * den;
+    if (rr < 0) {
+      rr += den;
+      qq -= 1;
+    }
+    q = qq;
+    r = rr;
+  } else {
     long long qq = num / den, rr = num % den;
     if (rr < 0) {
       rr += den;
@@ -45,6 +54,20 @@ struct FloorDiv {
     }
     q = (int)qq;
     r = (int)rr;
+  }
+}
+__device__ __forceinline__ int floordiv_i(long long num, int den) {
+  int q, r;
+  divmod_floor(num, den, q, r);
+  return q;
+}
+
+// Floor division with a non-negative remainder, for incremental stepping.
+struct FloorDiv {
+  int q, r, d;
+  __device__ __forceinline__ void init(long long num, int den) {
+    d = den;
+    divmod_floor(num, den, q, r);
   }
   // num += dq * d + dr with 0 <= dr < d
   __device__ __forceinline__ void step(int dq, int dr) {

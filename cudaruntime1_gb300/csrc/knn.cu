@@ -653,8 +653,8 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
     if (b1 < b0) continue;
     int lo = 0, hi = n - 1;
     if (banded) {
-      lo = (int)max(0ll, -floordiv_ll(-((long long)b0 * (n - 1) - W), m - 1));
-      hi = (int)min((long long)n - 1, floordiv_ll((long long)b1 * (n - 1) + W, m - 1));
+      lo = max(0, floordiv_i((long long)b0 * (n - 1) - W + (m - 2), m - 1));  // ceil
+      hi = min(n - 1, floordiv_i((long long)b1 * (n - 1) + W, m - 1));
     }
     if (lo > hi) return TSIM_INF;  // a column with no admissible row: infeasible
     const float4 qx = qtable_box(T, lo, hi);
@@ -673,11 +673,13 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
   if (n > 2) {
     const int L = (n - 2 + kRowSegs - 1) / kRowSegs;
     const long long d = n - 1, sl = (long long)L * (m - 1);
-    const long long K = W / d + 1;
+    const long long K = floordiv_i(W, (int)d) + 1;
     long long xl = (long long)(m - 1) - W + (d - 1) + K * d;  // lo numerator at row 1
     long long xh = (long long)L * (m - 1) + W;                // hi numerator at row L
-    int ql = (int)(xl / d), rl = (int)(xl % d), qh = (int)(xh / d), rh = (int)(xh % d);
-    const int sq = (int)(sl / d), sr = (int)(sl % d);
+    int ql, rl, qh, rh, sq, sr;
+    divmod_floor(xl, (int)d, ql, rl);
+    divmod_floor(xh, (int)d, qh, rh);
+    divmod_floor(sl, (int)d, sq, sr);
     int sf = 0;
     for (int r0 = 1; r0 <= n - 2; r0 += L) {
       const int r1 = min(n - 2, r0 + L - 1);
@@ -767,12 +769,14 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
   const int n = a.qlen[q];
   const float4 qb = a.qbox[q];
   const float t = a.thr[q];
-  // a query longer than the table was sized for passes every pair (the
-  // bound is skipped, never guessed)
+  // the query's sparse table of row boxes, built in global memory by
+  // qtable_global_kernel (read through L1: a copy in shared memory per CTA
+  // held occupancy to 3 CTAs per SM); a query longer than the table was
+  // sized for passes every pair (the bound is skipped, never guessed)
   constexpr bool kTable = MEAS == M_DTW || MEAS == M_LCSS;
   const bool use_table = n <= a.max_qlen;
   QTable T;
-  if (kTable && use_table) qtable_build(T, A, n, reinterpret_cast<float4*>(smem_raw));
+  if (kTable && use_table) T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
   const float e2 = __fmul_ru(a.eps, 1.0f + 1.0f / 1048576.0f);
   // LCSS: an occupancy grid of the query in shared memory, cells of side
   // gs >= 1.01 eps, each query point marking its cell and the 8 around it.
@@ -780,7 +784,7 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
   // lies in a marked cell: its cell index differs from that query point's
   // by at most 1 per axis, the index arithmetic's rounding (< 1e-3 cell)
   // being covered by the 1 % margin.  Points outside the grid match nothing.
-  uint32_t* grid = reinterpret_cast<uint32_t*>(smem_raw + (size_t)a.tstride * sizeof(float4));
+  uint32_t* grid = reinterpret_cast<uint32_t*>(smem_raw);
   float gx0 = 0.0f, gy0 = 0.0f, ginv = 0.0f;
   int gnx = 0, gny = 0;
   if (MEAS == M_LCSS && a.eps > 0.0f) {
@@ -852,7 +856,11 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
           hi_d.init((long long)j0 * (n - 1) + W, D);
         }
         const long long inc = 32ll * (n - 1);
-        const int dq = (int)(inc / D), dr = (int)(inc % D);
+        int dq = 0, dr = 0;
+        if (banded) divmod_floor(inc, D, dq, dr);
+        // no early exit: an infeasible pair's bound is +inf whatever the sum,
+        // and a loop without one keeps several point loads in flight
+#pragma unroll 4
         for (int j = j0; j < m - 1; j += 32) {
           int lo = 0, hi = n - 1;
           if (banded) {
@@ -861,9 +869,9 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
             lo_d.step(dq, dr);
             hi_d.step(dq, dr);
           }
-          if (lo > hi) {
+          if (lo > hi) {  // a column with no admissible row
             feasible = false;
-            break;
+            lo = hi = min(lo, n - 1);
           }
           const float4 bx = qtable_box(T, lo, hi);
           const float2 p = B[j];
@@ -1387,11 +1395,10 @@ __global__ void stats_kernel(KArgs a, unsigned long long* counters, int with_res
 // the round-striped kernel (G lanes x R rows) for the rest
 // latency: a round of few pairs (seeds, round 1, re-score), whose launch
 // lasts as long as its longest pair.  A step of a warp per pair costs R rows
-// of instructions on one warp; a CTA per pair spreads the rows over 8 warps
-// for a barrier per step, which pays off once a warp would need 8 or more
-// FP32 rows per lane, or 4 or more compensated (two-float) ones (measured: at
-// R = 2 the barrier made the compensated re-score of the batched DTW workload
-// 0.43 -> 0.58 ms).
+// of instructions on one warp; two warps or a CTA of 8 per pair spread the
+// rows for a barrier per step.  Two warps pay off as long as they need at
+// most 2 rows per lane; a CTA once a single warp would need 8 or more FP32
+// rows per lane, or 4 or more compensated (two-float) ones.
 int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& d,
            bool latency = false) {
   const bool diag_kind = kind == DP_DTW_SQ || kind == DP_DTW_EU || kind == DP_LCSS ||
@@ -1400,11 +1407,14 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
   if (!diag_kind || a.rdiag == 0) return launch_dp(ctx, kind, G, R, d, a.max_clen);
   const bool twofloat = kind == DP_DTW_SQC || kind == DP_DTW_EUC || kind == DP_FRECHET_SQC;
   // Latency rounds (few pairs, one wave) pick the kernel by the pair shape
-  // (not by the throughput-tuned R): compensated pairs take two warps per
-  // pair while 64 lanes need at most 2 rows each (lone 512-point pair: 188 us
-  // against 212 us on a warp and 196 us on a CTA; 640 pairs: 207, 234 and
-  // 432 us), longer shapes a CTA per pair.
-  const bool w2 = latency && twofloat && a.rdiag_w2 > 0 && a.rdiag_w2 <= 2;
+  // (not by the throughput-tuned R): two warps per pair while 64 lanes need
+  // at most 2 rows each, longer shapes a CTA per pair.  640 pairs of up to
+  // 512 x 512 points, band 10%: compensated 172 us on two warps against 247
+  // on one and 409 on a CTA; FP32 122, 146 and 270 us.  FP32 rounds of more
+  // pairs than SM sub-partitions (the batched workload's seeds and round 1,
+  // with abandoning) ran slower on two warps, so they keep one.
+  const bool w2 = latency && a.rdiag_w2 > 0 && a.rdiag_w2 <= 2 &&
+                  (twofloat || d.npairs <= 4 * ctx->num_sms);
   if (!w2 && latency && a.rdiag_cta > 0 && a.rdiag_shape >= (twofloat ? 4 : 8)) {
     TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag_cta, d, a.max_clen, a.spill, a.nspill, a.spill2,
                             a.nspill2, 8));
@@ -1611,8 +1621,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   // CTAs per query of the grid-stride filter kernels: about 8 per SM over the
   // whole request, so a single query against a large database fills the GPU
   const int ch = std::max(1, std::min(65535, (8 * ctx->num_sms + nq - 1) / nq));
-  size_t lb2_smem = (MEAS == M_DTW || MEAS == M_LCSS) ? qtable_bytes(max_qlen) : 0;
-  if (MEAS == M_LCSS) lb2_smem = (size_t)a.tstride * sizeof(float4) + sizeof(uint32_t) * kGridWords;
+  const size_t lb2_smem = MEAS == M_LCSS ? sizeof(uint32_t) * kGridWords : 0;
   if (lb2_smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(lb2_kernel<MEAS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)lb2_smem));

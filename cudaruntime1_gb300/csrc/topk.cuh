@@ -64,6 +64,20 @@ struct SelScratch {
 __device__ inline void block_select_k(const unsigned long long* keys, int N, int K,
                                       unsigned long long* out, SelScratch& S) {
   if (K <= 0) return;
+  if (K <= 4) {  // a few block minima cost less than the digit passes
+    unsigned long long prev = 0ull;
+    for (int k = 0; k < K; ++k) {
+      unsigned long long best = ~0ull;
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const unsigned long long x = keys[i];
+        if ((k == 0 || x > prev) && x < best) best = x;
+      }
+      prev = block_min_u64(best, S.cand);
+      if (threadIdx.x == 0) out[k] = prev;
+    }
+    __syncthreads();
+    return;
+  }
   if (threadIdx.x == 0) {
     S.pfx = 0;
     S.need = K;

@@ -153,7 +153,8 @@ inline void launched(tsim_ctx* ctx, int n = 1) { ctx->launches += n; }
 __host__ __device__ inline int band_w(int n, int m, int band_pct) {
   if (band_pct < 0) return -1;
   int L = n > m ? n : m;
-  return (int)(((long long)band_pct * L + 99) / 100);
+  const long long v = (long long)band_pct * L + 99;
+  return v <= 2147483647ll ? (int)v / 100 : (int)(v / 100);  // 32-bit when it fits
 }
 
 __host__ __device__ inline long long floordiv_ll(long long a, long long b) {
