@@ -409,9 +409,26 @@ int launch_chain(tsim_ctx* ctx, int R0, int warps, const DpArgs& a, int max_m, i
   // (fewer rows in flight, fewer masked cells); the last pass writes `spill`.
   // A warp per pair goes to R = 16 (full rows of up to 497 columns), two or
   // eight warps per pair to R = 4 (253 or 1021 columns).
+  // A pass takes every pair with both lengths >= 2 once the widest band
+  // (any band width is at most that of the longest lengths, and
+  // 2 (min(n,m) - 1) <= n + m - 2), the window or the longest full row fits
+  // its lanes: the chain stops there, and only degenerate pairs are left for
+  // the striped kernel.
   const int rmax = warps == 1 ? 16 : 4;
+  const int lanes = 32 * warps;
+  auto takes_all = [&](int R) {
+    if (a.max_n <= 0) return false;  // query lengths unknown
+    const long long span = (long long)(lanes - 1) * R;
+    const bool lcss = std::is_same<P, PolLcss>::value;
+    const int wd = lcss ? a.delta : band_w(a.max_n, max_m, a.band_pct);
+    if (wd < 0) return max_m <= span + 1;
+    return wd < span;
+  };
   std::vector<int> rs;
-  for (int R = std::max(1, std::min(R0, rmax)); R <= rmax; R *= 2) rs.push_back(R);
+  for (int R = std::max(1, std::min(R0, rmax)); R <= rmax; R *= 2) {
+    rs.push_back(R);
+    if (takes_all(R)) break;
+  }
   const int np = (int)rs.size();
   DpArgs in = a;
   for (int p = 0; p < np; ++p) {

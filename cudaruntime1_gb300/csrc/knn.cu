@@ -1451,6 +1451,7 @@ int finish_knn(tsim_ctx* ctx, KArgs& a, int dpc, int dp64) {
   const int nq = a.nq;
   DpArgs d{};
   d.band_pct = MEAS == M_DTW ? a.band_pct : -1;
+  d.max_n = a.max_qlen;
   stage_begin(ctx, TSIM_STAGE_SELECT);
   seg_select_kernel<MEAS, 1><<<dim3(a.nseg, nq), kSelThreads, 0, s>>>(a, a.k);
   final_select_kernel<MEAS><<<nq, kSelThreads, 0, s>>>(a);
@@ -1473,6 +1474,7 @@ int finish_knn(tsim_ctx* ctx, KArgs& a, int dpc, int dp64) {
     r.npairs = nq * a.RC;
     r.out64 = a.rdc;
     r.band_pct = d.band_pct;
+    r.max_n = a.max_qlen;
     r.delta = -1;
     // compensated FP32 re-score of the set, then FP64 only for the pairs it
     // cannot order (near-ties within the compensated error bound)
@@ -1538,6 +1540,7 @@ int run_brute(tsim_ctx* ctx, KArgs& a, int dp32, int dpc, int dp64) {
   d.cpts = a.cpts;
   d.coff = a.coff;
   d.band_pct = MEAS == M_DTW ? a.band_pct : -1;
+  d.max_n = a.max_qlen;
   d.delta = a.delta;
   d.eps = a.eps;
   d.cells = ctx->dcounters + 1;
@@ -1582,6 +1585,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   d.cpts = a.cpts;
   d.coff = a.coff;
   d.band_pct = MEAS == M_DTW ? a.band_pct : -1;
+  d.max_n = a.max_qlen;
   d.delta = a.delta;
   d.eps = a.eps;
   d.cells = ctx->dcounters;
@@ -2248,6 +2252,7 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   d.out = d_out32;
   d.out64 = d_out64;
   d.band_pct = p->measure == TSIM_DTW ? p->band_pct : -1;
+  d.max_n = max_qlen;
   d.delta = p->delta;
   d.eps = p->epsilon;
   const int wd = p->measure == TSIM_LCSS ? p->delta : band_w(max_qlen, max_clen, d.band_pct);

@@ -232,6 +232,7 @@ struct DpArgs {
   int buf_len;        // shared-memory values per segment (>= max candidate length)
   unsigned long long* cells;  // optional: band cells actually computed (atomic)
   const int* order;   // optional: work item w is pair order[w] (shape-sorted schedule)
+  int max_n;          // optional: no query of the pairs is longer (0: unknown)
 };
 
 enum DpKind {
