@@ -1424,7 +1424,12 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
     TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag_w2, d, a.max_clen, a.spill, a.nspill, a.spill2,
                             a.nspill2, 2));
   } else {
-    TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag, d, a.max_clen, a.spill, a.nspill, a.spill2,
+    // latency rounds start at the smallest R the longest pair admits; the
+    // survivor round at the tuned R (which may be smaller: its first pass
+    // then runs the narrow-band pairs with fewer rows per lane and passes the
+    // others on)
+    const int r0 = latency ? std::max(a.rdiag, a.rdiag_shape) : a.rdiag;
+    TSIM_TRY(launch_dp_diag(ctx, kind, r0, d, a.max_clen, a.spill, a.nspill, a.spill2,
                             a.nspill2));
   }
   DpArgs sp = d;

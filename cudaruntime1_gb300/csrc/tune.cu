@@ -2,7 +2,7 @@
 // measurement on this GPU, per request shape class.
 //
 // Two choices are tuned: the first rows per lane-group R of the anti-diagonal
-// DP's passes (1 .. 16; 0 runs every pair on the round-striped kernel) and the number
+// DP's survivor passes (1 .. 16; 0 runs every pair on the round-striped kernel) and the number
 // of query chunks a request runs concurrently on child streams (1, 2, 4, 8).
 // tsim_autotune times every admissible pair of choices on the caller's own
 // request (device pointers, CUDA events on the context stream, the median of
@@ -65,9 +65,11 @@ extern "C" int tsim_autotune(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
   std::vector<int> rs{0};
   const bool dp = p->measure == TSIM_DTW || p->measure == TSIM_LCSS || p->measure == TSIM_FRECHET;
   if (dp) {
+    // from half the longest pair's R (narrow-band pairs at fewer rows per
+    // lane in a first pass, the rest in the next) to four times it
     const int r0 = min_rdiag(p, max_qlen, db);
     for (int R : {1, 2, 4, 8, 16})
-      if (R >= r0 && R <= 4 * r0) rs.push_back(R);
+      if (2 * R >= r0 && R <= 4 * r0) rs.push_back(R);
   }
   std::vector<int> ss;
   for (int s : {1, 2, 4, 8})
