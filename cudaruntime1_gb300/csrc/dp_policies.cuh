@@ -15,6 +15,18 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
   return r;
 }
 
+// Minimum of three normalised pairs.  A normalised pair's hi is its value
+// rounded to nearest, so pairs with different hi order as their hi parts;
+// among the operands whose hi is the smallest, the smallest lo decides.
+// Equal to two lexicographic minima, in fewer instructions.
+__device__ __forceinline__ df df_min3(df a, df b, df c) {
+  const float h = min3f(a.hi, b.hi, c.hi);
+  const float la = a.hi == h ? a.lo : TSIM_INF;
+  const float lb = b.hi == h ? b.lo : TSIM_INF;
+  const float lc = c.hi == h ? c.lo : TSIM_INF;
+  return df{h, min3f(la, lb, lc)};
+}
+
 // ---- cell policies ---------------------------------------------------------
 // V: value type; border(): value outside the matrix / band; origin(): D(-1,-1);
 // masked(left): value of a cell outside its row's band.
@@ -138,7 +150,7 @@ struct PolDtwSqC {
   __device__ static V origin() { return df{0.0f, 0.0f}; }
   __device__ static V masked(V) { return df_inf(); }
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    const df m = df_min(df_min(up, lf), dg);
+    const df m = df_min3(up, lf, dg);
     if (!(m.hi < TSIM_INF)) return df_inf();
     const float dx = qx - cx, dy = qy - cy;
     return df_add1(fmaf(dy, dy, dx * dx), m);
@@ -152,7 +164,7 @@ struct PolDtwEuC {
   __device__ static V origin() { return df{0.0f, 0.0f}; }
   __device__ static V masked(V) { return df_inf(); }
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    const df m = df_min(df_min(up, lf), dg);
+    const df m = df_min3(up, lf, dg);
     if (!(m.hi < TSIM_INF)) return df_inf();
     const float dx = qx - cx, dy = qy - cy;
     return df_add1(sqrtf(fmaf(dy, dy, dx * dx)), m);
@@ -166,7 +178,7 @@ struct PolFrechetSqC {
   __device__ static V origin() { return df{0.0f, 0.0f}; }
   __device__ static V masked(V) { return df_inf(); }
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
-    return df_max(df_sqdist(qx, qy, cx, cy), df_min(df_min(up, lf), dg));
+    return df_max(df_sqdist(qx, qy, cx, cy), df_min3(up, lf, dg));
   }
 };
 
