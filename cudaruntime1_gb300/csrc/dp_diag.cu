@@ -136,7 +136,24 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
   const int npairs = a.npairs_dev ? min(*a.npairs_dev, a.npairs) : a.npairs;
   float2* cs = diag_cand + (W == 1 ? (size_t)warp * col_cap : 0);  // this pair's candidate
 
-  for (int wk = slot; wk < npairs; wk += nslots) {
+  // Work items.  A warp per pair strides over the pairs (sorted longest
+  // first).  Two warps or a CTA per pair (latency rounds, whose lists hold
+  // padding entries: a query's re-score slots beyond its set) take their
+  // first pair by slot, then the next unclaimed one from the launch's counter
+  // (nspill[1], zeroed with the spill count): a static stride could hand one
+  // CTA two real pairs and double the round's latency (re-score stage 0.25
+  // -> 0.19 ms).  For a warp per pair the claim's round trip cost more than
+  // the shorter tail saved.
+  __shared__ int next_item;
+  auto fetch = [&](int wk) -> int {
+    if (W == 1 || nspill == nullptr) return wk + nslots;
+    if (threadIdx.x == 0) next_item = nslots + atomicAdd(nspill + 1, 1);
+    __syncthreads();
+    const int v = next_item;
+    __syncthreads();
+    return v;
+  };
+  for (int wk = slot; wk < npairs; wk = fetch(wk)) {
     const int pid = a.order ? a.order[wk] : wk;
     const int2 pr = a.pairs[pid];
     if (pr.y < 0) continue;
@@ -435,7 +452,7 @@ int launch_chain(tsim_ctx* ctx, int R0, int warps, const DpArgs& a, int max_m, i
     const bool to_spill = ((np - 1 - p) & 1) == 0;
     int* out = to_spill ? spill : tmp;
     int* nout = to_spill ? nspill : ntmp;
-    TSIM_CUDA(cudaMemsetAsync(nout, 0, sizeof(int), ctx->stream));
+    TSIM_CUDA(cudaMemsetAsync(nout, 0, 2 * sizeof(int), ctx->stream));  // spills, work counter
     if (warps == 1)
       TSIM_TRY((launch_diag_r<P, 1>(ctx, rs[p], in, max_m, out, nout)));
     else if (warps == 2)

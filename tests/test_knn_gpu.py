@@ -263,3 +263,33 @@ def test_knn_mixed_query_lengths_one_call(tsim, cuda_ctx, oracle, measure, kw):
                                flags=tsim.api.FLAG_ALWAYS_PRUNE, **kw)
     assert np.array_equal(ids, want_ids)
     db.close()
+
+
+@pytest.mark.parametrize("pruned", [False, True])
+def test_knn_k64_with_many_ties(tsim, cuda_ctx, oracle, pruned):
+    """k at its maximum (64) over a database in which every trajectory occurs
+    eight times: the block selections (radix passes over the packed keys,
+    ties broken by candidate index) against the oracle."""
+    base, bo = _db(60, 12, 70, 900)
+    reps = 8
+    parts, offs = [], [0]
+    for r in range(reps):
+        for t in range(60):
+            seg = base[bo[t]:bo[t + 1]]
+            parts.append(seg)
+            offs.append(offs[-1] + len(seg))
+    cp = np.concatenate(parts)
+    co = np.array(offs, np.int64)
+    ql = G.uniform_lengths(6, 12, 70, 901)
+    qp, qo = G.random_walks(6, ql, 902)
+    db = tsim.Database(cuda_ctx, cp, co)
+    k = 64
+    for measure, kw, okw in [("dtw", dict(band_pct=20), dict(band_pct=20)),
+                             ("lcss", dict(epsilon=1.5, delta=-1), dict(eps=1.5, delta=-1)),
+                             ("hausdorff", {}, {})]:
+        want_ids, want_d = oracle.knn(measure, qp, qo, cp, co, k, **okw)
+        if pruned:
+            kw = dict(kw, flags=tsim.api.FLAG_ALWAYS_PRUNE)
+        ids, d, _, _ = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, k, **kw)
+        assert np.array_equal(ids, want_ids), (measure, pruned)
+    db.close()
