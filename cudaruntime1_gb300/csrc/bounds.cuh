@@ -80,4 +80,36 @@ struct FloorDiv {
   }
 };
 
+// Sparse table of a query for O(1) range boxes: level l holds, for block b,
+// the box of blocks [b, b + 2^l).  Block = f consecutive rows (f = 1 for
+// queries up to kMaxTable rows, a power of two beyond, which widens boxes and
+// keeps the bound valid).
+constexpr int kMaxTable = 512;  // sparse-table columns (query rows, downsampled beyond)
+struct QTable {
+  const float4* t;  // [levels][nb] as (x0, y0, x1, y1)
+  int nb, f_log, levels;
+};
+
+// box of query rows [lo, hi] (non-empty)
+__device__ __forceinline__ float4 qtable_box(const QTable& T, int lo, int hi) {
+  const int b0 = lo >> T.f_log, b1 = hi >> T.f_log;
+  const int l = 31 - __clz(b1 - b0 + 1);
+  const float4 u = T.t[(size_t)l * T.nb + b0], v = T.t[(size_t)l * T.nb + b1 - (1 << l) + 1];
+  return make_float4(fminf(u.x, v.x), fminf(u.y, v.y), fmaxf(u.z, v.z), fmaxf(u.w, v.w));
+}
+
+// view of a table built for a query of n rows
+__device__ __forceinline__ QTable qtable_view(const float4* t, int n) {
+  QTable T;
+  int f_log = 0;
+  while ((n + (1 << f_log) - 1) >> f_log > kMaxTable) ++f_log;
+  T.t = t;
+  T.f_log = f_log;
+  T.nb = (n + (1 << f_log) - 1) >> f_log;
+  int levels = 1;
+  while ((1 << levels) <= T.nb) ++levels;
+  T.levels = levels;
+  return T;
+}
+
 }  // namespace tsim

@@ -29,6 +29,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "bounds.cuh"
 #include "dp_policies.cuh"
 
 namespace tsim {
@@ -101,6 +102,21 @@ __device__ __forceinline__ Ramps make_ramps(int n, int m, int wd, bool lcss) {
   }
   rp.K = (int)(rp.Wl / rp.d) + 1;
   return rp;
+}
+
+// DTW on a warp per pair, abandoning against thresholds with the queries'
+// sparse tables at hand: each pair's columns get a lower bound (the distance
+// from the candidate point to the box of the query rows its band admits),
+// whose suffix sums are kept in shared memory next to the staged candidate.
+template <class P, int W>
+__host__ __device__ bool diag_suffix(const DpArgs& a) {
+  return W == 1 && (std::is_same<P, PolDtwSq>::value || std::is_same<P, PolDtwEu>::value) &&
+         a.qtab != nullptr && a.thr != nullptr && a.max_n > 0;
+}
+
+// abandon checks (every 16 steps) of a pair of up to max_n x col_cap points
+__host__ __device__ inline int diag_checks(int max_n, int col_cap) {
+  return (max_n + col_cap) / 16 + 2;
 }
 
 // resident CTAs per SM asked of the register allocator: 8 (32 warps) where
@@ -191,6 +207,70 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
     // candidate point of column j; columns outside 0 .. m-1 (cells outside
     // the band, whose values are masked) read point m-1
     auto cand = [&](int j) -> float2 { return C[min((unsigned)j, (unsigned)(m - 1))]; };
+
+    // Remaining-columns bound (DTW, warp per pair): every path crosses every
+    // column after the one where it crosses anti-diagonals t-1, t, and a cell
+    // of column j costs at least the distance from candidate point j to the
+    // box of the query rows j's band admits.  sfx[j] = sum of those bounds
+    // over columns j .. m-1 (rounded down; sfx[m] = 0), built once per pair;
+    // chk[c] = the part of it the abandon check at step 16c + 15 adds (the
+    // columns after the last one of anti-diagonals 16c + 14 and 16c + 15).
+    // The FP32 path sum that adds those columns' costs can round below their
+    // exact sum by at most (n+m+8) 2^-24 relative, so the check compares with
+    // the threshold divided by 1 minus that.
+    const int sfx_cap = col_cap + 1, chk_cap = diag_checks(a.max_n, col_cap);
+    float* sfx = reinterpret_cast<float*>(diag_cand + (size_t)(blockDim.x >> 5) * col_cap) +
+                 (size_t)warp * (sfx_cap + chk_cap);
+    float* chk = sfx + sfx_cap;
+    const int t_last = n + m - 2;
+    const bool suffix = diag_suffix<P, W>(a) && staged && n <= a.max_n &&
+                        (t_last >> 4) < chk_cap;
+    float thr_chk = thr;  // threshold of the abandon check
+    if (suffix) {
+      const long long wband = w >= 0 ? (long long)w * (min(n, m) - 1) : -1;
+      const QTable T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
+      float carry = 0.0f;  // bound of the columns after the current block
+      for (int b0 = ((m - 1) >> 5) << 5; b0 >= 0; b0 -= 32) {  // blocks of 32 columns, last first
+        const int j = b0 + lane;
+        float v = 0.0f;
+        if (j < m) {
+          int lo = 0, hi = n - 1;
+          if (wband >= 0) {
+            lo = max(0, floordiv_i((long long)j * (n - 1) - wband + (m - 2), m - 1));  // ceil
+            hi = min(n - 1, floordiv_i((long long)j * (n - 1) + wband, m - 1));
+          }
+          if (lo <= hi) {
+            const float4 bx = qtable_box(T, lo, hi);
+            const float2 c = cs[j];
+            v = box_pt_d2_rd(bx.x, bx.y, bx.z, bx.w, c.x, c.y);
+            if (std::is_same<P, PolDtwEu>::value) v = __fsqrt_rd(v);
+          } else {
+            v = TSIM_INF;  // a column with no admissible row: no path
+          }
+        }
+        // suffix sums inside the block (lane l: columns j .. b0 + 31), then
+        // the columns after it
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const float u = __shfl_down_sync(0xffffffffu, v, o);
+          if (lane + o < 32) v = __fadd_rd(v, u);
+        }
+        v = __fadd_rd(v, carry);
+        if (j < m) sfx[j] = v;
+        carry = __shfl_sync(0xffffffffu, v, 0);
+      }
+      if (lane == 0) sfx[m] = 0.0f;
+      __syncwarp();
+      for (int c = lane; c <= (t_last >> 4); c += 32) {
+        const int t = 16 * c + 15;  // the largest column of anti-diagonals t-1, t
+        int jmax = min(t, m - 1);
+        if (wband >= 0) jmax = min(jmax, floordiv_i((long long)t * (m - 1) + wband, n + m - 2));
+        chk[c] = sfx[jmax + 1];
+      }
+      __syncwarp();
+      const float shrink = __fsub_rd(1.0f, __fmul_ru((float)(n + m + 8), 6.03e-8f));
+      thr_chk = __fdiv_ru(thr, shrink);
+    }
 
     const Ramps rp = make_ramps(n, m, wd, kLcss);
     const int row_q = (int)(rp.a / rp.d), row_r = (int)(rp.a % rp.d);
@@ -335,6 +415,7 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
         if ((t & 15) == 15) {
           const float two = fminf(mstep, prev);
           float lb = __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(two)));
+          if (suffix) lb = __fadd_rd(lb, chk[t >> 4]);  // plus the remaining columns
           if (W > 1) {  // over the pair's warps (reads after this step's barrier)
             if (lane == 0) xred[warp] = lb;
             if (lane == 31) xbuf[t & 1][warp] = out;
@@ -342,7 +423,7 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
 #pragma unroll
             for (int w2 = 0; w2 < W; ++w2) lb = fminf(lb, xred[w2]);
           }
-          if (lb > thr) {  // uniform across the pair
+          if (lb > thr_chk) {  // uniform across the pair
             alive = false;
             t_ab = t;
             break;
@@ -388,7 +469,9 @@ int launch_diag_one(tsim_ctx* ctx, const DpArgs& a, int max_m, int* spill, int* 
   const int threads = W == 1 ? kDiagThreads : 32 * W;
   const int pairs_per_cta = W == 1 ? kDiagThreads / 32 : 1;
   const int col_cap = (std::min(max_m, W == 1 ? kMaxStagedCols : kMaxStagedColsCta) + 1) & ~1;
-  const size_t smem = (size_t)pairs_per_cta * col_cap * sizeof(float2);
+  size_t smem = (size_t)pairs_per_cta * col_cap * sizeof(float2);
+  if (diag_suffix<P, W>(a))
+    smem += (size_t)pairs_per_cta * (col_cap + 1 + diag_checks(a.max_n, col_cap)) * sizeof(float);
   auto kern = dp_diag_kernel<P, R, W>;
   if (smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -44,9 +44,8 @@ constexpr int kChunk = 256;     // candidates per stage-A CTA
 constexpr int kSelThreads = 256;
 constexpr int kSeg = 2048;       // list entries per CTA of the two-level selections
 constexpr int kLb2Warps = 8;
-constexpr int kGridWords = 4096;
-constexpr int kQBlocks = 8;       // row blocks of a query in the O(1) bound  // LCSS occupancy grid of a query: 131,072 cells (16 KiB)
-constexpr int kMaxTable = 512;  // sparse-table columns (query rows, downsampled beyond)
+constexpr int kGridWords = 4096;  // LCSS occupancy grid of a query: 131,072 cells (16 KiB)
+constexpr int kQBlocks = 8;       // row blocks of a query in the O(1) bound
 
 enum Meas { M_DTW = 0, M_LCSS = 1, M_FRECHET = 2, M_HAUSDORFF = 3, M_EUCLID = 4 };
 
@@ -405,15 +404,8 @@ __global__ void thresh_kernel(KArgs a) {
 // ---------------------------------------------------------------------------
 // stage C: compaction and O(length) bounds
 // ---------------------------------------------------------------------------
-// Sparse table of the query for O(1) range boxes: level l holds, for block b,
-// the box of blocks [b, b + 2^l).  Block = f consecutive rows (f = 1 for
-// queries up to kMaxTable rows, a power of two beyond, which widens boxes and
-// keeps the bound valid).
-struct QTable {
-  float4* t;  // [levels][nb] as (x0, y0, x1, y1)
-  int nb, f_log, levels;
-};
-
+// The query's sparse table (QTable, bounds.cuh), built in shared or global
+// memory by one CTA.
 __device__ __forceinline__ void qtable_build(QTable& T, const float2* A, int n, float4* smem) {
   int f_log = 0;
   while ((n + (1 << f_log) - 1) >> f_log > kMaxTable) ++f_log;
@@ -448,14 +440,6 @@ __device__ __forceinline__ void qtable_build(QTable& T, const float2* A, int n, 
   }
 }
 
-// box of query rows [lo, hi] (non-empty)
-__device__ __forceinline__ float4 qtable_box(const QTable& T, int lo, int hi) {
-  const int b0 = lo >> T.f_log, b1 = hi >> T.f_log;
-  const int l = 31 - __clz(b1 - b0 + 1);
-  const float4 u = T.t[(size_t)l * T.nb + b0], v = T.t[(size_t)l * T.nb + b1 - (1 << l) + 1];
-  return make_float4(fminf(u.x, v.x), fminf(u.y, v.y), fmaxf(u.z, v.z), fmaxf(u.w, v.w));
-}
-
 // Bytes of the largest table of any query of up to max_n rows.  The size is
 // not monotone in n (a 512-row query keeps 512 blocks, a 600-row one 300
 // blocks of 2 rows), so a buffer shared by queries of different lengths is
@@ -466,20 +450,6 @@ size_t qtable_bytes(int max_n) {
   int levels = 1;
   while ((1 << levels) <= nb) ++levels;
   return (size_t)levels * nb * sizeof(float4);
-}
-
-// view of a query table built by qtable_build for a query of n rows
-__device__ __forceinline__ QTable qtable_view(float4* t, int n) {
-  QTable T;
-  int f_log = 0;
-  while ((n + (1 << f_log) - 1) >> f_log > kMaxTable) ++f_log;
-  T.t = t;
-  T.f_log = f_log;
-  T.nb = (n + (1 << f_log) - 1) >> f_log;
-  int levels = 1;
-  while ((1 << levels) <= T.nb) ++levels;
-  T.levels = levels;
-  return T;
 }
 
 // one CTA per query: its sparse table and its FP64 prefix sums in global
@@ -1627,6 +1597,10 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
                            256, 0, s>>>(a);
   launched(ctx);
   launched(ctx, 2);
+  if (MEAS == M_DTW) {  // the survivor round abandons with the remaining columns' bound
+    d.qtab = a.qtab;
+    d.tstride = a.tstride;
+  }
   // CTAs per query of the grid-stride filter kernels: about 8 per SM over the
   // whole request, so a single query against a large database fills the GPU
   const int ch = std::max(1, std::min(65535, (8 * ctx->num_sms + nq - 1) / nq));
@@ -1649,6 +1623,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
     r1.npairs = nq * a.M;
     r1.out = a.r1vals;
     r1.thr = a.thr;
+    r1.qtab = nullptr;  // the best pairs by bound rarely abandon: no remaining-columns bound
     if (a.plain) {
       for (int i = 0; i < nq * a.M; ++i) {
         DpArgs one = r1;

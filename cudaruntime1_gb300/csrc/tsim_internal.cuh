@@ -233,6 +233,8 @@ struct DpArgs {
   unsigned long long* cells;  // optional: band cells actually computed (atomic)
   const int* order;   // optional: work item w is pair order[w] (shape-sorted schedule)
   int max_n;          // optional: no query of the pairs is longer (0: unknown)
+  const float4* qtab; // optional: queries' sparse tables (tstride float4 each, queries of
+  int tstride;        //   up to max_n rows): DTW abandoning adds the remaining columns' bound
 };
 
 enum DpKind {
