@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
     const float2* A = a.qpts;
     const float2* B = a.cpts;
     float thr = TSIM_INF;
+    float aux = a.eps;  // the cell policy's parameter: eps, or the pair's aux value
     if (has) {
       int2 pr = a.pairs[pid];
       q = pr.x;
@@ -64,6 +65,7 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
       A += qo;
       B += co;
       if (a.thr) thr = a.thr[q];
+      if (a.aux) aux = (float)a.aux[pid];
     }
     const int w = band_w(n, m, a.band_pct);
     const int rrow = result_row<P>(n, m, a.delta);
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
 #pragma unroll
           for (int k = 0; k < R; ++k) {
             const V lf = left[k];
-            V v = P::cell(qx[k], qy[k], cp.x, cp.y, u, lf, dg, a.eps);
+            V v = P::cell(qx[k], qy[k], cp.x, cp.y, u, lf, dg, aux);
             const bool in = (unsigned)(j - jlo[k]) <= (unsigned)(jhi[k] - jlo[k]);
             v = in ? v : P::masked(lf);
             dg = lf;
@@ -254,6 +256,7 @@ int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a_in, int max
     case DP_DTW_SQC: return launch_g64<PolDtwSqC>(ctx, G, R, a);
     case DP_DTW_EUC: return launch_g64<PolDtwEuC>(ctx, G, R, a);
     case DP_FRECHET_SQC: return launch_g64<PolFrechetSqC>(ctx, G, R, a);
+    case DP_FRECHET_WIN: return launch_g64<PolFrechetWin>(ctx, G, R, a);
   }
   return fail(TSIM_ERR_INVALID_ARG, "unknown dp kind");
 }

@@ -139,6 +139,44 @@ struct PolFrechetSq64 {
   }
 };
 
+// Exact FP64 discrete Frechet (squared) without an FP64 DP.  A Frechet
+// value is a min over paths of a max over cells, so it equals one cell's
+// cost.  With FP32 costs d32 (the FP32 DP's arithmetic) and FP64 costs d64
+// (the FP64 oracle's), |d32 - d64| <= 8u d64 for normal numbers (u = 2^-24),
+// so the FP64 optimum v64 lies within 16u of the pair's FP32 optimum v32
+// (passed as the pair's aux value).  A cell whose d32 is at most v32 (1 - 32u)
+// has d64 below v64: taking its cost as 0 cannot change any path's maximum
+// that could be the optimum; one whose d32 is at least v32 (1 + 32u) has d64
+// above v64 and cannot lie on an optimal path, so it is blocked.  Only the
+// cells between get their FP64 cost, computed as the oracle does.  Values are
+// the bit patterns of non-negative doubles, whose unsigned order is the
+// doubles' order: min and max run on the integer ALU, not the FP64 units.
+// Below v32 = 1e-20 (FP32 underflow voids the relative bound) every cell
+// gets its FP64 cost.
+struct PolFrechetWin {
+  using V = unsigned long long;
+  static constexpr bool kMin = true;
+  __device__ static V border() { return 0x7ff0000000000000ull; }  // +inf
+  __device__ static V origin() { return 0ull; }                   // +0
+  __device__ static V masked(V) { return border(); }
+  __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float v32) {
+    const V mn = umin(umin(up, lf), dg);
+    const float dx = qx - cx, dy = qy - cy;
+    const float d = fmaf(dy, dy, dx * dx);
+    const bool exact = !(v32 >= 1e-20f);
+    V c;
+    if (!exact && d <= __fmul_rd(v32, 1.0f - 32.0f / 16777216.0f)) {
+      c = 0ull;  // below any candidate optimum
+    } else if (!exact && d >= __fmul_ru(v32, 1.0f + 32.0f / 16777216.0f)) {
+      c = border();  // above it
+    } else {
+      c = (V)__double_as_longlong(d2_64(qx, qy, cx, cy));
+    }
+    return c > mn ? c : mn;
+  }
+  __device__ static V umin(V a, V b) { return b < a ? b : a; }
+};
+
 // Compensated FP32 re-score policies: values are (hi, lo) pairs (dfloat.cuh).
 // DTW: each cell cost in FP32 (<= 4u relative error, one FMA), the path sum
 // compensated; the value is then within 4u + O(P u^2) of exact -- a single
@@ -227,6 +265,9 @@ struct RowBand<PolLcss> {
 __device__ __forceinline__ void store_result(const DpArgs& a, int pid, float v) { a.out[pid] = v; }
 __device__ __forceinline__ void store_result(const DpArgs& a, int pid, int v) { a.out[pid] = (float)v; }
 __device__ __forceinline__ void store_result(const DpArgs& a, int pid, double v) { a.out64[pid] = v; }
+__device__ __forceinline__ void store_result(const DpArgs& a, int pid, unsigned long long v) {
+  a.out64[pid] = __longlong_as_double((long long)v);  // the bits of a double
+}
 __device__ __forceinline__ void store_result(const DpArgs& a, int pid, df v) {
   a.out64[pid] = v.hi < TSIM_INF ? df_to_double(v) : __longlong_as_double(0x7ff0000000000000ll);
 }
@@ -234,6 +275,9 @@ __device__ __forceinline__ float vf(float v) { return v; }
 __device__ __forceinline__ float vf(int v) { return (float)v; }
 __device__ __forceinline__ float vf(double v) { return (float)v; }
 __device__ __forceinline__ float vf(df v) { return v.hi; }
+__device__ __forceinline__ float vf(unsigned long long v) {
+  return (float)__longlong_as_double((long long)v);
+}
 
 template <class V>
 __device__ __forceinline__ V shfl_up_seg(V v, int G) {

@@ -1457,7 +1457,10 @@ int finish_knn(tsim_ctx* ctx, KArgs& a, int dpc, int dp64) {
     cluster_kernel<MEAS><<<(nq + kRankWarps - 1) / kRankWarps, 32 * kRankWarps, 0, s>>>(a);
     r.pairs = a.r64pairs;
     r.out64 = a.r64;
-    if (is_dp(MEAS)) {
+    if (MEAS == M_FRECHET) {  // exact FP64 values from the FP32 ones: no FP64 DP
+      r.aux = a.rdc;
+      TSIM_TRY(launch_dp(ctx, DP_FRECHET_WIN, 32, 1, r, a.max_clen));
+    } else if (is_dp(MEAS)) {
       TSIM_TRY(launch_dp(ctx, dp64, 32, 1, r, a.max_clen));
     } else {
       PwArgs p{a.qpts, a.qoff, a.cpts, a.coff, a.r64pairs, nq * a.RC, nullptr, nullptr, nullptr,

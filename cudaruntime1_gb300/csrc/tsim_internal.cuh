@@ -233,6 +233,7 @@ struct DpArgs {
   unsigned long long* cells;  // optional: band cells actually computed (atomic)
   const int* order;   // optional: work item w is pair order[w] (shape-sorted schedule)
   int max_n;          // optional: no query of the pairs is longer (0: unknown)
+  const double* aux;  // optional: a value per pair, passed to the cell policy (else eps)
   const float4* qtab; // optional: queries' sparse tables (tstride float4 each, queries of
   int tstride;        //   up to max_n rows): DTW abandoning adds the remaining columns' bound
 };
@@ -250,6 +251,8 @@ enum DpKind {
   DP_DTW_SQC,       // compensated FP32 (hi, lo) re-score kinds
   DP_DTW_EUC,
   DP_FRECHET_SQC,
+  DP_FRECHET_WIN,   // exact FP64 Frechet from the pair's FP32 value (aux): FP64 costs
+                    // only inside the window that can hold the FP64 optimum
   DP_NUM_KINDS
 };
 

@@ -66,10 +66,16 @@ extern "C" int tsim_autotune(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
   const bool dp = p->measure == TSIM_DTW || p->measure == TSIM_LCSS || p->measure == TSIM_FRECHET;
   if (dp) {
     // from half the longest pair's R (narrow-band pairs at fewer rows per
-    // lane in a first pass, the rest in the next) to four times it
+    // lane in a first pass, the rest in the next) to four times it; with
+    // full rows (no band, no window) every R from 1: a pair needs as many
+    // rows per lane-group as its candidate is long, so a chain from R = 1
+    // runs each pair at the fewest its length admits
     const int r0 = min_rdiag(p, max_qlen, db);
+    const bool full_rows = p->measure == TSIM_FRECHET ||
+                           (p->measure == TSIM_DTW && p->band_pct < 0) ||
+                           (p->measure == TSIM_LCSS && p->delta < 0);
     for (int R : {1, 2, 4, 8, 16})
-      if (2 * R >= r0 && R <= 4 * r0) rs.push_back(R);
+      if (full_rows || (2 * R >= r0 && R <= 4 * r0)) rs.push_back(R);
   }
   std::vector<int> ss;
   for (int s : {1, 2, 4, 8})
