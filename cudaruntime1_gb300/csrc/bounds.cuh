@@ -98,6 +98,17 @@ __device__ __forceinline__ float4 qtable_box(const QTable& T, int lo, int hi) {
   return make_float4(fminf(u.x, v.x), fminf(u.y, v.y), fmaxf(u.z, v.z), fmaxf(u.w, v.w));
 }
 
+// float4 entries of a table buffer for queries of up to max_n rows: the
+// table size is not monotone in n (a 512-row query keeps 512 blocks, a
+// 600-row one 300 blocks of 2 rows), so the buffer is sized for
+// min(max_n, kMaxTable) blocks, whose level count no shorter query exceeds
+__host__ __device__ inline int qtable_stride(int max_n) {
+  const int nb = max_n < 1 ? 1 : (max_n < kMaxTable ? max_n : kMaxTable);
+  int levels = 1;
+  while ((1 << levels) <= nb) ++levels;
+  return levels * nb;
+}
+
 // view of a table built for a query of n rows
 __device__ __forceinline__ QTable qtable_view(const float4* t, int n) {
   QTable T;

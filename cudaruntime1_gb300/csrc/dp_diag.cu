@@ -119,15 +119,17 @@ __host__ __device__ inline int diag_checks(int max_n, int col_cap) {
   return (max_n + col_cap) / 16 + 2;
 }
 
-// resident CTAs per SM asked of the register allocator: 8 (32 warps) where
-// the FP32 policies fit 64 registers without spilling, fewer for the
-// compensated (two-float) values and for R = 4
+// resident CTAs per SM asked of the register allocator.  FP32 R <= 2: 7
+// (28 warps, 72 registers): at 8 CTAs (64 registers) the allocator spilled
+// 44 to 60 bytes in the step loop depending on the argument struct's layout,
+// and the survivor launch's tail leaves about 30 % of the warps active
+// anyway.  Fewer for the compensated (two-float) values and for R = 4.
 template <class P, int R>
 constexpr int diag_min_blocks() {
   return R >= 8                             ? 1  // long unbanded rows: latency, not occupancy
          : sizeof(typename P::V) > 4        ? (R == 1 ? 8 : (R == 2 ? 6 : 4))
          : std::is_same<P, PolDtwEu>::value ? (R == 1 ? 8 : (R == 2 ? 6 : 4))
-                                            : (R <= 2 ? 8 : 5);
+                                            : (R <= 2 ? 7 : 5);
 }
 
 // W warps per pair: 1 (a warp per pair, kDiagThreads per CTA) or kCtaWarps
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
     float thr_chk = thr;  // threshold of the abandon check
     if (suffix) {
       const long long wband = w >= 0 ? (long long)w * (min(n, m) - 1) : -1;
-      const QTable T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
+      const QTable T = qtable_view(a.qtab + (size_t)q * qtable_stride(a.max_n), n);
       float carry = 0.0f;  // bound of the columns after the current block
       for (int b0 = ((m - 1) >> 5) << 5; b0 >= 0; b0 -= 32) {  // blocks of 32 columns, last first
         const int j = b0 + lane;

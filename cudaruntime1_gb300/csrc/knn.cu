@@ -440,17 +440,8 @@ __device__ __forceinline__ void qtable_build(QTable& T, const float2* A, int n, 
   }
 }
 
-// Bytes of the largest table of any query of up to max_n rows.  The size is
-// not monotone in n (a 512-row query keeps 512 blocks, a 600-row one 300
-// blocks of 2 rows), so a buffer shared by queries of different lengths is
-// sized for the worst case: min(max_n, kMaxTable) blocks, whose level count
-// no shorter query exceeds.
-size_t qtable_bytes(int max_n) {
-  const int nb = std::max(1, std::min(max_n, kMaxTable));
-  int levels = 1;
-  while ((1 << levels) <= nb) ++levels;
-  return (size_t)levels * nb * sizeof(float4);
-}
+// Bytes of the table buffer of a query of up to max_n rows.
+size_t qtable_bytes(int max_n) { return (size_t)qtable_stride(max_n) * sizeof(float4); }
 
 // one CTA per query: its sparse table and its FP64 prefix sums in global
 // memory (read by the segment bounds of every pair of the query)
@@ -1600,10 +1591,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
                            256, 0, s>>>(a);
   launched(ctx);
   launched(ctx, 2);
-  if (MEAS == M_DTW) {  // the survivor round abandons with the remaining columns' bound
-    d.qtab = a.qtab;
-    d.tstride = a.tstride;
-  }
+  if (MEAS == M_DTW) d.qtab = a.qtab;  // the survivor round: remaining columns' bound
   // CTAs per query of the grid-stride filter kernels: about 8 per SM over the
   // whole request, so a single query against a large database fills the GPU
   const int ch = std::max(1, std::min(65535, (8 * ctx->num_sms + nq - 1) / nq));
@@ -1750,7 +1738,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
   a.C = C;
   a.max_clen = db->max_len;
   a.max_qlen = max_qlen;
-  a.tstride = (int)(qtable_bytes(max_qlen) / sizeof(float4));
+  a.tstride = qtable_stride(max_qlen);
   a.k = k;
   a.S = std::min(C, std::min(64, std::max(2 * k, 16)));
   a.M = std::min(64, std::max(2 * k, 32));
@@ -2232,8 +2220,10 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   d.coff = d_coff;
   d.pairs = reinterpret_cast<const int2*>(d_pairs);
   d.npairs = npairs;
-  d.out = d_out32;
-  d.out64 = d_out64;
+  if (precision == 0)  // one output slot: FP32, or FP64 / compensated
+    d.out = d_out32;
+  else
+    d.out64 = d_out64;
   d.band_pct = p->measure == TSIM_DTW ? p->band_pct : -1;
   d.max_n = max_qlen;
   d.delta = p->delta;

@@ -215,28 +215,36 @@ __host__ __device__ inline float ord2f(unsigned u) {
 // ---------------------------------------------------------------------------
 // launch helpers implemented in the .cu files
 // ---------------------------------------------------------------------------
+// Arguments of the DP kernels, passed by value: kept at 120 bytes.  A
+// version at 136 bytes (two more fields) made the serving workload, which
+// issues tens of thousands of small DP launches per second, 20 % slower (p50
+// 20 -> 24 ms, same build otherwise); hence the shared output slot and the
+// table stride derived from max_n.
 struct DpArgs {
   const float2* qpts;
   const int64_t* qoff;
   const float2* cpts;
   const int64_t* coff;
   const int2* pairs;  // (query, candidate)
-  int npairs;
-  float* out;         // per pair: distance (FP32 domain) or LCSS count
-  double* out64;      // per pair, FP64 kinds
+  union {             // per pair; a launch writes one of the two:
+    float* out;       //   distance (FP32 domain) or LCSS count (FP32 kinds)
+    double* out64;    //   FP64 and compensated kinds
+  };
   const int* npairs_dev;  // when set, the pair count is min(*npairs_dev, npairs)
   const float* thr;   // per query abandon threshold, or null
+  unsigned long long* cells;  // optional: band cells actually computed (atomic)
+  const int* order;   // optional: work item w is pair order[w] (shape-sorted schedule)
+  const double* aux;  // optional: a value per pair, passed to the cell policy (else eps)
+  const float4* qtab; // optional: queries' sparse tables (qtable_stride(max_n) float4 each):
+                      //   DTW abandoning adds the remaining columns' bound
+  int npairs;
   int band_pct;       // DTW/Frechet band, <0 none
   int delta;          // LCSS window, <0 none
   float eps;          // LCSS threshold
   int buf_len;        // shared-memory values per segment (>= max candidate length)
-  unsigned long long* cells;  // optional: band cells actually computed (atomic)
-  const int* order;   // optional: work item w is pair order[w] (shape-sorted schedule)
   int max_n;          // optional: no query of the pairs is longer (0: unknown)
-  const double* aux;  // optional: a value per pair, passed to the cell policy (else eps)
-  const float4* qtab; // optional: queries' sparse tables (tstride float4 each, queries of
-  int tstride;        //   up to max_n rows): DTW abandoning adds the remaining columns' bound
 };
+static_assert(sizeof(DpArgs) == 120, "DpArgs is passed by value to every DP launch");
 
 enum DpKind {
   DP_DTW_REF = 0,   // Euclidean cost, no FMA: the reference's dtw.cpp arithmetic

@@ -293,3 +293,32 @@ def test_knn_k64_with_many_ties(tsim, cuda_ctx, oracle, pruned):
         ids, d, _, _ = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, k, **kw)
         assert np.array_equal(ids, want_ids), (measure, pruned)
     db.close()
+
+
+def test_frechet_fp64_window_and_tiny_values(tsim, cuda_ctx, oracle):
+    """The exact FP64 Frechet re-score (FP64 costs only in the window around
+    the FP32 optimum) against the oracle, bit for bit: exact duplicates (value
+    0), near-duplicates whose optimum is below 1e-20 (every cell in FP64) and
+    offsets that keep it in the window."""
+    base, bo = G.random_walks(6, 40, 1200)
+    parts, offs = [], [0]
+    rng = np.random.default_rng(1201)
+    for t in range(6):
+        seg = base[bo[t]:bo[t + 1]].astype(np.float64)
+        for scale in (0.0, 1e-12, 1e-3, 0.5):
+            v = seg + scale * rng.standard_normal(seg.shape)
+            parts.append(v.astype(np.float32))
+            offs.append(offs[-1] + len(seg))
+    cp = np.concatenate(parts)
+    co = np.array(offs, np.int64)
+    qp = np.concatenate([base[bo[t]:bo[t + 1]] for t in (0, 3)])
+    qo = np.array([0, 40, 80], np.int64)
+    db = tsim.Database(cuda_ctx, cp, co)
+    k = 8
+    want_ids, want_d = oracle.knn("frechet", qp, qo, cp, co, k)
+    for flags in (tsim.api.FLAG_FP64_RESCORE,
+                  tsim.api.FLAG_FP64_RESCORE | tsim.api.FLAG_ALWAYS_PRUNE):
+        ids, _, d64, _ = _device_knn(tsim, cuda_ctx, db, qp, qo, "frechet", k, flags=flags)
+        assert np.array_equal(ids, want_ids)
+        assert np.array_equal(d64, want_d)
+    db.close()
