@@ -39,7 +39,7 @@ DP_FLOPS_PER_CELL = 8  # 2 sub, mul, fma (2), 2 min, add
 # dram__bytes_read.sum + dram__bytes_write.sum of the survivor-round DP launch
 # of this workload (single stream, planner's R), one ncu capture of
 # `python -m cudaruntime1_gb300.profile_pass 1` on a GB300
-SURVIVOR_DP_DRAM_BYTES = 11568896
+SURVIVOR_DP_DRAM_BYTES = 11567872
 L2_FLUSH_BYTES = 512 << 20
 
 
