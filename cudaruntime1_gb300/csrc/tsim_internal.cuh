@@ -216,10 +216,12 @@ __host__ __device__ inline float ord2f(unsigned u) {
 // launch helpers implemented in the .cu files
 // ---------------------------------------------------------------------------
 // Arguments of the DP kernels, passed by value: kept at 120 bytes.  A
-// version at 136 bytes (two more fields) made the serving workload, which
-// issues tens of thousands of small DP launches per second, 20 % slower (p50
-// 20 -> 24 ms, same build otherwise); hence the shared output slot and the
-// table stride derived from max_n.
+// version at 136 bytes (two more fields) made the serving workload 20 %
+// slower (p50 20 -> 24 ms, same build otherwise, same GPU).  The launch rate
+// does not depend on the argument size (488K empty launches/s from 64 to 512
+// bytes), so the difference lies in the DP kernels' code generation, which
+// near their register caps moves with this struct's definition; hence the
+// shared output slot and the table stride derived from max_n.
 struct DpArgs {
   const float2* qpts;
   const int64_t* qoff;
