@@ -493,8 +493,8 @@ int launch_diag_r(tsim_ctx* ctx, int R, const DpArgs& a, int max_m, int* spill, 
     case 1: return launch_diag_one<P, 1, W>(ctx, a, max_m, spill, nspill);
     case 2: return launch_diag_one<P, 2, W>(ctx, a, max_m, spill, nspill);
     case 4: return launch_diag_one<P, 4, W>(ctx, a, max_m, spill, nspill);
-    case 8:
-      if (W == 1) return launch_diag_one<P, 8, 1>(ctx, a, max_m, spill, nspill);
+    case 8:  // a warp, or a CTA of 8 warps (full rows of up to 2041 columns)
+      if constexpr (W == 1 || W == kCtaWarps) return launch_diag_one<P, 8, W>(ctx, a, max_m, spill, nspill);
       break;
     default:
       if (W == 1) return launch_diag_one<P, 16, 1>(ctx, a, max_m, spill, nspill);
@@ -509,14 +509,14 @@ int launch_chain(tsim_ctx* ctx, int R0, int warps, const DpArgs& a, int max_m, i
   // R0, 2 R0, .. Rmax: each pass takes the pairs the previous one spilled, so
   // every pair runs with the fewest rows per lane-group its shape admits
   // (fewer rows in flight, fewer masked cells); the last pass writes `spill`.
-  // A warp per pair goes to R = 16 (full rows of up to 497 columns), two or
-  // eight warps per pair to R = 4 (253 or 1021 columns).
+  // A warp per pair goes to R = 16 (full rows of up to 497 columns), two
+  // warps per pair to R = 4 (253 columns), a CTA of eight to R = 8 (2041).
   // A pass takes every pair with both lengths >= 2 once the widest band
   // (any band width is at most that of the longest lengths, and
   // 2 (min(n,m) - 1) <= n + m - 2), the window or the longest full row fits
   // its lanes: the chain stops there, and only degenerate pairs are left for
   // the striped kernel.
-  const int rmax = warps == 1 ? 16 : 4;
+  const int rmax = warps == 1 ? 16 : (warps == kCtaWarps ? 8 : 4);
   const int lanes = 32 * warps;
   auto takes_all = [&](int R) {
     if (a.max_n <= 0) return false;  // query lengths unknown

@@ -1772,7 +1772,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
         break;
       }
     a.rdiag_cta = 0;
-    for (int R : {1, 2, 4})
+    for (int R : {1, 2, 4, 8})
       if (diag_ok(p->measure == TSIM_LCSS, n, m, wd, R, 256)) {
         a.rdiag_cta = R;
         break;
@@ -2243,8 +2243,9 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   if (Rd == 0) Rd = 16;  // none fits the longest pair: the widest takes the rest
   const int lanes = kernel == 3 ? 256 : 64;  // a CTA of 8 warps, or 2 warps, per pair
   int Rc = 4;  // the smallest R that fits the longest pair
-  for (int R2 : {4, 2, 1})
-    if (diag_ok(p->measure == TSIM_LCSS, max_qlen, max_clen, wd, R2, lanes)) Rc = R2;
+  for (int R2 : {8, 4, 2, 1})  // R = 8 for a CTA only
+    if ((R2 < 8 || kernel == 3) && diag_ok(p->measure == TSIM_LCSS, max_qlen, max_clen, wd, R2, lanes))
+      Rc = R2;
   TSIM_TRY(arena_reserve(ctx, 2 * align256(sizeof(int) * (size_t)npairs) + 512));
   int* spill = arena_take<int>(ctx, npairs);
   int* nspill = arena_take<int>(ctx, 4);
