@@ -1,31 +1,37 @@
 // dp_diag.cu -- anti-diagonal wavefront DP for banded / windowed pairs.
 //
-// One warp per (query, candidate) pair.  Cell (i, j) is computed at step
-// t = i + j.  Rows are dealt to lanes in groups of R consecutive rows, round
-// robin: lane l owns rows R*(l + 32k) .. R*(l + 32k) + R - 1 for k = 0, 1, ...
-// At step t a lane computes column t - i of each row i of its current group,
-// so all R cells of a step depend only on the previous step: the row above a
-// group (the last row of the previous lane's group) arrives by one register
-// shuffle, and there is no shared-memory row buffer and no per-round skew --
-// the critical path of a pair is its n + m - 1 anti-diagonals.
+// One warp per (query, candidate) pair (or 2 or 8 warps, for the
+// latency-bound rounds).  Cell (i, j) is computed at step t = i + j.  Rows
+// are dealt to lanes in groups of R consecutive rows, round robin: lane l
+// owns rows R*(l + 32k) .. R*(l + 32k) + R - 1 for k = 0, 1, ...  At step t a
+// lane computes column t - i of each row i of its current group, so all R
+// cells of a step depend only on the previous step: the row above a group
+// (the last row of the previous lane's group) arrives by one register
+// shuffle (across warps, through shared memory behind a barrier), and there
+// is no row buffer and no per-round skew -- the critical path of a pair is
+// its n + m - 1 anti-diagonals.
 //
 // A lane moves to its next group when that group's first cell comes up.
 // This is valid when a group has finished -- and the next lane has consumed
 // its last row -- before the lane's next group starts.  With the band
 // |i(m-1) - j(n-1)| <= W (W = w (min(n,m)-1)) that holds whenever
 // 2W < 31 R (n + m - 2); for a full row (no band) when m <= 31 R + 1; for
-// an LCSS window |i - j| <= delta when delta <= 31 R.  Pairs that fail the
-// condition are listed for the round-striped kernel instead (dp_kernels.cu).
+// an LCSS window |i - j| <= delta when delta <= 31 R (32 W lanes: 32 W - 1
+// in place of 31).  Pairs that fail the condition are listed for the next
+// pass, the last one for the round-striped kernel (dp_kernels.cu).
 //
-// No row buffer in shared memory: a lane's band columns come from integer ramps stepped
-// by additions, the query points of its next group are prefetched into
-// registers one group ahead, and the candidate point of the next step is
-// loaded one step ahead from the pair's copy in shared memory (through L1
-// for candidates too long to stage).
+// A lane's band columns come from integer ramps stepped by additions; its
+// next group (band bases and widths, query points, the first candidate
+// point) is prepared ahead for all lanes at once on every 16th step, so a
+// switch is register moves; the candidate point of the next step is loaded
+// one step ahead from the pair's copy in shared memory (through L1 for
+// candidates too long to stage).  The step loop runs two steps per
+// iteration.  Multi-warp pairs are claimed dynamically from a counter.
 //
 // Early abandon: every warping path crosses one of any two consecutive
 // anti-diagonals and DP values never decrease along a path, so the minimum
-// over the last two anti-diagonals bounds the final value from below.
+// over the last two anti-diagonals bounds the final value from below; DTW's
+// survivor round adds the LB_Keogh terms of the columns still ahead.
 #include <type_traits>
 #include <vector>
 
