@@ -114,10 +114,12 @@ __device__ __forceinline__ Ramps make_ramps(int n, int m, int wd, bool lcss) {
 // sparse tables at hand: each pair's columns get a lower bound (the distance
 // from the candidate point to the box of the query rows its band admits),
 // whose suffix sums are kept in shared memory next to the staged candidate.
+// (queries of up to 16,384 points: the per-check sums take (max_n + col_cap)
+// / 16 floats of shared memory per pair)
 template <class P, int W>
 __host__ __device__ bool diag_suffix(const DpArgs& a) {
   return W == 1 && (std::is_same<P, PolDtwSq>::value || std::is_same<P, PolDtwEu>::value) &&
-         a.qtab != nullptr && a.thr != nullptr && a.max_n > 0;
+         a.qtab != nullptr && a.thr != nullptr && a.max_n > 0 && a.max_n <= 16384;
 }
 
 // abandon checks (every 16 steps) of a pair of up to max_n x col_cap points
