@@ -33,7 +33,7 @@ def _rank(rank, world, port, out):
 def test_max_over_ranks_gloo():
     import torch.multiprocessing as mp
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
         assert dict(out) == {0: 11.0, 1: 11.0}
