@@ -17,6 +17,7 @@ _LOCK = threading.Lock()
 TSIM_OK = 0
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
           4: "timeout", 5: "unsupported", 6: "over budget", 7: "pending", 8: "queue full"}
+TSIM_ERR_INVALID_ARG = 1
 TSIM_ERR_BUDGET, TSIM_PENDING, TSIM_ERR_BUSY = 6, 7, 8
 
 DTW, LCSS, FRECHET, HAUSDORFF, EUCLIDEAN = range(5)

@@ -1,5 +1,6 @@
 // capi.cu -- context, scratch arena, device-resident database and status
 // reporting of the C ABI (include/tsim.h).
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
@@ -402,6 +403,7 @@ int tsim_ctx_destroy(tsim_ctx* c) {
   c->dbs.clear();
   if (c->arena && !c->arena_external) cudaFree(c->arena);
   if (c->pinned) cudaFreeHost(c->pinned);
+  if (c->hstage) cudaFree(c->hstage);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   for (auto& ev : c->stage_ev)
@@ -469,8 +471,10 @@ int tsim_db_create(tsim_ctx* ctx, const tsim_point* h_pts, const int64_t* h_off,
   int max_len = 0;
   for (int t = 0; t < count; ++t) {
     TSIM_CHECK_ARG(h_off[t + 1] > h_off[t], "trajectories must be non-empty (offsets increasing)");
+    TSIM_CHECK_ARG(h_off[t + 1] - h_off[t] <= INT32_MAX, "trajectory longer than 2^31 - 1 points");
     max_len = std::max<int64_t>(max_len, h_off[t + 1] - h_off[t]);
   }
+  TSIM_CHECK_ARG(h_pts != nullptr || count == 0, "h_pts is NULL");
   TSIM_CUDA(cudaSetDevice(ctx->device));
   tsim_db* db = new tsim_db;
   db->ctx = ctx;
@@ -527,9 +531,10 @@ int tsim_db_wrap_device(tsim_ctx* ctx, const tsim_point* d_pts, const int64_t* d
   db->total = db->h_off[count];
   int ml = 0;
   for (int t = 0; t < count; ++t) {
-    if (db->h_off[t + 1] <= db->h_off[t] || db->h_off[0] != 0) {
+    if (db->h_off[t + 1] <= db->h_off[t] || db->h_off[0] != 0 ||
+        db->h_off[t + 1] - db->h_off[t] > INT32_MAX) {
       delete db;
-      return fail(TSIM_ERR_INVALID_ARG, "tsim_db_wrap_device: offsets must start at 0 and increase");
+      return fail(TSIM_ERR_INVALID_ARG, "tsim_db_wrap_device: offsets must start at 0 and increase by at most 2^31 - 1");
     }
     ml = std::max<int64_t>(ml, db->h_off[t + 1] - db->h_off[t]);
   }

@@ -55,10 +55,15 @@ bool ensure(DevBuf& b, size_t bytes) {
 tsim_ctx* ctx() {
   int dev = 0;
   cudaGetDevice(&dev);
-  if (g_ctx && g_dev != dev) {
+  if (g_ctx && g_dev != dev) {  // the cached buffers live on the previous device
+    cudaSetDevice(g_dev);
     tsim_ctx_destroy(g_ctx);
     g_ctx = nullptr;
-    for (auto& b : g_buf) b = DevBuf{};
+    for (auto& b : g_buf) {
+      if (b.p) cudaFree(b.p);
+      b = DevBuf{};
+    }
+    cudaSetDevice(dev);
   }
   if (!g_ctx) {
     if (tsim_ctx_create(dev, nullptr, &g_ctx) != TSIM_OK) return nullptr;

@@ -180,8 +180,18 @@ extern "C" int tsim_db_load(tsim_ctx* ctx, const char* path, tsim_db** out) {
   if (h.version != kVersion) return fail(TSIM_ERR_UNSUPPORTED, "unknown database file version");
   if (h.segs != (uint32_t)kSegs)
     return fail(TSIM_ERR_UNSUPPORTED, "database file has another segment count; rebuild it");
-  if (h.count < 0 || h.count > 0x7fffffff || h.total < 0 || h.max_len < 0)
+  if (h.count < 0 || h.count > 0x7fffffff || h.total < 0 || h.total > (int64_t(1) << 56) ||
+      h.max_len < 0 || h.max_len > 0x7fffffff)
     return fail(TSIM_ERR_INVALID_ARG, "corrupt database header");
+  {  // the header's sizes must match the file's before anything is allocated
+    const uint64_t c = (uint64_t)h.count;
+    const uint64_t want = sizeof(Header) + 8 * (c + 1) + 8 * (uint64_t)h.total + 32 * c +
+                          pad8(4 * c) + (16 + 8) * (uint64_t)kSegs * c + 8;
+    if (fseeko(fh.f, 0, SEEK_END) != 0) return fail(TSIM_ERR_INVALID_ARG, "cannot seek database file");
+    const off_t have = ftello(fh.f);
+    if (have < 0 || (uint64_t)have != want || fseeko(fh.f, sizeof(Header), SEEK_SET) != 0)
+      return fail(TSIM_ERR_INVALID_ARG, "database file size does not match its header");
+  }
   Sum s;
   s.add(&h, sizeof(h));
   const size_t n = (size_t)h.count;

@@ -2146,18 +2146,19 @@ extern "C" int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
   const size_t out_bytes = tsim::align256(sizeof(int) * nq * p->k) + tsim::align256(sizeof(float) * nq * p->k);
   TSIM_TRY(tsim::pinned_reserve(ctx, in_bytes + out_bytes));
   // device staging lives in a separate allocation (the arena is reset by the knn call)
-  static thread_local void* dbuf = nullptr;
-  static thread_local size_t dcap = 0;
-  static thread_local int ddev = -1;
-  if (dcap < in_bytes + out_bytes || ddev != ctx->device) {
-    if (dbuf && ddev == ctx->device) cudaFree(dbuf);
-    dbuf = nullptr;
-    TSIM_CUDA(cudaMalloc(&dbuf, in_bytes + out_bytes));
-    dcap = in_bytes + out_bytes;
-    ddev = ctx->device;
+  if (ctx->hstage_cap < in_bytes + out_bytes) {
+    if (ctx->hstage) {
+      TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+      TSIM_CUDA(cudaFree(ctx->hstage));
+      ctx->hstage = nullptr;
+      ctx->hstage_cap = 0;
+    }
+    const size_t cap = std::max(in_bytes + out_bytes, size_t(1) << 20);
+    TSIM_CUDA(cudaMalloc(&ctx->hstage, cap));
+    ctx->hstage_cap = cap;
   }
   char* hp = (char*)ctx->pinned;
-  char* dp = (char*)dbuf;
+  char* dp = (char*)ctx->hstage;
   memcpy(hp, h_qpts, sizeof(tsim_point) * npts);
   memcpy(hp + tsim::align256(sizeof(tsim_point) * npts), h_qoff, 8 * (nq + 1));
   TSIM_CUDA(cudaMemcpyAsync(dp, hp, in_bytes, cudaMemcpyHostToDevice, ctx->stream));

@@ -61,9 +61,12 @@ struct tsim_ctx {
   size_t arena_cap = 0;
   size_t arena_used = 0;
   bool arena_external = false;  // arena lent by a server's pool (not freed or grown here)
-  // pinned host staging for the host-pointer entry points
+  // pinned host staging for the host-pointer entry points, and their device
+  // staging (apart from the arena, which the device-pointer call resets)
   void* pinned = nullptr;
   size_t pinned_cap = 0;
+  void* hstage = nullptr;
+  size_t hstage_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // instrumentation: kernels launched, and per-stage CUDA-event timing on
   // the context stream when profiling is on

@@ -33,5 +33,13 @@ def test_database_file_round_trip(tsim, cuda_ctx, tmp_path):
     short.write_bytes(path.read_bytes()[:-100])
     with pytest.raises(tsim.api._lib.TsimError):
         tsim.Database(cuda_ctx, path=short)
+    # a header claiming 2^31 - 1 trajectories is refused by its size, before
+    # anything is allocated for them
+    huge = bytearray(path.read_bytes())
+    huge[16:24] = (2 ** 31 - 1).to_bytes(8, "little")
+    hp = tmp_path / "huge.tsim"
+    hp.write_bytes(bytes(huge))
+    with pytest.raises(tsim.api._lib.TsimError, match="size does not match"):
+        tsim.Database(cuda_ctx, path=hp)
     db2.close()
     db.close()

@@ -139,6 +139,30 @@ def test_context_destroyed_before_database(tsim):
     ctx2.close()
 
 
+def test_host_calls_two_contexts_growing_requests(tsim, oracle):
+    """Host-pointer kNN on two contexts of one thread, interleaved, with
+    requests that grow (each context's device staging is its own and grows
+    with the request); a NULL point array is an argument error."""
+    import ctypes as C
+    cp, co = _db(200, 8, 40, 720)
+    ctxs = [tsim.Context(0), tsim.Context(0)]
+    dbs = [tsim.Database(c, cp, co) for c in ctxs]
+    for i, nq in enumerate([1, 3, 40, 2, 90]):
+        qp, qo = G.random_walks(nq, G.uniform_lengths(nq, 4, 60, 730 + i), 740 + i)
+        want_ids, _ = oracle.knn("dtw", qp, qo, cp, co, 4, band_pct=20)
+        for c, db in zip(ctxs, dbs):
+            ids, _, _ = tsim.knn(c, db, qp, qo, "dtw", 4, band_pct=20)
+            assert np.array_equal(ids, want_ids), (nq, ids, want_ids)
+    h = C.c_void_p()
+    off = np.array([0, 3], np.int64)
+    st = ctxs[0].L.tsim_db_create(ctxs[0].h, None, off.ctypes.data, 1, C.byref(h))
+    assert st == tsim._lib.TSIM_ERR_INVALID_ARG and not h.value
+    for db in dbs:
+        db.close()
+    for c in ctxs:
+        c.close()
+
+
 def test_euclidean_knn_prefix_rule_and_long_pairs(tsim, cuda_ctx, oracle):
     """Lock-step Euclidean: candidates of length 64 and a few of 1,100 points
     (> 1024: the FP64 accumulation branch) against queries of 1,100 points;
