@@ -184,7 +184,9 @@ TSIM_API int tsim_band_cells(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
 TSIM_API int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
                       const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
                       float* d_dists, double* d_dists64, tsim_stats* stats);
-/* Host pointers end to end: copies the queries in and the results out. */
+/* Host pointers end to end: copies the queries in and the results out
+ * through the context's pinned and device staging buffers (kept between
+ * calls, grown on demand, freed by tsim_ctx_destroy); synchronous. */
 TSIM_API int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_point* h_qpts,
                            const int64_t* h_qoff, int nq, tsim_db* db, int* h_ids,
                            float* h_dists, tsim_stats* stats);
