@@ -43,7 +43,7 @@ def test_reference_arm_under_torchrun():
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl",
-           "reference", "--steps", "1", "--warmup", "3"]
+           "reference", "--gpus", "2", "--steps", "1", "--warmup", "3"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600,
                        env=dict(os.environ, OMP_NUM_THREADS="2"))
     assert r.returncode == 0, r.stderr[-2000:]
@@ -52,3 +52,12 @@ def test_reference_arm_under_torchrun():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
+    # the bench line's contract, with the reference arm's e2e (no copies)
+    for key in ("metric", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config"):
+        assert key in line, key
+    assert line["n_gpus"] == 2 and line["steps"] == 1 and line["warmup"] == 3
+    assert line["higher_is_better"] is True and line["config"]["workload"]
+    assert line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"],
+                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
