@@ -5,14 +5,17 @@
 // on the device so the whole sequence can be captured in a CUDA graph):
 //   A  lb1_kernel      O(1) bound per (query, candidate) from 36-byte
 //                      summaries (box, first and last point, length); each
-//                      CTA also keeps its chunk's best few candidates;
+//                      CTA also keeps its chunk's best few candidates; once
+//                      B has set the threshold, compact_kernel lists the
+//                      pairs the O(1) bound keeps and segfilter_kernel
+//                      bounds them by 8 column segments per candidate;
 //   B  seeds           the S best chunk candidates per query are refined
 //                      exactly; the k-th best refined value, widened by the
 //                      FP32 error bound, is the query's pruning threshold;
-//   C  compact + lb2   pairs whose O(1) bound passes get the O(length)
-//                      bound (banded LB_Keogh from a sparse table of the
-//                      query in shared memory for DTW, box distances for
-//                      Frechet, the windowed eps-box count for LCSS);
+//   C  lb2_kernel      the listed pairs get the O(length) bound (banded
+//                      LB_Keogh from the query's sparse table in global
+//                      memory for DTW, box distances for Frechet, the
+//                      windowed eps-box count for LCSS);
 //   D  DP              the survivors run the wavefront DP with early
 //                      abandon against the threshold;
 //   E  final           the k-th best FP32 value fixes the re-score set (all
@@ -1370,8 +1373,8 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
   // Latency rounds (few pairs, one wave) pick the kernel by the pair shape
   // (not by the throughput-tuned R): two warps per pair while 64 lanes need
   // at most 2 rows each, longer shapes a CTA per pair.  640 pairs of up to
-  // 512 x 512 points, band 10%: compensated 172 us on two warps against 247
-  // on one and 409 on a CTA; FP32 122, 146 and 270 us.  FP32 rounds of more
+  // 512 x 512 points, band 10%: compensated 149 us on two warps against 206
+  // on one and 358 on a CTA; FP32 112, 128 and 257 us.  FP32 rounds of more
   // pairs than SM sub-partitions (the batched workload's seeds and round 1,
   // with abandoning) ran slower on two warps, so they keep one.
   const bool w2 = latency && a.rdiag_w2 > 0 && a.rdiag_w2 <= 2 &&
