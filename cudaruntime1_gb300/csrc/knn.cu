@@ -679,6 +679,31 @@ __device__ __forceinline__ void warp_append(bool take, int* count, int* list, in
   if (take) list[base + __popc(ball & ((1u << lane) - 1))] = value;
 }
 
+// The same for a whole block of kChunk threads (every thread calls it): one
+// atomic per block.  A query's list has one counter, so a per-warp atomic
+// from every warp of a 1M-candidate scan queued on it (compact_kernel: 311
+// us for 16 queries x 1M candidates at 12 % SM throughput).
+__device__ __forceinline__ void block_append(bool take, int* count, int* list, int value) {
+  __shared__ int wbase[kChunk / 32];
+  __shared__ int bbase;
+  const unsigned ball = __ballot_sync(0xffffffffu, take);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) wbase[warp] = __popc(ball);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int total = 0;
+#pragma unroll
+    for (int w = 0; w < kChunk / 32; ++w) {
+      const int n = wbase[w];
+      wbase[w] = total;
+      total += n;
+    }
+    bbase = total ? atomicAdd(count, total) : 0;
+  }
+  __syncthreads();
+  if (take) list[bbase + wbase[warp] + __popc(ball & ((1u << lane) - 1))] = value;
+}
+
 // Stage A, first half: the pairs the O(1) bound keeps (seeds excluded) are
 // listed (in list2, free until the O(length) stage) ...
 template <int MEAS>
@@ -692,7 +717,7 @@ __global__ void __launch_bounds__(kChunk) compact_kernel(KArgs a) {
     const float b = a.lb1[(size_t)q * a.C + c];
     pass = !seeded && (MEAS == M_LCSS ? (b >= t) : (b <= t));
   }
-  warp_append(pass, a.cnt0 + q, a.list2 + (size_t)q * a.C, c);
+  block_append(pass, a.cnt0 + q, a.list2 + (size_t)q * a.C, c);
 }
 
 // ... and their segment bounds are computed with every lane of a warp busy
