@@ -667,22 +667,11 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
   return fmaxf(fmaxf(acc, accr), lb1);
 }
 
-// append the pair to a per-query list (warp-aggregated)
-__device__ __forceinline__ void warp_append(bool take, int* count, int* list, int value) {
-  const unsigned ball = __ballot_sync(0xffffffffu, take);
-  if (!ball) return;
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(ball) - 1;
-  int base = 0;
-  if (lane == leader) base = atomicAdd(count, __popc(ball));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (take) list[base + __popc(ball & ((1u << lane) - 1))] = value;
-}
-
-// The same for a whole block of kChunk threads (every thread calls it): one
-// atomic per block.  A query's list has one counter, so a per-warp atomic
-// from every warp of a 1M-candidate scan queued on it (compact_kernel: 311
-// us for 16 queries x 1M candidates at 12 % SM throughput).
+// Append the pair to a per-query list, aggregated over a block of kChunk
+// threads (every thread of the block calls it): warp counts through shared
+// memory, one atomic per block.  A query's list has one counter; with an
+// atomic per warp, a 1M-candidate scan queued on it (compact_kernel: 311 us
+// for 16 queries x 1M candidates at 12 % SM throughput; 86 us per block).
 __device__ __forceinline__ void block_append(bool take, int* count, int* list, int value) {
   __shared__ int wbase[kChunk / 32];
   __shared__ int bbase;
@@ -732,7 +721,7 @@ __global__ void __launch_bounds__(256) segfilter_kernel(KArgs a) {
   const int n = a.qlen[q];
   const int start = blockIdx.x * blockDim.x;
   const int stride = gridDim.x * blockDim.x;
-  for (int e0 = start; e0 < cnt; e0 += stride) {  // uniform per warp: whole warps iterate
+  for (int e0 = start; e0 < cnt; e0 += stride) {  // uniform per block: whole blocks iterate
     const int e = e0 + threadIdx.x;
     bool pass = false;
     int c = 0;
@@ -743,7 +732,7 @@ __global__ void __launch_bounds__(256) segfilter_kernel(KArgs a) {
       pass = MEAS == M_LCSS ? (sbnd >= t) : (sbnd <= t);
       if (pass) a.lb1[(size_t)q * a.C + c] = sbnd;
     }
-    warp_append(pass, a.cnt1 + q, a.list1 + (size_t)q * a.C, c);
+    block_append(pass, a.cnt1 + q, a.list1 + (size_t)q * a.C, c);
   }
 }
 
