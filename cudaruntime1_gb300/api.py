@@ -32,7 +32,8 @@ def _pts(a) -> np.ndarray:
     a = np.ascontiguousarray(a, dtype=np.float32)
     if a.ndim == 1:
         a = a.reshape(-1, 2)
-    assert a.ndim == 2 and a.shape[1] == 2, "points must be [N, 2] float32"
+    if a.ndim != 2 or a.shape[1] != 2:
+        raise ValueError(f"points must be [N, 2] float32, got shape {a.shape}")
     return a
 
 

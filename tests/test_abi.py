@@ -5,6 +5,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -75,5 +76,8 @@ def test_loads_and_reports_errors_without_gpu(tsim):
 
 
 def test_python_api_raises_on_bad_input(tsim):
-    with pytest.raises(AssertionError):
+    with pytest.raises(ValueError):
         tsim.api._pts([[1.0, 2.0, 3.0]])
+    with pytest.raises(ValueError):  # reference-named entry points check sizes first
+        tsim.api.launch_dtw_batch_gpu_knn(np.zeros((10, 2), np.float32),
+                                          np.zeros((10, 2), np.float32), 4, 5, 5)
