@@ -81,3 +81,74 @@ def test_python_api_raises_on_bad_input(tsim):
     with pytest.raises(ValueError):  # reference-named entry points check sizes first
         tsim.api.launch_dtw_batch_gpu_knn(np.zeros((10, 2), np.float32),
                                           np.zeros((10, 2), np.float32), 4, 5, 5)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include "tsim.h"
+int main(void) {
+  tsim_ctx* ctx = NULL;
+  int st = tsim_ctx_create(0, NULL, &ctx);
+  printf("%d %s %d\n", tsim_version(), tsim_status_string(TSIM_OK), st);
+  if (st == TSIM_OK) return tsim_ctx_destroy(ctx);
+  printf("%s\n", tsim_last_error());
+  return 0;
+}
+"""
+
+CPP_CALLER = r"""
+#include <cmath>
+#include <cstdio>
+#include "dtw.cuh"
+#include "euclidean.cuh"
+#include "frechet.cuh"
+#include "hausdorff.cuh"
+#include "lcss.cuh"
+int main() {
+  Point a[8];
+  for (int i = 0; i < 8; ++i) a[i] = Point{float(i), float(i % 3)};
+  float out[2] = {-1.f, -1.f}, ms = 0.f;
+  launch_dtw_batch_gpu_knn(a, a, out, 2, 4, 4, ms);  // each query against itself
+  std::printf("%d %g %g\n", std::isnan(out[0]) ? 1 : 0, out[0], out[1]);
+  return 0;
+}
+"""
+
+
+def test_c_and_cpp_callers_build_against_the_headers(tsim, tmp_path):
+    """A C caller of include/tsim.h and a C++ caller of the reference-named
+    headers (include/compat/) compile, link against libtsim.so and run: the
+    same steps a reference caller takes after switching libraries.  Without
+    a GPU the context call fails with a status and the reference-named call
+    (TSIM_COMPAT_NO_EXIT set) reports and returns NaN."""
+    import shutil
+    import torch
+    if not (shutil.which("gcc") and shutil.which("g++")):
+        pytest.skip("no host C/C++ compiler")
+    libdir = os.path.dirname(tsim._lib.lib_path())
+    inc = os.path.join(ROOT, "include")
+    cuda_inc = "/usr/local/cuda/include"
+    link = ["-L" + libdir, "-ltsim", "-Wl,-rpath," + libdir]
+    (tmp_path / "c.c").write_text(C_CALLER)
+    (tmp_path / "cpp.cpp").write_text(CPP_CALLER)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I" + inc, str(tmp_path / "c.c"),
+                        "-o", str(tmp_path / "c_caller")] + link, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I" + os.path.join(inc, "compat"),
+                        "-I" + cuda_inc, str(tmp_path / "cpp.cpp"), "-o", str(tmp_path / "cpp_caller")]
+                       + link, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(tmp_path / "c_caller")], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    version, ok, status = out.stdout.split("\n")[0].split()
+    assert int(version) >= 10000 and ok == "ok"
+    assert (int(status) == 0) == torch.cuda.is_available()
+    env = dict(os.environ, TSIM_COMPAT_NO_EXIT="1")
+    out = subprocess.run([str(tmp_path / "cpp_caller")], capture_output=True, text=True,
+                         timeout=120, env=env)
+    assert out.returncode == 0, out.stderr
+    nan, v0, v1 = out.stdout.split()
+    if torch.cuda.is_available():
+        assert nan == "0" and float(v0) == 0.0 and float(v1) == 0.0
+    else:
+        assert nan == "1" and "Error" in out.stderr
