@@ -151,7 +151,9 @@ TSIM_API int tsim_probe_fp32_tflops(tsim_ctx* ctx, double* tflops);
 
 /* ---- device-resident candidate database ---------------------------------- */
 /* Copies host points/offsets to the device and builds per-trajectory
- * summaries (bounding box, first/last point). */
+ * summaries (bounding box, first/last point).  Offsets start at 0 and
+ * increase (no empty trajectory, none over 2^31 - 1 points); host_pts may be
+ * NULL only when count is 0.  TSIM_ERR_INVALID_ARG otherwise. */
 TSIM_API int tsim_db_create(tsim_ctx* ctx, const tsim_point* host_pts, const int64_t* host_off,
                             int count, tsim_db** out);
 /* Wraps device-resident points/offsets (not copied, caller keeps them alive).
