@@ -123,7 +123,12 @@ TSIM_API const char* tsim_last_error(void);
 TSIM_API int tsim_version(void);
 
 /* ---- context ------------------------------------------------------------ */
-/* stream: a cudaStream_t, or NULL for a stream the context creates. */
+/* Threads: a context, and the databases created on it, serve one thread at a
+ * time (the caller serialises calls on one context; separate contexts run
+ * concurrently).  A server's submit and wait may be called from any number
+ * of threads, and the reference-named entry points serialise themselves on
+ * their shared context.
+ * stream: a cudaStream_t, or NULL for a stream the context creates. */
 TSIM_API int tsim_ctx_create(int device, void* stream, tsim_ctx** out);
 TSIM_API int tsim_ctx_destroy(tsim_ctx* ctx);
 TSIM_API int tsim_ctx_set_stream(tsim_ctx* ctx, void* stream);
