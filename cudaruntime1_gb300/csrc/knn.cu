@@ -1422,7 +1422,7 @@ int refine32(tsim_ctx* ctx, const KArgs& a, int dp32, int G, int R, const DpArgs
              bool latency = false) {
   if (is_dp(MEAS)) return run_dp(ctx, a, dp32, G, R, d, latency);
   PwArgs p{d.qpts, d.qoff, d.cpts, d.coff, d.pairs, d.npairs, d.npairs_dev, d.order, d.out,
-           nullptr, d.thr};
+           nullptr, d.thr, d.cells};
   return launch_pairwise(ctx, MEAS == M_HAUSDORFF ? TSIM_HAUSDORFF : TSIM_EUCLIDEAN, p);
 }
 

@@ -30,11 +30,13 @@ __device__ __forceinline__ float d2f(float ax, float ay, float bx, float by) {
   return fmaf(dy, dy, dx * dx);
 }
 
-// max over S of min over T of |s - t|^2 (FP32); stops above `stop`
+// max over S of min over T of |s - t|^2 (FP32); stops above `stop`.
+// *pairs (lane 0's copy) grows by the point pairs compared.
 __device__ float warp_directed(const float2* S, int ns, const float2* T, int nt, float run,
-                               float stop) {
+                               float stop, long long* pairs) {
   const int lane = threadIdx.x & 31;
   for (int base = 0; base < ns; base += 32 * kMaxRegPts) {
+    *pairs += (long long)min(32 * kMaxRegPts, ns - base) * nt;
     float sx[kMaxRegPts], sy[kMaxRegPts], mn[kMaxRegPts];
 #pragma unroll
     for (int u = 0; u < kMaxRegPts; ++u) {
@@ -74,13 +76,17 @@ __global__ void __launch_bounds__(kPwThreads) hausdorff_refine_kernel(PwArgs a) 
     const int64_t qo = a.qoff[pr.x], co = a.coff[pr.y];
     const int n = (int)(a.qoff[pr.x + 1] - qo), m = (int)(a.coff[pr.y + 1] - co);
     float v = TSIM_INF;
+    long long pairs = 0;
     if (n > 0 && m > 0) {
       const float stop = a.thr ? a.thr[pr.x] : TSIM_INF;
-      v = warp_directed(a.qpts + qo, n, a.cpts + co, m, 0.0f, stop);
-      if (v <= stop) v = warp_directed(a.cpts + co, m, a.qpts + qo, n, v, stop);
+      v = warp_directed(a.qpts + qo, n, a.cpts + co, m, 0.0f, stop, &pairs);
+      if (v <= stop) v = warp_directed(a.cpts + co, m, a.qpts + qo, n, v, stop, &pairs);
       if (v > stop) v = TSIM_INF;  // abandoned: cannot be among the k best
     }
-    if (lane == 0) a.out[pid] = v;
+    if (lane == 0) {
+      a.out[pid] = v;
+      if (a.cells && pairs) atomicAdd(a.cells, (unsigned long long)pairs);
+    }
   }
 }
 
@@ -136,7 +142,10 @@ __global__ void __launch_bounds__(kPwThreads) euclid_refine_kernel(PwArgs a) {
       const float stop = a.thr ? a.thr[pr.x] : TSIM_INF;
       if (v > stop) v = TSIM_INF;
     }
-    if (lane == 0) a.out[pid] = v;
+    if (lane == 0) {
+      a.out[pid] = v;
+      if (a.cells && n >= m && m > 0) atomicAdd(a.cells, (unsigned long long)m);
+    }
   }
 }
 

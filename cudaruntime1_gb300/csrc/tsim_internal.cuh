@@ -300,6 +300,7 @@ struct PwArgs {
   float* out;       // FP32 pass: squared Hausdorff / squared Euclidean, +inf if abandoned
   double* out64;    // FP64 pass
   const float* thr; // per query abandon threshold or null
+  unsigned long long* cells = nullptr;  // point pairs compared (FP32 pass), or null
 };
 int launch_pairwise(tsim_ctx* ctx, int measure, const PwArgs& a);
 int launch_pairwise64(tsim_ctx* ctx, int measure, const PwArgs& a);

@@ -26,11 +26,13 @@ MEASURE_PARAMS = {
 }
 
 
-def device_random_walks(count: int, lo: int, hi: int, seed: int, device="cuda"):
+def device_random_walks(count: int, lo: int, hi: int, seed: int, device="cuda",
+                        keep_host: bool = False):
     """``count`` random walks with lengths U[lo, hi] (start uniform in
     [0,100]^2, N(0,1) steps per coordinate), generated on the host with
     numpy's seeded generator and copied to ``device``.  Returns (points
-    float32 [total, 2], offsets int64 [count+1], max_len) as torch tensors."""
+    float32 [total, 2], offsets int64 [count+1], max_len) as torch tensors,
+    followed by the host arrays (points, offsets) when ``keep_host``."""
     import torch
     rng = np.random.default_rng(seed)
     lens = rng.integers(lo, hi + 1, count).astype(np.int64)
@@ -42,8 +44,11 @@ def device_random_walks(count: int, lo: int, hi: int, seed: int, device="cuda"):
     del steps
     origin = rng.random((count, 2)) * 100.0
     cs -= np.repeat(cs[off[:-1]] - origin, lens, axis=0)
-    pts = torch.from_numpy(cs.astype(np.float32)).to(device)
-    return pts, torch.from_numpy(off).to(device), int(lens.max())
+    host = cs.astype(np.float32)
+    del cs
+    pts = torch.from_numpy(host).to(device)
+    out = (pts, torch.from_numpy(off).to(device), int(lens.max()))
+    return out + ((host, off),) if keep_host else out
 
 
 def make_requests(n: int, qlo: int, qhi: int, seed: int, measures=None):
@@ -63,10 +68,13 @@ def _pct(a, q):
     return float(np.percentile(np.asarray(a), q)) if len(a) else None
 
 
-def run_open_loop(server, requests, rate: float, k: int = 10, seed: int = 0):
+def run_open_loop(server, requests, rate: float, k: int = 10, seed: int = 0, keep=(),
+                  kept=None):
     """Submit ``requests`` at Poisson arrival times of ``rate`` per second and
     collect them.  Latency of a request = scheduled arrival -> results on the
-    host (includes any lag of the submitting thread)."""
+    host (includes any lag of the submitting thread).  The results (ids,
+    distances) of the requests whose indices are in ``keep`` are stored in
+    the dict ``kept``."""
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(requests)))
     tickets = [None] * len(requests)
@@ -93,7 +101,9 @@ def run_open_loop(server, requests, rate: float, k: int = 10, seed: int = 0):
     t_last = t0
     for i in range(len(requests)):
         ready.acquire()
-        _, _, info = server.wait(tickets[i])
+        ids, dists, info = server.wait(tickets[i])
+        if kept is not None and i in keep:
+            kept[i] = (ids, dists)
         t_last = max(t_last, time.perf_counter())
         info["measure"] = requests[i][0]
         info["qlen"] = int(requests[i][2][-1])

@@ -309,15 +309,19 @@ TSIM_API int tsim_ref_batch(tsim_ctx* ctx, int measure, const tsim_point* d_t1,
  * results as tsim_ref_batch, on the caller's stream (NULL = legacy default
  * stream), with no context and no cudaMalloc/cudaFree: scratch comes from a
  * fixed array of TSIM_STATIC_SCRATCH_BYTES in the library's device memory.
- * Limit: the call needs about 12*10*num_t + 16*(num_t+1) bytes of scratch and
- * its candidate keys (8*num_t bytes) plus envelopes (16*m bytes) must fit in
- * 200 KiB of shared memory; larger calls return TSIM_ERR_UNSUPPORTED.
- * The first call on each device looks up the array's device address with that
- * device current (cudaGetSymbolAddress); make that first call before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race, so the caller serialises them (one stream, or its own lock).  The
- * array keeps the last call's contents; nothing in it needs clearing, as
- * every entry read is written earlier in the same call. */
+ * Limit: the candidate keys (8*num_t bytes) and envelopes (16*m bytes) must
+ * fit in 200 KiB of shared memory, i.e. num_t <= 25600 - 2*m (the scratch
+ * array, about 136*num_t bytes, is not the binding limit); larger calls
+ * return TSIM_ERR_UNSUPPORTED.  The kernels run on the current device, and a
+ * non-NULL stream must belong to it (TSIM_ERR_INVALID_ARG otherwise).
+ * The first call in each CUDA context (per device: the runtime's primary
+ * context, or a driver-API context the caller made current; again after a
+ * cudaDeviceReset) looks up the array's device address in that context
+ * (cudaGetSymbolAddress) and caches it by the context's unique id; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race, so the caller serialises them (one stream,
+ * or its own lock).  The array keeps the last call's contents; nothing in it
+ * needs clearing, as every entry read is written earlier in the same call. */
 TSIM_API int tsim_ref_batch_static(int measure, const tsim_point* d_t1, const tsim_point* d_t2,
                                    int num_t, int n, int m, float epsilon, float* d_out,
                                    void* stream);

@@ -836,3 +836,291 @@ int orc_dtw_knn_pruned(const orc_params* p, const float* qpts, const int64_t* qo
   if (cells_out) *cells_out = cells_total;
   return 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* pruned exact kNN for every measure (parity checks on large databases)      */
+/* ------------------------------------------------------------------------- */
+
+/* Every bound below is a valid bound on the key the brute force ranks by,
+ * as computed in FP64: the rounding of each operation is monotone, so a
+ * bound assembled from the same float coordinates by the same (or fewer,
+ * smaller) operations never exceeds the computed value.  Candidates are
+ * visited in bound order in parallel chunks; a chunk is evaluated against
+ * the k-th key known when it starts (early abandon only when the computed
+ * value already exceeds it), and the visit stops at the first bound above
+ * the k-th key.  The result equals orc_knn's, ties included. */
+
+typedef struct {
+  double x0, x1, y0, y1;
+} dbox_t;
+
+static dbox_t box64(const float* t, int len) {
+  dbox_t b = {t[0], t[0], t[1], t[1]};
+  for (int i = 1; i < len; i++) {
+    double x = t[2 * i], y = t[2 * i + 1];
+    if (x < b.x0) b.x0 = x;
+    if (x > b.x1) b.x1 = x;
+    if (y < b.y0) b.y0 = y;
+    if (y > b.y1) b.y1 = y;
+  }
+  return b;
+}
+
+/* squared distance from p to the box: each axis gap is the difference of p
+ * and the nearest box edge, itself a coordinate of some point, so it never
+ * exceeds the computed gap to any point of the box's trajectory */
+static inline double ptbox_d2(const float* p, dbox_t b) {
+  double px = p[0], py = p[1];
+  double dx = px < b.x0 ? b.x0 - px : (px > b.x1 ? px - b.x1 : 0.0);
+  double dy = py < b.y0 ? b.y0 - py : (py > b.y1 ? py - b.y1 : 0.0);
+  return dx * dx + dy * dy;
+}
+
+/* max over the points of t of their squared distance to box b */
+static double max_ptbox_d2(const float* t, int len, dbox_t b) {
+  double mx = 0.0;
+  for (int i = 0; i < len; i++) {
+    double d = ptbox_d2(t + 2 * i, b);
+    if (d > mx) mx = d;
+  }
+  return mx;
+}
+
+/* LCSS: points of t that could match some point of the set boxed by b
+ * (|dx| < eps and |dy| < eps in float, as orc_lcss_count tests them) */
+static int lcss_matchable(const float* t, int len, const float* bx, int blen, float eps) {
+  float x0 = bx[0], x1 = bx[0], y0 = bx[1], y1 = bx[1];
+  for (int j = 1; j < blen; j++) {
+    float x = bx[2 * j], y = bx[2 * j + 1];
+    if (x < x0) x0 = x;
+    if (x > x1) x1 = x;
+    if (y < y0) y0 = y;
+    if (y > y1) y1 = y;
+  }
+  int cnt = 0;
+  for (int i = 0; i < len; i++) {
+    float x = t[2 * i], y = t[2 * i + 1];
+    int out = (x > x1 && fabsf(x - x1) >= eps) || (x < x0 && fabsf(x - x0) >= eps) ||
+              (y > y1 && fabsf(y - y1) >= eps) || (y < y0 && fabsf(y - y0) >= eps);
+    cnt += !out;
+  }
+  return cnt;
+}
+
+/* discrete Frechet (orc_frechet64's arithmetic) abandoning once a row's
+ * smallest value has a square root above thr */
+static double frechet64_ab(const float* a, int n, const float* b, int m, double thr) {
+  const double INF = INFINITY;
+  double* prev = (double*)malloc(sizeof(double) * 2 * (size_t)m);
+  double* cur = prev + m;
+  double r = INF;
+  for (int i = 0; i < n; i++) {
+    double rowmin = INF;
+    for (int j = 0; j < m; j++) {
+      double d = d2_64(a + 2 * i, b + 2 * j);
+      double mn;
+      if (i == 0 && j == 0)
+        mn = 0.0;
+      else {
+        double up = i > 0 ? prev[j] : INF;
+        double lf = j > 0 ? cur[j - 1] : INF;
+        double dg = (i > 0 && j > 0) ? prev[j - 1] : INF;
+        mn = up < lf ? up : lf;
+        mn = dg < mn ? dg : mn;
+      }
+      cur[j] = d > mn ? d : mn;
+      if (cur[j] < rowmin) rowmin = cur[j];
+    }
+    if (sqrt(rowmin) > thr) goto done;
+    double* t = prev;
+    prev = cur;
+    cur = t;
+  }
+  r = sqrt(prev[m - 1]);
+done:
+  free(prev < cur ? prev : cur);
+  return r;
+}
+
+/* directed64 with the early break of a point whose running minimum cannot
+ * raise the maximum, abandoning once the maximum's root exceeds thr;
+ * returns the squared directed distance, or +inf when abandoned */
+static double directed64_ab(const float* A, int na, const float* B, int nb, double mx,
+                            double thr) {
+  for (int i = 0; i < na; i++) {
+    double mn = INFINITY;
+    for (int j = 0; j < nb; j++) {
+      double d = d2_64(A + 2 * i, B + 2 * j);
+      if (d < mn) {
+        mn = d;
+        if (mn <= mx) break;
+      }
+    }
+    if (mn > mx) {
+      mx = mn;
+      if (sqrt(mx) > thr) return INFINITY;
+    }
+  }
+  return mx;
+}
+
+static double euclid64_ab(const float* q, int n, const float* c, int m, double thr) {
+  if (n < m) return INFINITY;
+  double s = 0.0;
+  for (int i = 0; i < m; i++) {
+    s += d2_64(q + 2 * i, c + 2 * i);
+    if ((i & 15) == 15 && sqrt(s) > thr) return INFINITY;
+  }
+  return sqrt(s);
+}
+
+/* banded LB_Keogh of DTW over the candidate's columns (first and last
+ * columns exact), as the CPU baseline computes it */
+static double dtw_lb64(const orc_params* p, const sparse_t* sp, const float* a, int n,
+                       const float* b, int m) {
+  int w = orc_band_w(n, m, p->band_pct);
+  double lb = 0.0;
+  for (int j = 0; j < m; j++) {
+    int lo, hi;
+    orc_band_row(j, m, n, w, &lo, &hi);
+    if (lo > hi) return INFINITY;
+    double t;
+    if (j == 0)
+      t = d2_64(a, b);
+    else if (j == m - 1)
+      t = d2_64(a + 2 * (n - 1), b + 2 * j);
+    else
+      t = sparse_box_d2(sp, lo, hi, b + 2 * j);
+    if (p->cost == ORC_COST_EUCLID) t = sqrt(t);
+    lb += t;
+  }
+  if (m == 1 && n > 1) {
+    double t = d2_64(a + 2 * (n - 1), b);
+    lb += p->cost == ORC_COST_EUCLID ? sqrt(t) : t;
+  }
+  return lb;
+}
+
+int orc_knn_pruned(const orc_params* p, const float* qpts, const int64_t* qoff, int nq,
+                   const float* dbpts, const int64_t* dboff, int ndb, int* ids, double* dists,
+                   int nthreads, int64_t* evaluated_out) {
+  const int k = p->k;
+  if (k <= 0) return 1;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#endif
+  const int lcss = p->measure == ORC_LCSS;
+  /* DTW's bound and DP sum round differently (both ~1e-16 relative) */
+  const double slack = p->measure == ORC_DTW ? 1.0 + 1e-12 : 1.0;
+  int maxm = 1;
+  for (int c = 0; c < ndb; c++) {
+    int m = (int)(dboff[c + 1] - dboff[c]);
+    if (m > maxm) maxm = m;
+  }
+  lbk_t* order = (lbk_t*)malloc(sizeof(lbk_t) * (ndb > 0 ? ndb : 1));
+  int chunk_cap = 8 * nthreads;
+  double* val = (double*)malloc(sizeof(double) * chunk_cap);
+  dk_t* top = (dk_t*)malloc(sizeof(dk_t) * k);
+  int64_t evaluated = 0;
+  for (int q = 0; q < nq; q++) {
+    const float* a = qpts + 2 * qoff[q];
+    const int n = (int)(qoff[q + 1] - qoff[q]);
+    const dbox_t qb = box64(a, n);
+    sparse_t sp;
+    sp.mn_x = NULL;
+    if (p->measure == ORC_DTW) sparse_build(&sp, a, n);
+    /* keys: the brute force's ranking key (LCSS: minus the count) */
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+    for (int c = 0; c < ndb; c++) {
+      const float* b = dbpts + 2 * dboff[c];
+      const int m = (int)(dboff[c + 1] - dboff[c]);
+      double lb;
+      switch (p->measure) {
+        case ORC_DTW: lb = dtw_lb64(p, &sp, a, n, b, m); break;
+        case ORC_LCSS: {
+          int ua = lcss_matchable(a, n, b, m, p->epsilon);
+          int ub = lcss_matchable(b, m, a, n, p->epsilon);
+          lb = -(double)(ua < ub ? ua : ub);
+          break;
+        }
+        case ORC_FRECHET:
+        case ORC_HAUSDORFF: {
+          double e2 = max_ptbox_d2(b, m, qb), d2 = max_ptbox_d2(a, n, box64(b, m));
+          if (p->measure == ORC_FRECHET) {
+            double t = d2_64(a, b);
+            if (t > e2) e2 = t;
+            t = d2_64(a + 2 * (n - 1), b + 2 * (m - 1));
+            if (t > e2) e2 = t;
+          }
+          lb = sqrt(e2 > d2 ? e2 : d2);
+          break;
+        }
+        default: { /* lock-step: the first and last terms of the sum */
+          if (n < m) {
+            lb = INFINITY;
+          } else {
+            double s = d2_64(a, b);
+            if (m > 1) s += d2_64(a + 2 * (m - 1), b + 2 * (m - 1));
+            lb = sqrt(s);
+          }
+          break;
+        }
+      }
+      order[c].lb = lb;
+      order[c].idx = c;
+    }
+    free(sp.mn_x);
+    qsort(order, ndb, sizeof(lbk_t), lbk_cmp);
+    int cnt = 0;
+    double thr = INFINITY;
+    int e = 0;
+    while (e < ndb) {
+      if (cnt == k && order[e].lb > thr * slack) break;
+      int nch = 0;
+      while (nch < chunk_cap && e + nch < ndb && !(cnt == k && order[e + nch].lb > thr * slack))
+        nch++;
+      const double thr0 = thr;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1)
+      for (int t = 0; t < nch; t++) {
+        const int c = order[e + t].idx;
+        const float* b = dbpts + 2 * dboff[c];
+        const int m = (int)(dboff[c + 1] - dboff[c]);
+        double v;
+        switch (p->measure) {
+          case ORC_DTW: {
+            double* rows = (double*)malloc(sizeof(double) * 2 * (size_t)maxm);
+            v = dtw64_core(a, n, b, m, orc_band_w(n, m, p->band_pct), p->cost, thr0, rows,
+                           rows + maxm, NULL);
+            free(rows);
+            break;
+          }
+          case ORC_LCSS: v = -(double)orc_lcss_count(a, n, b, m, p->epsilon, p->delta); break;
+          case ORC_FRECHET: v = frechet64_ab(a, n, b, m, thr0); break;
+          case ORC_HAUSDORFF: {
+            double h1 = directed64_ab(a, n, b, m, 0.0, thr0);
+            double h = h1 == INFINITY ? INFINITY : directed64_ab(b, m, a, n, h1, thr0);
+            v = h == INFINITY ? INFINITY : sqrt(h);
+            break;
+          }
+          default: v = euclid64_ab(a, n, b, m, thr0); break;
+        }
+        val[t] = v;
+      }
+      evaluated += nch;
+      /* abandoned values (+inf) lie above the k-th key and are refused */
+      for (int t = 0; t < nch; t++) topk_insert(top, &cnt, k, val[t], order[e + t].idx);
+      if (cnt == k) thr = top[k - 1].key;
+      e += nch;
+    }
+    for (int x = 0; x < k; x++) {
+      ids[(size_t)q * k + x] = x < cnt ? top[x].idx : -1;
+      dists[(size_t)q * k + x] = x < cnt ? (lcss ? -top[x].key : top[x].key)
+                                         : (lcss ? -1.0 : INFINITY);
+    }
+  }
+  free(order);
+  free(val);
+  free(top);
+  if (evaluated_out) *evaluated_out = evaluated;
+  return 0;
+}

@@ -101,6 +101,17 @@ int orc_dtw_knn_pruned(const orc_params* p, const float* qpts, const int64_t* qo
                        const float* dbpts, const int64_t* dboff, int ndb, int* ids,
                        double* dists, int nthreads, int64_t* cells_out);
 
+/* Exact kNN with bound pruning for every measure: candidates visited in
+ * order of an FP64 bound on their ranking key (DTW: banded LB_Keogh;
+ * Frechet / Hausdorff: endpoints and point-to-box distances; LCSS: points
+ * that could match the other's epsilon-inflated box; Euclidean: first and
+ * last terms), in parallel chunks with early abandon against the k-th key.
+ * Results equal orc_knn's, ties included; *evaluated (may be NULL) counts
+ * the candidates whose exact value was computed. */
+int orc_knn_pruned(const orc_params* p, const float* qpts, const int64_t* qoff, int nq,
+                   const float* dbpts, const int64_t* dboff, int ndb, int* ids, double* dists,
+                   int nthreads, int64_t* evaluated);
+
 int orc_num_threads(void);
 
 #ifdef __cplusplus

@@ -39,13 +39,26 @@ class OrcParams(C.Structure):
                 ("band_pct", C.c_int), ("epsilon", C.c_float), ("delta", C.c_int)]
 
 
+# where the reference's CPU sources are read from: TSIM_REFERENCE_DIR, else
+# the read-only checkout of the build host (absent on other machines)
+REFERENCE_DIR_DEFAULT = "/root/reference/CudaRuntime1"
+
+
+def reference_dir():
+    """The directory holding the reference's dtw.cpp, lcss.cpp, frechet.cpp,
+    or None where there is none."""
+    d = os.environ.get("TSIM_REFERENCE_DIR") or REFERENCE_DIR_DEFAULT
+    return d if os.path.isfile(os.path.join(d, "dtw.cpp")) else None
+
+
 def build(ref: bool = True) -> None:
     """Compile liboracle.so (always) and _ref/libref.so (when the reference
-    sources are present)."""
+    sources are present), passing the reference directory to make."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if ref and os.path.isdir(os.environ.get("TSIM_REFERENCE_DIR",
-                                            "/root/reference/CudaRuntime1")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    d = reference_dir()
+    if ref and d:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "refgpu", "REF=" + os.path.abspath(d)],
+                       check=True)
 
 
 def lib():
@@ -84,6 +97,8 @@ def lib():
                                   _ip, _dp, C.c_int]
             L.orc_dtw_knn_pruned.argtypes = [C.POINTER(OrcParams), _fp, _i64p, C.c_int, _fp,
                                              _i64p, C.c_int, _ip, _dp, C.c_int, _i64p]
+            L.orc_knn_pruned.argtypes = [C.POINTER(OrcParams), _fp, _i64p, C.c_int, _fp, _i64p,
+                                         C.c_int, _ip, _dp, C.c_int, _i64p]
             L.orc_num_threads.restype = C.c_int
             _LIB = L
     return _LIB
@@ -239,6 +254,26 @@ def dtw_knn_pruned(qpts, qoff, dbpts, dboff, k: int, *, band_pct=-1, cost=COST_S
                              dboff.ctypes.data_as(_i64p), ndb, ids.ctypes.data_as(_ip),
                              d.ctypes.data_as(_dp), nthreads, C.byref(cells))
     return ids.reshape(nq, k), d.reshape(nq, k), cells.value
+
+
+def knn_pruned(measure: str, qpts, qoff, dbpts, dboff, k: int, *, band_pct=-1,
+               cost=COST_SQEUCLID, eps=0.5, delta=-1, nthreads=0, evaluated=False):
+    """Exact kNN with FP64 bound pruning (same results as ``knn``, ties
+    included), for parity checks against large databases.  Returns (ids,
+    dists) or, with ``evaluated``, (ids, dists, candidates evaluated)."""
+    qpts, dbpts = _pts(qpts), _pts(dbpts)
+    qoff = np.ascontiguousarray(qoff, np.int64)
+    dboff = np.ascontiguousarray(dboff, np.int64)
+    nq, ndb = len(qoff) - 1, len(dboff) - 1
+    ids = np.zeros(nq * k, np.int32)
+    d = np.zeros(nq * k, np.float64)
+    ev = C.c_int64(0)
+    p = _params(measure, k, cost, band_pct, eps, delta)
+    lib().orc_knn_pruned(C.byref(p), _f(qpts), qoff.ctypes.data_as(_i64p), nq, _f(dbpts),
+                         dboff.ctypes.data_as(_i64p), ndb, ids.ctypes.data_as(_ip),
+                         d.ctypes.data_as(_dp), nthreads, C.byref(ev))
+    out = (ids.reshape(nq, k), d.reshape(nq, k))
+    return out + (ev.value,) if evaluated else out
 
 
 def num_threads() -> int:

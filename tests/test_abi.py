@@ -152,3 +152,86 @@ def test_c_and_cpp_callers_build_against_the_headers(tsim, tmp_path):
         assert nan == "0" and float(v0) == 0.0 and float(v1) == 0.0
     else:
         assert nan == "1" and "Error" in out.stderr
+
+
+CPP_GOLDEN_CALLER = r"""
+#include <cstdio>
+#include <vector>
+#include "dtw.cuh"
+#include "frechet.cuh"
+#include "hausdorff.cuh"
+#include "lcss.cuh"
+// reads num_t, n, m, eps and the two AoS point sets; writes DTW, LCSS,
+// Frechet and Hausdorff (R-tree pipeline, top_k 10) results, num_t each
+int main(int argc, char** argv) {
+  if (argc != 3) return 2;
+  FILE* f = std::fopen(argv[1], "rb");
+  if (!f) return 3;
+  int dims[3];
+  float eps;
+  if (std::fread(dims, sizeof(int), 3, f) != 3 || std::fread(&eps, sizeof(float), 1, f) != 1)
+    return 4;
+  const int num_t = dims[0], n = dims[1], m = dims[2];
+  std::vector<Point> t1((size_t)num_t * n), t2((size_t)num_t * m);
+  if (std::fread(t1.data(), sizeof(Point), t1.size(), f) != t1.size() ||
+      std::fread(t2.data(), sizeof(Point), t2.size(), f) != t2.size())
+    return 5;
+  std::fclose(f);
+  std::vector<float> out(4 * (size_t)num_t, -1.f);
+  float ms = 0.f;
+  launch_dtw_batch_gpu_knn(t1.data(), t2.data(), out.data(), num_t, n, m, ms);
+  launch_lcss_batch_gpu_wavefront_knn(t1.data(), t2.data(), out.data() + num_t, num_t, n, m, eps,
+                                      ms);
+  launch_frechet_batch_gpu_wavefront(t1.data(), t2.data(), out.data() + 2 * num_t, num_t, n, m,
+                                     ms);
+  run_hausdorff_rtree_gpu_pipeline(t1.data(), num_t, n, t2.data(), num_t, m,
+                                   out.data() + 3 * num_t);
+  FILE* g = std::fopen(argv[2], "wb");
+  if (!g || std::fwrite(out.data(), sizeof(float), out.size(), g) != out.size()) return 6;
+  std::fclose(g);
+  return 0;
+}
+"""
+
+
+@pytest.mark.gpu
+def test_cpp_caller_matches_reference_goldens_on_gpu(tsim, oracle, tmp_path):
+    """A C++ caller written against the reference-named headers
+    (include/compat/), compiled with g++ and linked against libtsim.so, runs
+    on the GPU on the golden inputs: DTW, LCSS and Frechet are bit-exact
+    against the reference's own CPU outputs (CudaRuntime1/dtw.cpp, lcss.cpp,
+    frechet.cpp, compiled into the fixture), Hausdorff against the oracle's
+    restatement of the reference's candidate loop over the same bounding-box
+    candidates -- the relink path a reference user takes."""
+    import shutil
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    libdir = os.path.dirname(tsim._lib.lib_path())
+    inc = os.path.join(ROOT, "include")
+    (tmp_path / "gold.cpp").write_text(CPP_GOLDEN_CALLER)
+    exe = str(tmp_path / "gold_caller")
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I" + os.path.join(inc, "compat"),
+                        "-I/usr/local/cuda/include", str(tmp_path / "gold.cpp"), "-o", exe,
+                        "-L" + libdir, "-ltsim", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    z = np.load(os.path.join(ROOT, "tests", "golden", "ref_batch.npz"))
+    for ci in range(int(z["ncases"][0])):
+        num_t, n, m = (int(v) for v in z[f"c{ci}_meta"])
+        eps = np.float32(z[f"c{ci}_eps"][0])
+        t1 = np.ascontiguousarray(z[f"c{ci}_t1"], np.float32)
+        t2 = np.ascontiguousarray(z[f"c{ci}_t2"], np.float32)
+        inp = tmp_path / f"in{ci}.bin"
+        inp.write_bytes(np.array([num_t, n, m], np.int32).tobytes() + eps.tobytes() +
+                        t1.tobytes() + t2.tobytes())
+        outp = tmp_path / f"out{ci}.bin"
+        res = subprocess.run([exe, str(inp), str(outp)], capture_output=True, text=True,
+                             timeout=300)
+        assert res.returncode == 0, (ci, res.stdout, res.stderr)
+        got = np.fromfile(outp, np.float32).reshape(4, num_t)
+        for row, meas in enumerate(("dtw", "lcss", "frechet")):
+            want = z[f"c{ci}_{meas}"]
+            assert np.array_equal(got[row].view(np.uint32), want.view(np.uint32)), (ci, meas)
+        cand = oracle.mbr_knn(t1, n, t2, m, 10)
+        want_h = oracle.ref_hausdorff_cands(t1, n, t2, m, cand)
+        assert np.array_equal(got[3].view(np.uint32), want_h.view(np.uint32)), (ci, "hausdorff")

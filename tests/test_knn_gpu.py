@@ -346,3 +346,33 @@ def test_frechet_fp64_window_and_tiny_values(tsim, cuda_ctx, oracle):
         assert np.array_equal(ids, want_ids)
         assert np.array_equal(d64, want_d)
     db.close()
+
+
+@pytest.mark.parametrize("pruned", [False, True])
+def test_plain_small_workload_full_size(tsim, cuda_ctx, oracle, pruned):
+    """The small plain workload at its own size: 8 queries x 1,024 candidates,
+    every trajectory 128 points (N(0,1) random walks), all five measures with
+    the full DP (no band, no LCSS window), top-10 -- ids bit-exact against
+    the FP64 brute-force oracle, LCSS counts exact, distances within 1e-5."""
+    from cudaruntime1_gb300 import datagen as G
+    cp, co = G.random_walks(1024, 128, 11 + 3)
+    qp, qo = G.random_walks(8, 128, 11 + 4)
+    db = tsim.Database(cuda_ctx, cp, co)
+    runs = [("dtw", dict(band_pct=-1, cost=0)), ("lcss", dict(epsilon=0.5, delta=-1)),
+            ("frechet", {}), ("hausdorff", {}), ("euclidean", {})]
+    for measure, kw in runs:
+        okw = dict(kw)
+        if "epsilon" in okw:
+            okw["eps"] = okw.pop("epsilon")
+        want_ids, want_d = oracle.knn(measure, qp, qo, cp, co, 10, **okw)
+        if pruned:
+            kw = dict(kw, flags=tsim.api.FLAG_ALWAYS_PRUNE)
+        ids, d, d64, st = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 10, **kw)
+        assert np.array_equal(ids, want_ids), measure
+        if measure == "lcss":
+            assert np.array_equal(d.astype(np.float64), want_d)
+        else:
+            rel = np.abs(d.astype(np.float64) - want_d) / np.maximum(want_d, 1e-30)
+            assert rel.max() <= REL_TOL, (measure, rel.max())
+        assert st["pairs"] == 8 * 1024
+    db.close()

@@ -121,3 +121,35 @@ def test_knn_ties_break_by_index(oracle):
     ids, d = oracle.knn("dtw", q, np.array([0, 30]), db, doff, 4)
     assert list(ids[0]) == [1, 2, 0, 3]
     assert d[0][0] == d[0][1] == 0.0 and d[0][2] == d[0][3]
+
+
+@pytest.mark.parametrize("measure,kw", [
+    ("dtw", dict(band_pct=10)), ("dtw", dict(band_pct=-1, cost=1)),
+    ("lcss", dict(eps=0.5, delta=5)), ("lcss", dict(eps=1.0)),
+    ("frechet", {}), ("hausdorff", {}), ("euclidean", {})])
+def test_pruned_knn_equals_brute_force(oracle, measure, kw):
+    """The pruned exact kNN that checks parity against large databases gives
+    the brute force's ids and values, ties and infinite values included."""
+    ql = G.uniform_lengths(7, 10, 70, 21)
+    cl = G.uniform_lengths(400, 10, 70, 22)
+    qp, qo = G.random_walks(7, ql, 23, start_range=30.0)
+    cp, co = G.random_walks(400, cl, 24, start_range=30.0)
+    # duplicates of the first candidates (index ties) and a copy of query 0
+    # (distance 0 / a full LCSS count)
+    dup = cp[co[0]:co[3]]
+    q0 = qp[qo[0]:qo[1]]
+    cp = np.concatenate([cp, dup, dup, q0])
+    co = np.concatenate([co, co[-1] + np.cumsum(np.diff(co[:4])),
+                         co[-1] + co[3] + np.cumsum(np.diff(co[:4])),
+                         [co[-1] + 2 * co[3] + len(q0)]]).astype(np.int64)
+    for k in (1, 8):
+        ids_b, d_b = oracle.knn(measure, qp, qo, cp, co, k, **kw)
+        ids_p, d_p, ev = oracle.knn_pruned(measure, qp, qo, cp, co, k, evaluated=True, **kw)
+        assert np.array_equal(ids_b, ids_p), (measure, k)
+        assert np.array_equal(d_b, d_p), (measure, k)
+        assert ev <= len(qo[:-1]) * (len(co) - 1)
+    if measure == "euclidean":  # many candidates longer than the queries: +inf
+        assert np.isinf(oracle.knn(measure, qp, qo, cp, co, 300)[1]).any()
+        ids_b, d_b = oracle.knn(measure, qp, qo, cp, co, 300)
+        ids_p, d_p = oracle.knn_pruned(measure, qp, qo, cp, co, 300)
+        assert np.array_equal(ids_b, ids_p) and np.array_equal(d_b, d_p)
