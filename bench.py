@@ -171,29 +171,44 @@ def dp_saturated(ctx, T, api, qpt, qot, maxq, cp, co, w, fp32_peak, stream, reps
     cells = api.band_cells(ctx, db2, qpt.data_ptr(), qot.data_ptr(), nq, "dtw", **kw)
     db2.close()
 
-    def call():
-        api.dp_pairs(ctx, "dtw", 0, 0, qpt.data_ptr(), qot.data_ptr(), maxq, cpt.data_ptr(),
-                     cot.data_ptr(), maxc, pairs.data_ptr(), npairs, out.data_ptr(), 0, **kw)
+    def timed(kernel):
+        def call():
+            api.dp_pairs(ctx, "dtw", 0, kernel, qpt.data_ptr(), qot.data_ptr(), maxq,
+                         cpt.data_ptr(), cot.data_ptr(), maxc, pairs.data_ptr(), npairs,
+                         out.data_ptr(), 0, **kw)
 
-    call()
-    torch.cuda.synchronize()
-    ctx.counters(reset=True)
-    ms = []
-    for _ in range(reps):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
         call()
-        b.record(stream)
         torch.cuda.synchronize()
-        ms.append(a.elapsed_time(b))
-    launches = ctx.counters(reset=True)["launches"] / reps
-    t = statistics.median(ms)
+        ctx.counters(reset=True)
+        ms = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            call()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        launches = ctx.counters(reset=True)["launches"] / reps
+        return statistics.median(ms), ms, launches, out.cpu().numpy().copy()
+
+    by_kernel, vals = {}, {}
+    for name, kernel in (("warp_per_pair", 2), ("lane_per_pair", 5)):
+        t, ms, launches, v = timed(kernel)
+        vals[name] = v
+        by_kernel[name] = {"ms": t, "ms_all": ms, "gcups": cells / (t * 1e6),
+                           "launches_per_call": launches,
+                           "frac": cells * DP_FLOPS_PER_CELL / (t * 1e-3) / 1e12 / fp32_peak
+                           if fp32_peak else None}
+    best = min(by_kernel, key=lambda k: by_kernel[k]["ms"])
+    t = by_kernel[best]["ms"]
     tflops = cells * DP_FLOPS_PER_CELL / (t * 1e-3) / 1e12
-    return {"pairs": npairs, "band_cells": int(cells), "ms": t, "ms_all": ms,
+    return {"pairs": npairs, "band_cells": int(cells), "kernel": best, "ms": t,
             "gcups": cells / (t * 1e6), "achieved": tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-            "frac": tflops / fp32_peak if fp32_peak else None, "launches_per_call": launches,
+            "frac": tflops / fp32_peak if fp32_peak else None, "by_kernel": by_kernel,
+            "values_bit_identical_across_kernels": bool(np.array_equal(
+                vals["warp_per_pair"].view(np.uint32), vals["lane_per_pair"].view(np.uint32))),
             "what": f"{nq} queries x first {nc} candidates of the workload, FP32 DTW band "
-                    f"{w['band_pct']}%, no threshold, tsim_dp_pairs (automatic kernel), "
+                    f"{w['band_pct']}%, no threshold, tsim_dp_pairs per kernel, "
                     f"median of {reps} calls"}
 
 

@@ -23,6 +23,7 @@ TSIM_ERR_BUDGET, TSIM_PENDING, TSIM_ERR_BUSY = 6, 7, 8
 DTW, LCSS, FRECHET, HAUSDORFF, EUCLIDEAN = range(5)
 COST_SQEUCLID, COST_EUCLID = 0, 1
 FLAG_NO_PRUNE, FLAG_PLAIN, FLAG_NO_GRAPH, FLAG_FP64_RESCORE, FLAG_ALWAYS_PRUNE = 1, 2, 4, 8, 16
+FLAG_NO_LANE_DP, FLAG_NO_WAVE_DP = 32, 64
 STAGES = ["summary", "lb1", "seed", "filter", "dp", "select", "rescore", "ref", "dp_survivors"]
 
 _vp = C.c_void_p
@@ -133,6 +134,8 @@ def load(build_if_missing: bool = False):
             "tsim_ctx_counters": ([_vp, C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int], C.c_int),
             "tsim_probe_fp32_tflops": ([_vp, C.POINTER(C.c_double)], C.c_int),
+            "tsim_debug_fail_allocations": ([C.c_int, C.c_int], C.c_int),
+            "tsim_debug_set_canary": ([C.c_int], C.c_int),
             "tsim_ctx_set_concurrency": ([_vp, C.c_int], C.c_int),
             "tsim_ctx_survivor_cells": ([_vp, C.POINTER(C.c_int64)], C.c_int),
             "tsim_band_cells": ([_vp, C.POINTER(TsimParams), _vp, _vp, C.c_int, _vp,

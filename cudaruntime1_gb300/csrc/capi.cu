@@ -1,5 +1,6 @@
 // capi.cu -- context, scratch arena, device-resident database and status
 // reporting of the C ABI (include/tsim.h).
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -27,9 +28,43 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
   return e == cudaErrorMemoryAllocation ? TSIM_ERR_OUT_OF_MEMORY : TSIM_ERR_CUDA;
 }
 
+// Allocation-failure injection (tsim_debug_fail_allocations): after `skip`
+// more allocations succeed, the next `count` fail as out of memory.
+std::atomic<long long> g_fail_skip{0};
+std::atomic<long long> g_fail_count{0};
+std::atomic<int> g_canary{0};
+
+static bool injected_failure() {
+  if (g_fail_count.load() <= 0) return false;
+  if (g_fail_skip.fetch_sub(1) > 0) return false;
+  return g_fail_count.fetch_sub(1) > 0;
+}
+
+cudaError_t dev_malloc(void** p, size_t bytes) {
+  if (injected_failure()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
+
+cudaError_t host_alloc(void** p, size_t bytes) {
+  if (injected_failure()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+}
+
+bool debug_canary() { return g_canary.load() != 0; }
+
 int arena_reserve(tsim_ctx* ctx, size_t bytes) {
   ctx->arena_used = 0;
-  if (bytes <= ctx->arena_cap) return TSIM_OK;
+  if (bytes <= ctx->arena_cap) {
+    if (debug_canary() && bytes)
+      TSIM_CUDA(cudaMemsetAsync(ctx->arena, 0xff, bytes, ctx->stream));
+    return TSIM_OK;
+  }
   if (ctx->arena_external)  // a block lent by a server: it never grows
     return fail(TSIM_ERR_BUDGET, "request needs more scratch than it was admitted with");
   size_t cap = std::max(bytes + bytes / 4, size_t(1) << 20);
@@ -39,9 +74,10 @@ int arena_reserve(tsim_ctx* ctx, size_t bytes) {
     ctx->arena = nullptr;
     ctx->arena_cap = 0;
   }
-  TSIM_CUDA(cudaMalloc(&ctx->arena, cap));
+  TSIM_CUDA(dev_malloc(reinterpret_cast<void**>(&ctx->arena), cap));
   ctx->arena_cap = cap;
   ctx->arena_gen++;  // graphs captured over the old arena are stale
+  if (debug_canary()) TSIM_CUDA(cudaMemsetAsync(ctx->arena, 0xff, bytes, ctx->stream));
   return TSIM_OK;
 }
 
@@ -54,7 +90,7 @@ int pinned_reserve(tsim_ctx* ctx, size_t bytes) {
     ctx->pinned = nullptr;
     ctx->pinned_cap = 0;
   }
-  TSIM_CUDA(cudaMallocHost(&ctx->pinned, cap));
+  TSIM_CUDA(host_alloc(&ctx->pinned, cap));
   ctx->pinned_cap = cap;
   return TSIM_OK;
 }
@@ -304,6 +340,19 @@ extern "C" int tsim_ctx_survivor_cells(tsim_ctx* ctx, int64_t* cells) {
   return TSIM_OK;
 }
 
+extern "C" int tsim_debug_fail_allocations(int skip, int count) {
+  TSIM_CHECK_ARG(skip >= 0 && count >= 0, "skip and count must be >= 0");
+  tsim::g_fail_count.store(0);  // disarmed while the new values go in
+  tsim::g_fail_skip.store(skip);
+  tsim::g_fail_count.store(count);
+  return TSIM_OK;
+}
+
+extern "C" int tsim_debug_set_canary(int on) {
+  tsim::g_canary.store(on ? 1 : 0);
+  return TSIM_OK;
+}
+
 extern "C" int tsim_probe_fp32_tflops(tsim_ctx* ctx, double* tflops) {
   TSIM_CHECK_ARG(ctx && tflops, "NULL argument");
   TSIM_CUDA(cudaSetDevice(ctx->device));
@@ -371,7 +420,7 @@ int tsim_ctx_create(int device, void* stream, tsim_ctx** out) {
   }
   cudaEventCreate(&c->ev0);
   cudaEventCreate(&c->ev1);
-  e = cudaMalloc(&c->dcounters, 64 * sizeof(unsigned long long));
+  e = dev_malloc(reinterpret_cast<void**>(&c->dcounters), 64 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(c->dcounters, 0, 64 * sizeof(unsigned long long));
   if (e != cudaSuccess) {
     if (c->owns_stream) cudaStreamDestroy(c->stream);
@@ -437,11 +486,11 @@ int tsim_ctx_synchronize(tsim_ctx* c) {
 int64_t tsim_ctx_scratch_bytes(const tsim_ctx* c) { return c ? (int64_t)c->arena_cap : 0; }
 
 static int db_alloc(tsim_db* db) {
-  TSIM_CUDA(cudaMalloc(&db->segbox, sizeof(float4) * kSegs * std::max(db->count, 1)));
-  TSIM_CUDA(cudaMalloc(&db->segsum, sizeof(float2) * kSegs * std::max(db->count, 1)));
-  TSIM_CUDA(cudaMalloc(&db->box, sizeof(float4) * std::max(db->count, 1)));
-  TSIM_CUDA(cudaMalloc(&db->ends, sizeof(float4) * std::max(db->count, 1)));
-  TSIM_CUDA(cudaMalloc(&db->len, sizeof(int) * std::max(db->count, 1)));
+  TSIM_CUDA(dev_malloc(reinterpret_cast<void**>(&db->segbox), sizeof(float4) * kSegs * std::max(db->count, 1)));
+  TSIM_CUDA(dev_malloc(reinterpret_cast<void**>(&db->segsum), sizeof(float2) * kSegs * std::max(db->count, 1)));
+  TSIM_CUDA(dev_malloc(reinterpret_cast<void**>(&db->box), sizeof(float4) * std::max(db->count, 1)));
+  TSIM_CUDA(dev_malloc(reinterpret_cast<void**>(&db->ends), sizeof(float4) * std::max(db->count, 1)));
+  TSIM_CUDA(dev_malloc(reinterpret_cast<void**>(&db->len), sizeof(int) * std::max(db->count, 1)));
   return TSIM_OK;
 }
 
@@ -484,8 +533,10 @@ int tsim_db_create(tsim_ctx* ctx, const tsim_point* h_pts, const int64_t* h_off,
   db->owns = true;
   db->h_off.assign(h_off, h_off + count + 1);
   int s = TSIM_OK;
-  cudaError_t e = cudaMalloc(&db->pts, sizeof(float2) * std::max<int64_t>(db->total, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&db->off, sizeof(int64_t) * (count + 1));
+  cudaError_t e = dev_malloc(reinterpret_cast<void**>(&db->pts),
+                             sizeof(float2) * std::max<int64_t>(db->total, 1));
+  if (e == cudaSuccess)
+    e = dev_malloc(reinterpret_cast<void**>(&db->off), sizeof(int64_t) * (count + 1));
   if (e == cudaSuccess && db->total > 0)
     e = cudaMemcpyAsync(db->pts, h_pts, sizeof(float2) * db->total, cudaMemcpyHostToDevice,
                         ctx->stream);

@@ -44,7 +44,7 @@ bool ensure(DevBuf& b, size_t bytes) {
   b.p = nullptr;
   b.cap = 0;
   size_t cap = bytes + bytes / 8 + 256;
-  if (cudaMalloc(&b.p, cap) != cudaSuccess) {
+  if (tsim::dev_malloc(reinterpret_cast<void**>(&b.p), cap) != cudaSuccess) {
     tsim::set_error("cudaMalloc of compat buffer failed");
     return false;
   }

@@ -214,14 +214,14 @@ extern "C" int tsim_db_load(tsim_ctx* ctx, const char* path, tsim_db** out) {
   db->h_off = std::move(off);
   char* pinned = nullptr;
   int st = TSIM_OK;
-  cudaError_t e = cudaMalloc(&db->pts, sizeof(float2) * std::max<int64_t>(db->total, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&db->off, sizeof(int64_t) * (n + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&db->segbox, sizeof(float4) * kSegs * std::max<size_t>(n, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&db->segsum, sizeof(float2) * kSegs * std::max<size_t>(n, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&db->box, sizeof(float4) * std::max<size_t>(n, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&db->ends, sizeof(float4) * std::max<size_t>(n, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&db->len, sizeof(int) * std::max<size_t>(n, 1));
-  if (e == cudaSuccess) e = cudaHostAlloc((void**)&pinned, kChunkBytes, cudaHostAllocDefault);
+  cudaError_t e = dev_malloc(reinterpret_cast<void**>(&db->pts), sizeof(float2) * std::max<int64_t>(db->total, 1));
+  if (e == cudaSuccess) e = dev_malloc(reinterpret_cast<void**>(&db->off), sizeof(int64_t) * (n + 1));
+  if (e == cudaSuccess) e = dev_malloc(reinterpret_cast<void**>(&db->segbox), sizeof(float4) * kSegs * std::max<size_t>(n, 1));
+  if (e == cudaSuccess) e = dev_malloc(reinterpret_cast<void**>(&db->segsum), sizeof(float2) * kSegs * std::max<size_t>(n, 1));
+  if (e == cudaSuccess) e = dev_malloc(reinterpret_cast<void**>(&db->box), sizeof(float4) * std::max<size_t>(n, 1));
+  if (e == cudaSuccess) e = dev_malloc(reinterpret_cast<void**>(&db->ends), sizeof(float4) * std::max<size_t>(n, 1));
+  if (e == cudaSuccess) e = dev_malloc(reinterpret_cast<void**>(&db->len), sizeof(int) * std::max<size_t>(n, 1));
+  if (e == cudaSuccess) e = host_alloc((void**)&pinned, kChunkBytes);
   if (e != cudaSuccess) st = cuda_fail(e, "tsim_db_load allocation", __FILE__, __LINE__);
   if (st == TSIM_OK) {
     e = cudaMemcpyAsync(db->off, db->h_off.data(), sizeof(int64_t) * (n + 1),

@@ -29,7 +29,10 @@ __device__ __forceinline__ df df_min3(df a, df b, df c) {
 
 // ---- cell policies ---------------------------------------------------------
 // V: value type; border(): value outside the matrix / band; origin(): D(-1,-1);
-// masked(left): value of a cell outside its row's band.
+// masked(left): value of a cell outside its row's band.  The minimum
+// policies also split a cell into cost() and combine(cost, m), m the minimum
+// of up, left and diagonal: cell() == combine(cost(), min3(...)), operation
+// for operation (the band-relative kernel computes costs a step ahead).
 
 struct PolDtwRef {  // CudaRuntime1/dtw.cpp:88-93 arithmetic, bit for bit
   using V = float;
@@ -59,10 +62,16 @@ struct PolFrechetRef {  // CudaRuntime1/frechet.cpp:72-76, 103-108
 
 struct PolDtwSq {  // squared cost; FMA allowed, error bounded by the caller
   using V = float;
+  using C = float;
   static constexpr bool kMin = true;
   __device__ static V border() { return TSIM_INF; }
   __device__ static V origin() { return 0.0f; }
   __device__ static V masked(V) { return TSIM_INF; }
+  __device__ static C cost(float qx, float qy, float cx, float cy) {
+    float dx = qx - cx, dy = qy - cy;
+    return fmaf(dy, dy, dx * dx);
+  }
+  __device__ static V combine(C c, V m) { return c + m; }
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     float dx = qx - cx, dy = qy - cy;
     float c = fmaf(dy, dy, dx * dx);
@@ -72,10 +81,16 @@ struct PolDtwSq {  // squared cost; FMA allowed, error bounded by the caller
 
 struct PolDtwEu {
   using V = float;
+  using C = float;
   static constexpr bool kMin = true;
   __device__ static V border() { return TSIM_INF; }
   __device__ static V origin() { return 0.0f; }
   __device__ static V masked(V) { return TSIM_INF; }
+  __device__ static C cost(float qx, float qy, float cx, float cy) {
+    float dx = qx - cx, dy = qy - cy;
+    return sqrtf(fmaf(dy, dy, dx * dx));
+  }
+  __device__ static V combine(C c, V m) { return c + m; }
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     float dx = qx - cx, dy = qy - cy;
     float c = sqrtf(fmaf(dy, dy, dx * dx));
@@ -85,10 +100,16 @@ struct PolDtwEu {
 
 struct PolFrechetSq {  // squared domain; sqrt is applied once at the end
   using V = float;
+  using C = float;
   static constexpr bool kMin = true;
   __device__ static V border() { return TSIM_INF; }
   __device__ static V origin() { return 0.0f; }
   __device__ static V masked(V) { return TSIM_INF; }
+  __device__ static C cost(float qx, float qy, float cx, float cy) {
+    float dx = qx - cx, dy = qy - cy;
+    return fmaf(dy, dy, dx * dx);
+  }
+  __device__ static V combine(C c, V m) { return fmaxf(c, m); }
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     float dx = qx - cx, dy = qy - cy;
     float d2 = fmaf(dy, dy, dx * dx);
@@ -183,10 +204,16 @@ struct PolFrechetWin {
 // cost's rounding, not P of them.
 struct PolDtwSqC {
   using V = df;
+  using C = float;
   static constexpr bool kMin = true;
   __device__ static V border() { return df_inf(); }
   __device__ static V origin() { return df{0.0f, 0.0f}; }
   __device__ static V masked(V) { return df_inf(); }
+  __device__ static C cost(float qx, float qy, float cx, float cy) {
+    const float dx = qx - cx, dy = qy - cy;
+    return fmaf(dy, dy, dx * dx);
+  }
+  __device__ static V combine(C c, V m) { return m.hi < TSIM_INF ? df_add1(c, m) : df_inf(); }
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     const df m = df_min3(up, lf, dg);
     if (!(m.hi < TSIM_INF)) return df_inf();
@@ -197,10 +224,16 @@ struct PolDtwSqC {
 
 struct PolDtwEuC {
   using V = df;
+  using C = float;
   static constexpr bool kMin = true;
   __device__ static V border() { return df_inf(); }
   __device__ static V origin() { return df{0.0f, 0.0f}; }
   __device__ static V masked(V) { return df_inf(); }
+  __device__ static C cost(float qx, float qy, float cx, float cy) {
+    const float dx = qx - cx, dy = qy - cy;
+    return sqrtf(fmaf(dy, dy, dx * dx));
+  }
+  __device__ static V combine(C c, V m) { return m.hi < TSIM_INF ? df_add1(c, m) : df_inf(); }
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     const df m = df_min3(up, lf, dg);
     if (!(m.hi < TSIM_INF)) return df_inf();
@@ -211,10 +244,13 @@ struct PolDtwEuC {
 
 struct PolFrechetSqC {
   using V = df;
+  using C = df;
   static constexpr bool kMin = true;
   __device__ static V border() { return df_inf(); }
   __device__ static V origin() { return df{0.0f, 0.0f}; }
   __device__ static V masked(V) { return df_inf(); }
+  __device__ static C cost(float qx, float qy, float cx, float cy) { return df_sqdist(qx, qy, cx, cy); }
+  __device__ static V combine(C c, V m) { return df_max(c, m); }
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float) {
     return df_max(df_sqdist(qx, qy, cx, cy), df_min3(up, lf, dg));
   }

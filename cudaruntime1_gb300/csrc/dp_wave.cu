@@ -1,0 +1,328 @@
+// dp_wave.cu -- band-relative anti-diagonal DP for DTW and discrete Frechet:
+// a warp per (query, candidate) pair, lane p holding the p-th live cell of
+// the current anti-diagonal (R cells per lane for anti-diagonals of up to
+// 32 R live cells).  The latency form of the DP: a round of few pairs lasts
+// as long as its longest pair, whose n+m-1 anti-diagonals are its steps.
+//
+// Anti-diagonal t = i + j holds the band's cells i in [ilo(t), ihi(t)]
+// (|i(m-1) - j(n-1)| <= W inside the matrix), L(t) of them.  From one
+// anti-diagonal to the next ilo advances by s = 0 or 1, the same for the
+// whole pair.  Position q of step t is cell (ilo(t) + q, t - ilo(t) - q);
+// with s = 0 it moves one column right, with s = 1 one row down:
+//   s = 0:  up = position q-1, left = position q,    diag = left of q-1
+//   s = 1:  up = position q,   left = position q+1,  diag = left of q
+// With M_q = min(V_q, the left value V_q was computed from), a cell is
+//   s = 0:  combine(cost, min(M_{q-1}, V_q)),   s = 1:  combine(cost, min(M_q, V_{q+1}))
+// -- min(M, V) is the minimum of up, left and diagonal, exact in any order,
+// so values are the same bits as the other DP kernels'.  One shuffle per
+// step moves the neighbour across lanes: M from the lane above when s = 0,
+// V from the lane below when s = 1.  Positions at or past L(t) hold +inf.
+//
+// Edges: above position 0 lies row ilo(t) - 1, outside the band on
+// anti-diagonal t; its left neighbour (position 0's diagonal when s = 0) is
+// inside when the previous step had s = 1, and is then position 0's value
+// two steps back, which lane 0 keeps.  Below the last position lies +inf.
+//
+// Per step a lane does: one shuffle, R cells, and the costs of the next
+// step's R cells from the pair's points staged in shared memory (padded so
+// that positions past L read inside the buffers and are masked).  The
+// geometry (ilo, L) of every anti-diagonal is a table built per pair from
+// exact integer ramps.  Steps run in straight-line blocks of 16.  Early
+// abandon: every warping path crosses one of any two consecutive
+// anti-diagonals and values never decrease along a path, so after every
+// block the minimum over its last two anti-diagonals is compared with the
+// query's threshold.
+//
+// Reference kernels replaced: dtw_refine_kernel (CudaRuntime1/dtw.cu:41-96)
+// and frechet_refine_kernel_m (CudaRuntime1/frechet.cu:44-117): a CTA per
+// pair, a full anti-diagonal of threads and two barriers per step.
+#include <vector>
+
+#include "dp_policies.cuh"
+
+namespace tsim {
+namespace {
+using namespace dp;
+
+constexpr int kWaveThreads = 128;
+constexpr int kWavePad = 64;  // points staged past the ends (positions beyond L read them)
+constexpr int kWaveMaxLen = 2048;  // longest trajectory staged in shared memory
+
+template <class V>
+__device__ __forceinline__ V vmin(V a, V b) {
+  return b < a ? b : a;
+}
+__device__ __forceinline__ float vmin(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ df vmin(df a, df b) { return df_min3(a, b, b); }
+
+__device__ __forceinline__ float wshfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ df wshfl(df v, int src) {
+  return df{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+// the most live cells any anti-diagonal of an n x m pair holds
+__host__ __device__ inline int wave_lmax(int n, int m, int w) {
+  const int mn = n < m ? n : m;
+  if (w < 0 || n < 2 || m < 2) return mn;
+  const long long W = (long long)w * (mn - 1);
+  const long long l = 2 * W / (n + m - 2) + 1;
+  return (int)(l < mn ? l : mn);
+}
+
+template <class P, int R>
+__global__ void __launch_bounds__(kWaveThreads)
+    dp_wave_kernel(DpArgs a, int qcap, int ccap, int tcap, int* spill, int* nspill) {
+  static_assert(P::kMin, "the band-relative kernel serves the minimum measures");
+  using V = typename P::V;
+  using C = typename P::C;
+  // per warp: query points (qcap + pad), candidate points (pad + ccap + pad),
+  // then ilo | L << 16 of every anti-diagonal (tcap)
+  extern __shared__ __align__(16) float2 wave_smem[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const size_t per_warp = (size_t)(qcap + kWavePad) + (ccap + 2 * kWavePad) + tcap / 2;
+  float2* qs = wave_smem + (size_t)warp * per_warp;
+  float2* cs = qs + qcap + kWavePad + kWavePad;  // cs[-kWavePad .. ccap + kWavePad)
+  int* tab = reinterpret_cast<int*>(cs + ccap + kWavePad);
+  const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nslots = (gridDim.x * blockDim.x) >> 5;
+  const int npairs = a.npairs_dev ? min(*a.npairs_dev, a.npairs) : a.npairs;
+  const bool check = a.thr != nullptr;
+  const int src_dn = (lane + 31) & 31, src_up = (lane + 1) & 31;
+
+  for (int wk = slot; wk < npairs; wk += nslots) {
+    const int pid = a.order ? a.order[wk] : wk;
+    const int2 pr = a.pairs[pid];
+    if (pr.y < 0) continue;
+    const int q = pr.x;
+    const int64_t qo = a.qoff[q], co = a.coff[pr.y];
+    const int n = (int)(a.qoff[q + 1] - qo), m = (int)(a.coff[pr.y + 1] - co);
+    const int w = band_w(n, m, a.band_pct);
+    const int t_end = n + m - 2;
+    if (n < 2 || m < 2 || n > qcap || m > ccap || t_end + 3 > tcap || wave_lmax(n, m, w) > 32 * R) {
+      if (lane == 0 && spill) spill[atomicAdd(nspill, 1)] = pid;
+      continue;
+    }
+    const float thr = check ? a.thr[q] : TSIM_INF;
+
+    // the pair's points, and the geometry of every anti-diagonal:
+    // ilo(t) = max(0, t-m+1, ceil((t(n-1) - W) / D)),
+    // ihi(t) = min(n-1, t, floor((t(n-1) + W) / D)),  D = n+m-2,
+    // stepped by 32 anti-diagonals per lane as quotient and remainder
+    __syncwarp();
+    {
+      const float2* A = a.qpts + qo;
+      const float2* B = a.cpts + co;
+      for (int i = lane; i < n; i += 32) qs[i] = __ldg(A + i);
+      for (int j = lane; j < m; j += 32) cs[j] = __ldg(B + j);
+      const int D = t_end;
+      const int W = w < 0 ? -1 : w * (min(n, m) - 1);
+      const int step = 32 * (n - 1), sq = step / D, sr = step % D;
+      // lo numerator shifted by K D (K D > W) to stay non-negative
+      const int K = W < 0 ? 0 : W / D + 1;
+      int lq = 0, lr = 0, hq = 0, hr = 0;
+      if (W >= 0 && lane <= t_end) {
+        const int xl = lane * (n - 1) - W + (D - 1) + K * D, xh = lane * (n - 1) + W;
+        lq = xl / D;
+        lr = xl % D;
+        hq = xh / D;
+        hr = xh % D;
+      }
+      for (int t = lane; t <= t_end; t += 32) {
+        int lo = max(0, t - (m - 1)), hi = min(n - 1, t);
+        if (W >= 0) {
+          lo = max(lo, lq - K);
+          hi = min(hi, hq);
+          lq += sq;
+          lr += sr;
+          if (lr >= D) lr -= D, ++lq;
+          hq += sq;
+          hr += sr;
+          if (hr >= D) hr -= D, ++hq;
+        }
+        tab[t] = lo | (max(0, hi - lo + 1) << 16);
+      }
+      // two entries past the last anti-diagonal: the step after it reads
+      // them (its cells are never used)
+      if (lane < 2) tab[t_end + 1 + lane] = (n - 1) | (1 << 16);
+    }
+    __syncwarp();
+
+    // step 0: cell (0, 0) at position 0; every other position outside
+    V v[R], mm[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = mm[r] = P::border();
+    if (lane == 0) {
+      const float2 p = qs[0], c = cs[0];
+      v[0] = P::cell(p.x, p.y, c.x, c.y, P::border(), P::border(), P::origin(), a.eps);
+      mm[0] = v[0];  // its left (0, -1) is outside
+    }
+    // costs of the cells of step tt (positions lane R + r), geometry lo
+    auto costs = [&](C* out, int tt, int lo) {
+      const int i0 = lo + lane * R, j0 = tt - lo - lane * R;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float2 qp = qs[i0 + r], cp = cs[j0 - r];
+        out[r] = P::cost(qp.x, qp.y, cp.x, cp.y);
+      }
+    };
+    C cst[R];
+    int e = tab[1];   // geometry of the step computed next
+    int e1 = tab[2];  // and of the one after (the table runs two entries past t_end)
+    costs(cst, 1, e & 0xffff);
+    V edge = P::border();  // lane 0: position 0's diagonal when the next shift is 0
+    int ilo = 0;
+    bool alive = true;
+    // one anti-diagonal: the shuffle, R cells, and the next step's costs
+    // (computed past the last step too: the padding keeps them in bounds)
+    auto step = [&](const int t) {
+      const int nlo = e & 0xffff, L = e >> 16;
+      const int s = nlo - ilo;  // 0 or 1, uniform
+      // across lanes: s = 0 takes M of the lane above's last position, s = 1
+      // V of the lane below's first position
+      const V xin = wshfl(s ? v[0] : mm[R - 1], s ? src_up : src_dn);
+      C cn[R];
+      costs(cn, t + 1, e1 & 0xffff);
+      const int e2 = tab[t + 2];
+      const V edge_next = s ? v[0] : P::border();
+      V nv[R], nm[R];  // every position reads the last step's values
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const V mdu0 = r > 0 ? mm[r > 0 ? r - 1 : 0] : (lane == 0 ? edge : xin);
+        const V lft1 = r + 1 < R ? v[r + 1 < R ? r + 1 : 0] : (lane == 31 ? P::border() : xin);
+        const V mdu = s ? mm[r] : mdu0;
+        const V lft = s ? lft1 : v[r];
+        const V c = P::combine(cst[r], vmin(mdu, lft));
+        const bool in = lane * R + r < L;
+        nv[r] = in ? c : P::border();
+        nm[r] = in ? vmin(c, lft) : P::border();
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        v[r] = nv[r];
+        mm[r] = nm[r];
+        cst[r] = cn[r];
+      }
+      edge = edge_next;
+      ilo = nlo;
+      e = e1;
+      e1 = e2;
+    };
+    auto lane_min = [&]() {
+      float x = vf(v[0]);
+#pragma unroll
+      for (int r = 1; r < R; ++r) x = fminf(x, vf(v[r]));
+      return x;
+    };
+    // blocks of 16 straight-line steps; after each, the abandon test over
+    // its last two anti-diagonals
+    int t = 1;
+    for (; t + 15 <= t_end; t += 16) {
+      float m14 = TSIM_INF;
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        step(t + u);
+        if (u == 14) m14 = lane_min();
+      }
+      if (check) {
+        const float two = fminf(lane_min(), m14);
+        const float lb = __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(two)));
+        if (lb > thr) {  // uniform across the warp
+          alive = false;
+          t += 15;
+          break;
+        }
+      }
+    }
+    if (alive)
+      for (; t <= t_end; ++t) step(t);
+    if (a.cells) {  // cells of the anti-diagonals computed, inside the band
+      const int t_done = alive ? t_end : min(t, t_end);
+      long long cells = 0;
+      for (int u = lane; u <= t_done; u += 32) cells += tab[u] >> 16;
+      for (int o = 16; o; o >>= 1) cells += __shfl_xor_sync(0xffffffffu, cells, o);
+      if (lane == 0) atomicAdd(a.cells, (unsigned long long)cells);
+    }
+    // the result: cell (n-1, m-1), position 0 of the last anti-diagonal
+    if (lane == 0) store_result(a, pid, alive ? v[0] : P::border());
+  }
+}
+
+template <class P, int R>
+int launch_wave_one(tsim_ctx* ctx, const DpArgs& a, int qcap, int ccap, int tcap, int* spill,
+                    int* nspill) {
+  if (a.npairs <= 0) return TSIM_OK;
+  auto kern = dp_wave_kernel<P, R>;
+  const size_t per_warp = (size_t)(qcap + kWavePad) + (ccap + 2 * kWavePad) + tcap / 2;
+  const size_t smem = (size_t)(kWaveThreads / 32) * per_warp * sizeof(float2);
+  if (smem > 48 * 1024)
+    TSIM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  TSIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWaveThreads, smem));
+  if (per_sm < 1) return fail(TSIM_ERR_UNSUPPORTED, "wave kernel does not fit on an SM");
+  const long long warps = kWaveThreads / 32;
+  const long long blocks = std::min<long long>((a.npairs + warps - 1) / warps,
+                                               (long long)per_sm * ctx->num_sms);
+  kern<<<(unsigned)std::max(blocks, 1ll), kWaveThreads, smem, ctx->stream>>>(a, qcap, ccap, tcap,
+                                                                             spill, nspill);
+  TSIM_CUDA(cudaGetLastError());
+  launched(ctx);
+  return TSIM_OK;
+}
+
+template <class P>
+int wave_chain(tsim_ctx* ctx, const DpArgs& a, int max_n, int max_m, int* spill, int* nspill,
+               int* tmp, int* ntmp) {
+  // passes R = 1, 2: each takes the pairs whose widest anti-diagonal fits
+  // 32 R lanes, the chain stopping at the first that takes every pair (the
+  // longest lengths give the widest band); pairs longer than the staging
+  // capacity or wider than 64 cells per anti-diagonal are left in spill
+  const int qcap = (std::min(max_n, kWaveMaxLen) + 1) & ~1;
+  const int ccap = (std::min(max_m, kWaveMaxLen) + 1) & ~1;
+  const int tcap = ((qcap + ccap + 2) / 2) * 2;  // n+m-1 anti-diagonals and two past them
+  const int lmax = wave_lmax(max_n, max_m, band_w(max_n, max_m, a.band_pct));
+  std::vector<int> rs;
+  for (int R = 1; R <= 2; R *= 2) {
+    rs.push_back(R);
+    if (lmax <= 32 * R) break;
+  }
+  const int np = (int)rs.size();
+  DpArgs in = a;
+  for (int p = 0; p < np; ++p) {
+    const bool to_spill = ((np - 1 - p) & 1) == 0;
+    int* out = to_spill ? spill : tmp;
+    int* nout = to_spill ? nspill : ntmp;
+    TSIM_CUDA(cudaMemsetAsync(nout, 0, sizeof(int), ctx->stream));
+    if (rs[p] == 1)
+      TSIM_TRY((launch_wave_one<P, 1>(ctx, in, qcap, ccap, tcap, out, nout)));
+    else
+      TSIM_TRY((launch_wave_one<P, 2>(ctx, in, qcap, ccap, tcap, out, nout)));
+    in.order = out;
+    in.npairs_dev = nout;
+  }
+  return TSIM_OK;
+}
+
+}  // namespace
+
+bool wave_kind(int kind) {
+  return kind == DP_DTW_SQ || kind == DP_DTW_EU || kind == DP_FRECHET_SQ || kind == DP_DTW_SQC ||
+         kind == DP_DTW_EUC || kind == DP_FRECHET_SQC;
+}
+
+int launch_dp_wave(tsim_ctx* ctx, int kind, const DpArgs& a, int max_n, int max_m, int* spill,
+                   int* nspill, int* tmp, int* ntmp) {
+  switch (kind) {
+    case DP_DTW_SQ: return wave_chain<PolDtwSq>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_EU: return wave_chain<PolDtwEu>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
+    case DP_FRECHET_SQ:
+      return wave_chain<PolFrechetSq>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_SQC: return wave_chain<PolDtwSqC>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_EUC: return wave_chain<PolDtwEuC>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
+    case DP_FRECHET_SQC:
+      return wave_chain<PolFrechetSqC>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
+  }
+  return fail(TSIM_ERR_UNSUPPORTED, "no band-relative kernel for this DP kind");
+}
+
+}  // namespace tsim

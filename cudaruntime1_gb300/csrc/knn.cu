@@ -114,6 +114,16 @@ struct KArgs {
   int* nspill;
   int* spill2;              // the list between passes of the anti-diagonal kernel
   int* nspill2;
+  int* lanes;               // what the lane-per-pair kernel leaves to the warp-per-pair ones
+  int* nlanes;
+  int lane_gate;            // survivor rounds of at least this many pairs run a lane per
+                            // pair (0: never)
+  int lane_ring;            // its ring size (64 or 128)
+  int* waves;               // what the band-relative kernel leaves to the row-group ones
+  int* nwaves;
+  int* waves2;              // the list between its two passes
+  int* nwaves2;
+  int wave;                 // DTW / Frechet rounds start on the band-relative kernel
   int rdiag;                // rows per lane-group of the anti-diagonal kernel (0: off)
   int rdiag_shape;          // the smallest R a warp per pair admits for the longest pair
   int rdiag_cta;            // the same for a CTA per pair (0: no R fits the longest pair)
@@ -1382,7 +1392,38 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
   const bool diag_kind = kind == DP_DTW_SQ || kind == DP_DTW_EU || kind == DP_LCSS ||
                          kind == DP_FRECHET_SQ || kind == DP_DTW_SQC || kind == DP_DTW_EUC ||
                          kind == DP_FRECHET_SQC;
+  if (!latency && a.lane_gate > 0 && lane_kind(kind)) {
+    // many pairs: a lane per pair, with a latency of one pair's cells but a
+    // few instructions per cell; the kernel itself passes a round of fewer
+    // than lane_gate pairs (a count only the device knows) on whole
+    TSIM_TRY(launch_dp_lane(ctx, kind, d, a.lane_ring, a.lanes, a.nlanes, a.lane_gate));
+    DpArgs rest = d;
+    rest.order = a.lanes;
+    rest.npairs_dev = a.nlanes;
+    KArgs b = a;
+    b.lane_gate = 0;
+    return run_dp(ctx, b, kind, G, R, rest, latency);
+  }
   if (!diag_kind || a.rdiag == 0) return launch_dp(ctx, kind, G, R, d, a.max_clen);
+  const bool twofloat_kind = kind == DP_DTW_SQC || kind == DP_DTW_EUC || kind == DP_FRECHET_SQC;
+  if (a.wave && latency && wave_kind(kind) && !twofloat_kind) {
+    // lanes along the anti-diagonal, straight-line blocks of 16 steps: the
+    // shortest FP32 step of the warp-per-pair forms (a lone 512 x 486 pair
+    // 83 us against 104 on two warps per pair; compensated pairs are faster
+    // on two warps, 131 against 203 us), for the latency rounds; the
+    // survivor round stays on the row-group kernel, whose abandon test adds
+    // the remaining columns' bound (without it the batched workload's round
+    // computed 62 M cells instead of 38 M, 0.57 against 0.20 ms); pairs with
+    // more than 64 cells per anti-diagonal go on to the row-group kernels
+    TSIM_TRY(launch_dp_wave(ctx, kind, d, d.max_n > 0 ? d.max_n : a.max_qlen, a.max_clen,
+                            a.waves, a.nwaves, a.waves2, a.nwaves2));
+    DpArgs rest = d;
+    rest.order = a.waves;
+    rest.npairs_dev = a.nwaves;
+    KArgs b = a;
+    b.wave = 0;
+    return run_dp(ctx, b, kind, G, R, rest, latency);
+  }
   const bool twofloat = kind == DP_DTW_SQC || kind == DP_DTW_EUC || kind == DP_FRECHET_SQC;
   // Latency rounds (few pairs, one wave) pick the kernel by the pair shape
   // (not by the throughput-tuned R): two warps per pair while 64 lanes need
@@ -1802,6 +1843,15 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
       }
     a.rdiag_shape = a.rdiag;
     if (a.plain || (p->flags & TSIM_FLAG_NO_PRUNE)) a.rdiag = 0;
+    // the lane-per-pair kernel for survivor rounds of many pairs (pruned and
+    // brute force): it wins once the round's total work, not its longest
+    // pair, sets the time
+    const int kind32 = p->measure == TSIM_LCSS ? DP_LCSS
+                       : p->measure == TSIM_FRECHET ? DP_FRECHET_SQ
+                       : p->cost ? DP_DTW_EU : DP_DTW_SQ;
+    a.lane_ring = lane_ring_for(kind32, n, m, p->measure == TSIM_DTW ? p->band_pct : -1, p->delta);
+    a.lane_gate = (a.plain || (p->flags & TSIM_FLAG_NO_LANE_DP)) ? 0 : lane_gate_for(kind32, n, m, p->band_pct, p->delta);
+    a.wave = (a.plain || (p->flags & TSIM_FLAG_NO_WAVE_DP)) ? 0 : 1;
   }
   a.cost = p->cost;
   a.band_pct = p->band_pct;
@@ -1828,7 +1878,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
                 align256(sizeof(float4) * (size_t)nq * a.tstride) +
                 align256(sizeof(double2) * (size_t)nq * (max_qlen + 1)) +
                 align256(sizeof(float4) * (size_t)nq * kQBlocks) +
-                2 * align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 2 * 256;
+                5 * align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 5 * 256;
   return need;
 }
 
@@ -1902,6 +1952,12 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.nspill = arena_take<int>(ctx, 4);
   a.spill2 = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
   a.nspill2 = arena_take<int>(ctx, 4);
+  a.lanes = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
+  a.nlanes = arena_take<int>(ctx, 4);
+  a.waves = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
+  a.nwaves = arena_take<int>(ctx, 4);
+  a.waves2 = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
+  a.nwaves2 = arena_take<int>(ctx, 4);
   a.csegbox = db->segbox;
   a.csegsum = db->segsum;
   a.order = arena_take<int>(ctx, nqC);
@@ -2171,7 +2227,7 @@ extern "C" int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
       ctx->hstage_cap = 0;
     }
     const size_t cap = std::max(in_bytes + out_bytes, size_t(1) << 20);
-    TSIM_CUDA(cudaMalloc(&ctx->hstage, cap));
+    TSIM_CUDA(tsim::dev_malloc(&ctx->hstage, cap));
     ctx->hstage_cap = cap;
   }
   char* hp = (char*)ctx->pinned;
@@ -2211,7 +2267,7 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   using namespace tsim;
   TSIM_CHECK_ARG(ctx && p && d_qpts && d_qoff && d_cpts && d_coff && d_pairs, "NULL argument");
   TSIM_CHECK_ARG(npairs >= 0 && max_qlen >= 1 && max_clen >= 1, "bad sizes");
-  TSIM_CHECK_ARG(precision >= 0 && precision <= 2 && kernel >= 0 && kernel <= 4, "bad mode");
+  TSIM_CHECK_ARG(precision >= 0 && precision <= 2 && kernel >= 0 && kernel <= 6, "bad mode");
   TSIM_CHECK_ARG(precision == 0 ? d_out32 != nullptr : d_out64 != nullptr, "NULL output");
   int kinds[3];
   if (p->measure == TSIM_DTW) {
@@ -2264,12 +2320,31 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   for (int R2 : {8, 4, 2, 1})  // R = 8 for a CTA only
     if ((R2 < 8 || kernel == 3) && diag_ok(p->measure == TSIM_LCSS, max_qlen, max_clen, wd, R2, lanes))
       Rc = R2;
-  TSIM_TRY(arena_reserve(ctx, 2 * align256(sizeof(int) * (size_t)npairs) + 512));
+  TSIM_TRY(arena_reserve(ctx, 4 * align256(sizeof(int) * (size_t)npairs) + 768 +
+                                  align256(sizeof(int) * (size_t)lane_sort_buckets())));
   int* spill = arena_take<int>(ctx, npairs);
   int* nspill = arena_take<int>(ctx, 4);
   int* tmp = arena_take<int>(ctx, npairs);
   int* ntmp = arena_take<int>(ctx, 4);
-  if (kernel >= 3)
+  int* rest = arena_take<int>(ctx, npairs);
+  int* nrest = arena_take<int>(ctx, 4);
+  int* sorted = arena_take<int>(ctx, npairs);
+  int* buckets = arena_take<int>(ctx, lane_sort_buckets());
+  if (kernel == 6 && wave_kind(kind)) {  // band-relative first; wider pairs on the others
+    TSIM_TRY(launch_dp_wave(ctx, kind, d, max_qlen, max_clen, rest, nrest, sorted, buckets));
+    d.order = rest;
+    d.npairs_dev = nrest;
+  } else if (kernel == 5 && lane_kind(kind)) {  // a lane per pair first; wider pairs on a warp
+    // neighbouring lanes get pairs of one shape
+    TSIM_TRY(lane_sort(ctx, d, sorted, buckets));
+    d.order = sorted;
+    TSIM_TRY(launch_dp_lane(ctx, kind, d,
+                            lane_ring_for(kind, max_qlen, max_clen, d.band_pct, d.delta), rest,
+                            nrest));
+    d.order = rest;
+    d.npairs_dev = nrest;
+  }
+  if (kernel == 3 || kernel == 4)
     TSIM_TRY(launch_dp_diag(ctx, kind, Rc, d, max_clen, spill, nspill, tmp, ntmp,
                             kernel == 3 ? 8 : 2));
   else

@@ -16,78 +16,78 @@ __device__ __forceinline__ float d2_exact(float ax, float ay, float bx, float by
 namespace {
 
 constexpr int kHdThreads = 256;
-constexpr int kHdA = 4;  // source points per thread per pass
 
-// max over a in S of min over b in T of |a-b|^2, S and T in shared memory.
-// Stops early once the running max reaches `stop` (the pair cannot win).
-__device__ float directed_max_min(const float2* S, int ns, const float2* T, int nt, float seed,
-                                  const unsigned* best_bits, float* red) {
-  float run = seed;
-  for (int base = 0; base < ns; base += kHdThreads * kHdA) {
-    float ax[kHdA], ay[kHdA], mn[kHdA];
-#pragma unroll
-    for (int u = 0; u < kHdA; ++u) {
-      int i = base + u * kHdThreads + threadIdx.x;
-      float2 p = i < ns ? S[i] : S[0];
-      ax[u] = p.x;
-      ay[u] = p.y;
-      mn[u] = TSIM_INF;
+// max over a in S of min over b in T of |a-b|^2, S and T in shared memory,
+// every thread of the CTA busy: with ns < kHdThreads sources, P threads
+// (P = ns rounded up to a power of two, at least a warp) take the sources
+// and the kHdThreads / P groups split the targets, their minima meeting in
+// shared memory (red: kHdThreads floats).  Minimum and maximum are exact in
+// any order, so the value is the sequential loop's.
+__device__ float directed_max_min(const float2* S, int ns, const float2* T, int nt, float* red) {
+  int P = 32;
+  while (P < ns && P < kHdThreads) P <<= 1;
+  const int G = kHdThreads / P;  // target groups
+  const int g = threadIdx.x / P, il = threadIdx.x % P;
+  float run = 0.0f;
+  for (int base = 0; base < ns; base += P) {
+    const int i = base + il;
+    const float2 a = S[i < ns ? i : 0];
+    float mn = TSIM_INF;
+    int j = g;
+    for (; j + 3 * G < nt; j += 4 * G) {  // four independent targets per iteration
+      const float2 b0 = T[j], b1 = T[j + G], b2 = T[j + 2 * G], b3 = T[j + 3 * G];
+      mn = fminf(mn, fminf(fminf(d2_exact(a.x, a.y, b0.x, b0.y), d2_exact(a.x, a.y, b1.x, b1.y)),
+                           fminf(d2_exact(a.x, a.y, b2.x, b2.y), d2_exact(a.x, a.y, b3.x, b3.y))));
     }
-    for (int j = 0; j < nt; ++j) {
-      const float2 b = T[j];
-#pragma unroll
-      for (int u = 0; u < kHdA; ++u) mn[u] = fminf(mn[u], d2_exact(ax[u], ay[u], b.x, b.y));
-    }
+    for (; j < nt; j += G) mn = fminf(mn, d2_exact(a.x, a.y, T[j].x, T[j].y));
+    red[threadIdx.x] = mn;
+    __syncthreads();
     float loc = 0.0f;
-#pragma unroll
-    for (int u = 0; u < kHdA; ++u)
-      if (base + u * kHdThreads + threadIdx.x < ns) loc = fmaxf(loc, mn[u]);
+    if (threadIdx.x < P && base + (int)threadIdx.x < ns) {
+      float m2 = red[threadIdx.x];
+      for (int h = 1; h < G; ++h) m2 = fminf(m2, red[h * P + threadIdx.x]);
+      loc = m2;
+    }
     for (int o = 16; o; o >>= 1) loc = fmaxf(loc, __shfl_xor_sync(0xffffffffu, loc, o));
+    __syncthreads();  // red is reused below
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = loc;
     __syncthreads();
-    float blk = run;
-    for (int w = 0; w < kHdThreads / 32; ++w) blk = fmaxf(blk, red[w]);
-    run = blk;
-    // a pair whose partial max already exceeds the query's best cannot win;
-    // thread 0 reads the (concurrently updated) best once for the whole CTA
-    if (threadIdx.x == 0)
-      red[kHdThreads / 32] =
-          (best_bits && run > __uint_as_float(*(volatile const unsigned*)best_bits)) ? 1.0f : 0.0f;
+    for (int w = 0; w < kHdThreads / 32; ++w) run = fmaxf(run, red[w]);
     __syncthreads();
-    const bool stop = red[kHdThreads / 32] != 0.0f;
-    __syncthreads();
-    if (stop) return run;
   }
   return run;
 }
 
-// One CTA per (query, candidate slot): both trajectories in shared memory,
-// symmetric Hausdorff^2 = max(h(A,B), h(B,A)), atomic min into the query's
-// best (non-negative floats order like their bit patterns).
+// One CTA per query: the query in shared memory once, its top_k candidates
+// in turn (the reference's hausdorff_tiled_rtree_kernel order,
+// CudaRuntime1/hausdorff.cu:84-122); symmetric Hausdorff^2 =
+// max(h(A,B), h(B,A)), the second direction skipped once the first already
+// exceeds the query's best.
 __global__ void __launch_bounds__(kHdThreads)
     hausdorff_cands_kernel(const float2* __restrict__ t1, int n, const float2* __restrict__ t2,
                            int num_t2, int m, const int* __restrict__ cand, int top_k,
                            unsigned* __restrict__ best_bits) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ float red[kHdThreads / 32 + 1];
+  __shared__ float red[kHdThreads];
   float2* A = reinterpret_cast<float2*>(smem_raw);
   float2* B = A + n;
-  const int q = blockIdx.x / top_k;
-  const int c = cand[blockIdx.x];
-  if (c < 0 || c >= num_t2) return;  // out-of-range candidate slots are ignored
+  const int q = blockIdx.x;
   const float2* ga = t1 + (size_t)q * n;
-  const float2* gb = t2 + (size_t)c * m;
   for (int i = threadIdx.x; i < n; i += kHdThreads) A[i] = ga[i];
-  for (int i = threadIdx.x; i < m; i += kHdThreads) B[i] = gb[i];
-  __syncthreads();
-  float h1 = directed_max_min(A, n, B, m, 0.0f, best_bits + q, red);
-  float h = directed_max_min(B, m, A, n, h1, best_bits + q, red);
-  if (threadIdx.x == 0) atomicMin(best_bits + q, __float_as_uint(h));
-}
-
-__global__ void init_bits_kernel(unsigned* p, int count, unsigned v) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < count) p[i] = v;
+  float best = TSIM_INF;
+  for (int k = 0; k < top_k; ++k) {
+    const int c = cand[(size_t)q * top_k + k];
+    if (c < 0 || c >= num_t2) continue;  // out-of-range candidate slots are ignored
+    const float2* gb = t2 + (size_t)c * m;
+    __syncthreads();  // the previous candidate is done with B
+    for (int i = threadIdx.x; i < m; i += kHdThreads) B[i] = gb[i];
+    __syncthreads();
+    const float h1 = directed_max_min(A, n, B, m, red);
+    if (!(h1 < best)) continue;  // uniform: every thread holds the same h1
+    const float h = fmaxf(h1, directed_max_min(B, m, A, n, red));
+    best = fminf(best, h);
+  }
+  if (threadIdx.x == 0) best_bits[q] = __float_as_uint(best);
 }
 
 __global__ void sqrt_bits_kernel(const unsigned* bits, float* out, int count) {
@@ -105,88 +105,84 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// Warp per CSR entry: compensated FP32 sum of squared point differences.
+// Warp per query (the reference's block per query, CudaRuntime1/euclidean.cu:
+// 17-73).  First its CSR entries four at a time, 8 lanes each: compensated
+// FP32 sums of squared point differences (TwoSum per lane, a compensated
+// butterfly over the 8); their order does not matter, since they only pick
+// the candidates whose sum lies within its rigorous error margin of the
+// smallest.  Those are re-scored in FP64 left to right exactly like
+// calc_exact_dist_sq (euclidean.cpp:27-40): the lanes compute 32 terms
+// dx^2 + dy^2 at a time, and every lane adds them to the running sum in
+// point order; out = (float)sqrt of the best.
 __global__ void __launch_bounds__(kEuThreads)
     euclid_cands_kernel(const float2* __restrict__ t1, const float2* __restrict__ t2,
                         const int* __restrict__ cand, const int* __restrict__ off, int num_t, int n,
-                        int total, float* __restrict__ s32) {
-  const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int e = gw; e < total; e += nw) {
-    // query owning entry e: binary search in off
-    int lo = 0, hi = num_t;
-    while (hi - lo > 1) {
-      int mid = (lo + hi) >> 1;
-      if (off[mid] <= e) lo = mid; else hi = mid;
-    }
-    const int ce = cand[e];
-    if (ce < 0 || ce >= num_t) {  // out-of-range candidates never win
-      if (lane == 0) s32[e] = TSIM_INF;
-      continue;
-    }
-    const float2* a = t1 + (size_t)lo * n;
-    const float2* b = t2 + (size_t)ce * n;
-    float s = 0.0f, c = 0.0f;
-    for (int i = lane; i < n; i += 32) {
-      float2 p = a[i], r = b[i];
-      float dx = p.x - r.x, dy = p.y - r.y;
-      float t = fmaf(dy, dy, dx * dx);
-      float ns, err;
-      two_sum(s, t, ns, err);
-      s = ns;
-      c += err;
-    }
-    for (int o = 16; o; o >>= 1) {
-      float s2 = __shfl_xor_sync(0xffffffffu, s, o);
-      float c2 = __shfl_xor_sync(0xffffffffu, c, o);
-      float ns, err;
-      two_sum(s, s2, ns, err);
-      s = ns;
-      c = c + c2 + err;
-    }
-    if (lane == 0) s32[e] = s + c;
-  }
-}
-
-// Warp per query: candidates whose compensated FP32 sum lies within the
-// rigorous error margin of the smallest are re-scored in FP64, left to right
-// exactly like calc_exact_dist_sq (euclidean.cpp:27-40); out = (float)sqrt.
-__global__ void euclid_rescore_kernel(const float2* __restrict__ t1,
-                                      const float2* __restrict__ t2,
-                                      const int* __restrict__ cand, const int* __restrict__ off,
-                                      const float* __restrict__ s32, int num_t, int n, int total,
-                                      float* __restrict__ out) {
+                        int total, float* __restrict__ s32, float* __restrict__ out) {
   const int lane = threadIdx.x & 31;
   const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (q >= num_t) return;
   // clamp caller offsets into [0, total] so a malformed CSR cannot read out of bounds
   const int b = min(max(off[q], 0), total), e = max(min(off[q + 1], total), b);
+  const float2* A = t1 + (size_t)q * n;
+  const int grp = lane >> 3, gl = lane & 7;
   float mn = TSIM_INF;
-  for (int i = b + lane; i < e; i += 32) mn = fminf(mn, s32[i]);
-  for (int o = 16; o; o >>= 1) mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+  for (int base = b; base < e; base += 4) {
+    const int idx = base + grp;
+    const int ce = idx < e ? cand[idx] : -1;
+    const bool ok = ce >= 0 && ce < num_t;  // out-of-range candidates never win
+    const float2* B = t2 + (size_t)(ok ? ce : 0) * n;
+    float sum = 0.0f, c = 0.0f;
+    for (int i = gl; i < n; i += 8) {
+      const float2 p = A[i], r = B[i];
+      const float dx = p.x - r.x, dy = p.y - r.y;
+      float ns, err;
+      two_sum(sum, fmaf(dy, dy, dx * dx), ns, err);
+      sum = ns;
+      c += err;
+    }
+    for (int o = 4; o; o >>= 1) {
+      const float s2 = __shfl_xor_sync(0xffffffffu, sum, o);
+      const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+      float ns, err;
+      two_sum(sum, s2, ns, err);
+      sum = ns;
+      c = c + c2 + err;
+    }
+    const float tot = ok ? sum + c : TSIM_INF;
+    if (gl == 0 && idx < e) s32[idx] = tot;
+    mn = fminf(mn, tot);
+  }
+  for (int o = 16; o >= 8; o >>= 1) mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+  __syncwarp();
   // |s32 - exact| <= g * exact with g = 2^-20 (terms 2u, TwoSum chain ~2u,
   // final fold ~2u, n*u^2 negligible for n < 2^20)
   const double g = 1.0 / (1 << 20);
   const double thr = (double)mn * (1.0 + g) / (1.0 - g);
   double best = 1.7976931348623157e308;
-  for (int i = b + lane; i < e; i += 32) {
-    if ((double)s32[i] > thr || cand[i] < 0 || cand[i] >= num_t) continue;
-    const float2* A = t1 + (size_t)q * n;
-    const float2* B = t2 + (size_t)cand[i] * n;
-    double s = 0.0;
-    for (int k = 0; k < n; ++k) {
-      double dx = (double)A[k].x - (double)B[k].x;
-      double dy = (double)A[k].y - (double)B[k].y;
-      s = __dadd_rn(s, __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+  for (int base = b; base < e; base += 32) {
+    const int idx = base + lane;
+    bool need = false;
+    if (idx < e) need = (double)s32[idx] <= thr && cand[idx] >= 0 && cand[idx] < num_t;
+    unsigned todo = __ballot_sync(0xffffffffu, need);
+    while (todo) {
+      const int l = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const float2* B = t2 + (size_t)cand[base + l] * n;
+      double s = 0.0;
+      for (int k0 = 0; k0 < n; k0 += 32) {
+        double t = 0.0;
+        if (k0 + lane < n) {
+          const double dx = (double)A[k0 + lane].x - (double)B[k0 + lane].x;
+          const double dy = (double)A[k0 + lane].y - (double)B[k0 + lane].y;
+          t = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+        }
+        const int cnt = min(32, n - k0);
+        for (int u = 0; u < cnt; ++u) s = __dadd_rn(s, __shfl_sync(0xffffffffu, t, u));
+      }
+      best = s < best ? s : best;
     }
-    best = s < best ? s : best;
   }
-  for (int o = 16; o; o >>= 1) {
-    double w = __shfl_xor_sync(0xffffffffu, best, o);
-    best = w < best ? w : best;
-  }
-  if (lane == 0) out[q] = e > b ? __double2float_rn(__dsqrt_rn(best)) : __double2float_rn(__dsqrt_rn(1.7976931348623157e308));
+  if (lane == 0) out[q] = __double2float_rn(__dsqrt_rn(best));
 }
 
 // ---- bounding boxes and box nearest neighbours --------------------------------
@@ -249,15 +245,13 @@ int hausdorff_cands(tsim_ctx* ctx, const float2* t1, int num_t1, int n, const fl
                     int m, const int* cand, int top_k, float* out) {
   TSIM_TRY(arena_reserve(ctx, align256(sizeof(unsigned) * num_t1)));
   unsigned* best = arena_take<unsigned>(ctx, num_t1);
-  init_bits_kernel<<<(num_t1 + 255) / 256, 256, 0, ctx->stream>>>(best, num_t1, 0x7f800000u);
   size_t smem = sizeof(float2) * ((size_t)n + m);
   TSIM_CHECK_ARG(smem <= 200 * 1024, "trajectories too long for the shared-memory Hausdorff kernel");
   if (smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(hausdorff_cands_kernel,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if ((long long)num_t1 * top_k > 0)
-    hausdorff_cands_kernel<<<num_t1 * top_k, kHdThreads, smem, ctx->stream>>>(t1, n, t2, num_t2, m,
-                                                                              cand, top_k, best);
+  hausdorff_cands_kernel<<<num_t1, kHdThreads, smem, ctx->stream>>>(t1, n, t2, num_t2, m, cand,
+                                                                     top_k, best);
   sqrt_bits_kernel<<<(num_t1 + 255) / 256, 256, 0, ctx->stream>>>(best, out, num_t1);
   TSIM_CUDA(cudaGetLastError());
   return TSIM_OK;
@@ -267,13 +261,9 @@ int euclid_cands(tsim_ctx* ctx, const float2* t1, const float2* t2, const int* c
                  int num_t, int n, int total, float* out) {
   TSIM_TRY(arena_reserve(ctx, align256(sizeof(float) * std::max(total, 1))));
   float* s32 = arena_take<float>(ctx, std::max(total, 1));
-  if (total > 0) {
-    int blocks = std::min((total + 3) / 4, ctx->num_sms * 16);
-    euclid_cands_kernel<<<blocks, kEuThreads, 0, ctx->stream>>>(t1, t2, cand, off, num_t, n, total,
-                                                               s32);
-  }
-  euclid_rescore_kernel<<<(num_t + 3) / 4, 128, 0, ctx->stream>>>(t1, t2, cand, off, s32, num_t, n,
-                                                                  total, out);
+  const int warps = kEuThreads / 32;
+  euclid_cands_kernel<<<(num_t + warps - 1) / warps, kEuThreads, 0, ctx->stream>>>(
+      t1, t2, cand, off, num_t, n, total, s32, out);
   TSIM_CUDA(cudaGetLastError());
   return TSIM_OK;
 }

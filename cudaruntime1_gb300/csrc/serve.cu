@@ -181,7 +181,7 @@ int launch(tsim_server* s, Slot& sl) {
     sl.pinned = nullptr;
     sl.pinned_cap = 0;
     const size_t cap = std::max<size_t>(sl.staging, size_t(1) << 20);
-    TSIM_CUDA(cudaHostAlloc((void**)&sl.pinned, cap, cudaHostAllocDefault));
+    TSIM_CUDA(host_alloc((void**)&sl.pinned, cap));
     sl.pinned_cap = cap;
   }
   // concatenate the queries and rebase their offsets
@@ -378,7 +378,7 @@ extern "C" int tsim_server_create(tsim_ctx* ctx, tsim_db* db, const tsim_server_
   s->queue_cap = opts && opts->queue_cap > 0 ? opts->queue_cap : 65536;
   s->slots.resize(nslots);
   int st = TSIM_OK;
-  cudaError_t e = cudaMalloc((void**)&s->pool_base, s->budget);
+  cudaError_t e = dev_malloc((void**)&s->pool_base, s->budget);
   if (e != cudaSuccess) st = cuda_fail(e, "server pool", __FILE__, __LINE__);
   for (int i = 0; i < nslots && st == TSIM_OK; ++i) {
     Slot& sl = s->slots[i];

@@ -142,6 +142,13 @@ T* arena_take(tsim_ctx* ctx, size_t count) {
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 int pinned_reserve(tsim_ctx* ctx, size_t bytes);
+// Every device and pinned-host allocation of the library goes through these,
+// so tsim_debug_fail_allocations can make any of them fail as out of memory.
+cudaError_t dev_malloc(void** p, size_t bytes);
+cudaError_t host_alloc(void** p, size_t bytes);
+// debug: fill every arena reservation with 0xff bytes (NaN floats, -1 ints)
+// before a call's kernels run, so scratch read before it is written shows
+bool debug_canary();
 int ensure_subs(tsim_ctx* ctx, int n);
 
 // stage timing: bracket one stage's launches; no-ops unless profiling is on
@@ -316,6 +323,33 @@ int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a, int max_m)
 // long, full-row pairs, where the latency of one pair is the launch's).
 int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, int* spill,
                    int* nspill, int* tmp, int* ntmp, int warps = 1);
+// Band-relative anti-diagonal kernel (dp_wave.cu) for DTW and Frechet, FP32
+// and compensated (wave_kind): a warp per pair, lane p holding the p-th live
+// cells of the anti-diagonal, passes with R = 1 and 2 cells per lane; pairs
+// whose band holds more than 64 cells per anti-diagonal (or longer than
+// 2048 points, or than max_n x max_m) are left in spill[] (count in *nspill).
+bool wave_kind(int kind);
+int launch_dp_wave(tsim_ctx* ctx, int kind, const DpArgs& a, int max_n, int max_m, int* spill,
+                   int* nspill, int* tmp, int* ntmp);
+// Lane-per-pair kernel (dp_lane.cu) for the FP32 DTW, Frechet and LCSS
+// kinds (lane_kind): a lane runs a whole pair in passes of 8 rows, the row
+// above a pass in a shared-memory ring of `ring` (64 or 128) values per lane
+// (lane_ring_for picks it from the longest pair); pairs wider than the ring,
+// or with fewer than two points on a side, are left in spill[] (count in
+// *nspill, cleared here).  When the list holds fewer than `gate` pairs (read
+// on the device) the kernel computes nothing and copies the whole list, in
+// order, to spill[] for the warp-per-pair kernels.
+bool lane_kind(int kind);
+// order[] := the indices 0 .. a.npairs-1 of a.pairs sorted by shape (longer
+// length / 16, shorter length / 16, longest first); counts: lane_sort_buckets() ints
+int lane_sort(tsim_ctx* ctx, const DpArgs& a, int* order, int* counts);
+int lane_sort_buckets();
+// pair count from which a survivor round of pairs up to max_n x max_m runs
+// on a lane per pair (band_pct / delta < 0: none)
+int lane_gate_for(int kind, int max_n, int max_m, int band_pct, int delta);
+int lane_ring_for(int kind, int max_n, int max_m, int band_pct, int delta);
+int launch_dp_lane(tsim_ctx* ctx, int kind, const DpArgs& a, int ring, int* spill, int* nspill,
+                   int gate = 0);
 // the anti-diagonal kernel's validity condition for a pair shape, R rows
 // per lane-group and `lanes` lanes per pair
 bool diag_ok(bool lcss, int n, int m, int wd, int R, int lanes = 32);

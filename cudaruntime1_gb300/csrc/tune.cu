@@ -85,8 +85,8 @@ extern "C" int tsim_autotune(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
   float* dd = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int st = TSIM_OK;
-  cudaError_t ce = cudaMalloc(&ids, sizeof(int) * (size_t)nq * p->k);
-  if (ce == cudaSuccess) ce = cudaMalloc(&dd, sizeof(float) * (size_t)nq * p->k);
+  cudaError_t ce = dev_malloc(reinterpret_cast<void**>(&ids), sizeof(int) * (size_t)nq * p->k);
+  if (ce == cudaSuccess) ce = dev_malloc(reinterpret_cast<void**>(&dd), sizeof(float) * (size_t)nq * p->k);
   if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
   if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
   if (ce != cudaSuccess) st = cuda_fail(ce, "tsim_autotune setup", __FILE__, __LINE__);

@@ -76,6 +76,12 @@ typedef enum tsim_cost {
                                        bit-identical to an FP64 evaluation */
 #define TSIM_FLAG_ALWAYS_PRUNE 0x10u /* run the bound stages even for requests small
                                         enough to refine every pair (the default) */
+#define TSIM_FLAG_NO_LANE_DP 0x20u  /* survivor rounds stay on the warp-per-pair DP
+                                       kernels even when they hold many pairs (the
+                                       lane-per-pair kernel is off); same values */
+#define TSIM_FLAG_NO_WAVE_DP 0x40u  /* DTW / Frechet rounds skip the band-relative DP
+                                       kernel (lanes along the anti-diagonal) and start
+                                       on the row-group ones; same values */
 
 typedef struct tsim_params {
   int measure;    /* tsim_measure */
@@ -153,6 +159,18 @@ TSIM_API int tsim_ctx_survivor_cells(tsim_ctx* ctx, int64_t* cells);
 /* Measured FP32 FMA throughput of this GPU in TFLOP/s (a short probe kernel,
  * for roofline denominators). */
 TSIM_API int tsim_probe_fp32_tflops(tsim_ctx* ctx, double* tflops);
+
+/* ---- debugging hooks (no counterpart in the reference, whose host code exits
+ * on the first CUDA error: CudaRuntime1/common.cuh CHECK) ------------------ */
+/* After `skip` more device or pinned-host allocations of the library succeed,
+ * the next `count` fail as if the GPU were out of memory: the call that meets
+ * one returns TSIM_ERR_OUT_OF_MEMORY and leaves its context usable.  count 0
+ * disarms.  Process-wide; for tests of the error paths. */
+TSIM_API int tsim_debug_fail_allocations(int skip, int count);
+/* on != 0: every call fills the scratch it reserves with 0xff bytes (NaN
+ * floats, -1 integers) before its kernels run, so a kernel that reads scratch
+ * before writing it changes results.  Process-wide; slows every call. */
+TSIM_API int tsim_debug_set_canary(int on);
 
 /* ---- device-resident candidate database ---------------------------------- */
 /* Copies host points/offsets to the device and builds per-trajectory
@@ -282,7 +300,13 @@ TSIM_API int tsim_server_destroy(tsim_server* s);
  * band / window / cost.  precision: 0 = FP32 (d_out32), 1 = compensated FP32
  * (d_out64), 2 = FP64 (d_out64).  kernel: 0 = automatic, 1 = round-striped
  * DP, 2 = anti-diagonal DP with a warp per pair, 3 = with a CTA of 8 warps
- * per pair, 4 = with 2 warps per pair (pairs they cannot take fall back to 1).  Frechet
+ * per pair, 4 = with 2 warps per pair (pairs they cannot take fall back to 1),
+ * 5 = a lane per pair (FP32 DTW, Frechet and LCSS, the throughput form for
+ * many pairs; pairs whose band is too wide for it, and the other precisions,
+ * go to 2, then 1), 6 = band-relative anti-diagonal with a warp per pair
+ * (DTW and Frechet; lanes hold the live cells of an anti-diagonal; pairs
+ * with more than 64 per anti-diagonal go to 2, then 1).  Every kernel
+ * computes the same cells with the same operations.  Frechet
  * values are squared distances; LCSS values are match counts. */
 TSIM_API int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision, int kernel,
                            const tsim_point* d_qpts, const int64_t* d_qoff, int max_qlen,

@@ -39,9 +39,10 @@ class OrcParams(C.Structure):
                 ("band_pct", C.c_int), ("epsilon", C.c_float), ("delta", C.c_int)]
 
 
-# where the reference's CPU sources are read from: TSIM_REFERENCE_DIR, else
-# the read-only checkout of the build host (absent on other machines)
-REFERENCE_DIR_DEFAULT = "/root/reference/CudaRuntime1"
+# where the reference's sources are read from: TSIM_REFERENCE_DIR, else a
+# checkout named reference/ beside this repository (absent on most machines)
+REFERENCE_DIR_DEFAULT = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference",
+                                     "CudaRuntime1")
 
 
 def reference_dir():

@@ -1,6 +1,8 @@
 """The DP kernels pair by pair against the FP64 oracle: every precision
-(FP32, compensated FP32, FP64) on both kernels (round-striped and
-anti-diagonal), across query/candidate shapes, bands and windows.
+(FP32, compensated FP32, FP64) on every kernel (round-striped; anti-diagonal
+with a warp, two warps or a CTA per pair; a lane per pair; band-relative
+with a warp per pair), across
+query/candidate shapes, bands and windows.
 FP64 values must be bit-identical, compensated within 1e-9, FP32 within the
 FP32 error bound (n+m+8)*2^-24, LCSS counts exact."""
 import numpy as np
@@ -58,7 +60,8 @@ def test_dp_pairs_all_kernels(tsim, cuda_ctx, oracle, measure, kw, lo, hi):
                      for a, b in pairs])
     n_ = np.diff(qo)[pairs[:, 0]]
     m_ = np.diff(co)[pairs[:, 1]]
-    for kernel in (1, 2, 3, 4):
+    fp32 = {}
+    for kernel in (1, 2, 3, 4, 5, 6):
         for precision in ((0,) if measure == "lcss" else (0, 1, 2)):
             o32 = torch.full((len(pairs),), float("nan"), dtype=torch.float32, device="cuda")
             o64 = torch.full((len(pairs),), float("nan"), dtype=torch.float64, device="cuda")
@@ -68,6 +71,8 @@ def test_dp_pairs_all_kernels(tsim, cuda_ctx, oracle, measure, kw, lo, hi):
                          len(pairs), o32.data_ptr(), o64.data_ptr(), **kw)
             torch.cuda.synchronize()
             got = (o32 if precision == 0 else o64).cpu().numpy().astype(np.float64)
+            if precision == 0:
+                fp32[kernel] = o32.cpu().numpy()
             w = want ** 2 if measure == "frechet" else want  # kernels report Frechet squared
             tag = (measure, kernel, precision)
             assert np.array_equal(np.isfinite(got), np.isfinite(w)), tag
@@ -85,3 +90,8 @@ def test_dp_pairs_all_kernels(tsim, cuda_ctx, oracle, measure, kw, lo, hi):
             else:
                 bound = (n_[f] + m_[f] + 8) * 2.0 ** -24 * 1.01 + 1e-12
                 assert np.all(rel <= bound), (tag, rel.max(), np.argmax(rel / bound))
+    # the same cells with the same operations: FP32 values agree to the bit
+    # between the warp-per-pair, lane-per-pair and band-relative kernels
+    for kernel in (5, 6):
+        assert np.array_equal(fp32[2].view(np.uint32), fp32[kernel].view(np.uint32)), \
+            (measure, kernel)

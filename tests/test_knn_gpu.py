@@ -376,3 +376,35 @@ def test_plain_small_workload_full_size(tsim, cuda_ctx, oracle, pruned):
             assert rel.max() <= REL_TOL, (measure, rel.max())
         assert st["pairs"] == 8 * 1024
     db.close()
+
+
+@pytest.mark.parametrize("measure,kw", [("dtw", dict(band_pct=10, cost=0)),
+                                        ("dtw", dict(band_pct=-1, cost=1)),
+                                        ("lcss", dict(epsilon=0.5, delta=8)),
+                                        ("frechet", {})])
+def test_dp_kernel_choices_agree(tsim, cuda_ctx, oracle, measure, kw):
+    """Rounds of many pairs run a lane per pair (dp_lane.cu), DTW and Frechet
+    rounds start on the band-relative kernel (dp_wave.cu); with
+    TSIM_FLAG_NO_LANE_DP / TSIM_FLAG_NO_WAVE_DP they run on the row-group
+    kernels instead.  Every choice gives the same ids and distance bits,
+    brute force (36,000 pairs, past the lane kernel's gate) and pruned, and
+    the ids equal the FP64 oracle's."""
+    cp, co = _db(3000, 16, 300, 91)
+    ql = G.uniform_lengths(12, 16, 300, 92)
+    qp, qo = G.random_walks(12, ql, 93)
+    db = tsim.Database(cuda_ctx, cp, co)
+    okw = {("eps" if k == "epsilon" else k): v for k, v in kw.items()}
+    want_ids, _ = oracle.knn(measure, qp, qo, cp, co, 10, **okw)
+    off = tsim.api.FLAG_NO_LANE_DP | tsim.api.FLAG_NO_WAVE_DP
+    for extra in (0, tsim.api.FLAG_ALWAYS_PRUNE):
+        base = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 10, flags=extra | off, **kw)
+        assert np.array_equal(base[0], want_ids), (measure, extra)
+        for choice in (0, tsim.api.FLAG_NO_LANE_DP, tsim.api.FLAG_NO_WAVE_DP):
+            got = _device_knn(tsim, cuda_ctx, db, qp, qo, measure, 10, flags=extra | choice, **kw)
+            assert np.array_equal(got[0], base[0]), (measure, extra, choice)
+            assert np.array_equal(got[1].view(np.uint32), base[1].view(np.uint32)), \
+                (measure, extra, choice)
+            if measure != "lcss":  # the FP64 re-scored distances
+                assert np.array_equal(got[2].view(np.uint64), base[2].view(np.uint64)), \
+                    (measure, extra, choice)
+    db.close()
