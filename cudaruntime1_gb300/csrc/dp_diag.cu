@@ -150,6 +150,9 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
       continue;
     }
     const float thr = a.thr ? a.thr[q] : TSIM_INF;
+    // the cell policy's parameter: eps, or the pair's aux value (the exact
+    // Frechet window's FP32 value)
+    const float aux = a.aux ? (float)a.aux[pid] : a.eps;
     const int rrow = result_row<P>(n, m, a.delta);
     if (pl == 0) store_result(a, pid, P::border());
 
@@ -356,7 +359,7 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
         const V lf = left[r];
         const V up = r > 0 ? left[r > 0 ? r - 1 : 0] : up_in;
         const V dg = r > 0 ? left2[r > 0 ? r - 1 : 0] : dg_in;
-        V v = P::cell(qx[r], qy[r], cw[r].x, cw[r].y, up, lf, dg, a.eps);
+        V v = P::cell(qx[r], qy[r], cw[r].x, cw[r].y, up, lf, dg, aux);
         const bool in = (unsigned)(t - base[r]) <= wdt[r];
         v = in ? v : P::masked(lf);
         left2[r] = lf;
@@ -457,7 +460,7 @@ int launch_diag_r(tsim_ctx* ctx, int R, const DpArgs& a, int max_m, int* spill, 
       if constexpr (W == 1 || W == kCtaWarps) return launch_diag_one<P, 8, W>(ctx, a, max_m, spill, nspill);
       break;
     default:
-      if (W == 1) return launch_diag_one<P, 16, 1>(ctx, a, max_m, spill, nspill);
+      if constexpr (W == 1) return launch_diag_one<P, 16, 1>(ctx, a, max_m, spill, nspill);
       break;
   }
   return fail(TSIM_ERR_UNSUPPORTED, "no CTA-per-pair kernel with this many rows per lane");
@@ -465,7 +468,7 @@ int launch_diag_r(tsim_ctx* ctx, int R, const DpArgs& a, int max_m, int* spill, 
 
 template <class P>
 int launch_chain(tsim_ctx* ctx, int R0, int warps, const DpArgs& a, int max_m, int* spill,
-                 int* nspill, int* tmp, int* ntmp) {
+                 int* nspill, int* tmp, int* ntmp, int rcap = 0) {
   // R0, 2 R0, .. Rmax: each pass takes the pairs the previous one spilled, so
   // every pair runs with the fewest rows per lane-group its shape admits
   // (fewer rows in flight, fewer masked cells); the last pass writes `spill`.
@@ -476,7 +479,8 @@ int launch_chain(tsim_ctx* ctx, int R0, int warps, const DpArgs& a, int max_m, i
   // 2 (min(n,m) - 1) <= n + m - 2), the window or the longest full row fits
   // its lanes: the chain stops there, and only degenerate pairs are left for
   // the striped kernel.
-  const int rmax = warps == 1 ? 16 : (warps == kCtaWarps ? 8 : 4);
+  int rmax = warps == 1 ? 16 : (warps == kCtaWarps ? 8 : 4);
+  if (rcap > 0) rmax = std::min(rmax, rcap);
   const int lanes = 32 * warps;
   auto takes_all = [&](int R) {
     if (a.max_n <= 0) return false;  // query lengths unknown
@@ -510,21 +514,51 @@ int launch_chain(tsim_ctx* ctx, int R0, int warps, const DpArgs& a, int max_m, i
   return TSIM_OK;
 }
 
+// the chain of launch_chain for a CTA per pair only (R = R0 .. 8)
+template <class P>
+int launch_chain_cta(tsim_ctx* ctx, int R0, const DpArgs& a, int max_m, int* spill, int* nspill,
+                     int* tmp, int* ntmp) {
+  std::vector<int> rs;
+  for (int R = std::max(1, std::min(R0, 8)); R <= 8; R *= 2) {
+    rs.push_back(R);
+    if (a.max_n > 0 && max_m <= (kCtaWarps * 32 - 1) * R + 1) break;  // full rows: all fit
+  }
+  const int np = (int)rs.size();
+  DpArgs in = a;
+  for (int p = 0; p < np; ++p) {
+    const bool to_spill = ((np - 1 - p) & 1) == 0;
+    int* out = to_spill ? spill : tmp;
+    int* nout = to_spill ? nspill : ntmp;
+    TSIM_CUDA(cudaMemsetAsync(nout, 0, 2 * sizeof(int), ctx->stream));  // spills, work counter
+    TSIM_TRY((launch_diag_r<P, kCtaWarps>(ctx, rs[p], in, max_m, out, nout)));
+    in.order = out;
+    in.npairs_dev = nout;
+  }
+  return TSIM_OK;
+}
+
 }  // namespace
 
 int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, int* spill,
-                   int* nspill, int* tmp, int* ntmp, int warps) {
+                   int* nspill, int* tmp, int* ntmp, int warps, int rmax) {
   const int W = warps > 2 ? kCtaWarps : warps;
+  if (kind == DP_FRECHET_WIN) {
+    // the exact FP64 Frechet re-score: few, possibly long full-row pairs
+    // (latency), on a CTA per pair only
+    if (W != kCtaWarps)
+      return fail(TSIM_ERR_UNSUPPORTED, "the exact Frechet re-score runs on a CTA per pair");
+    return launch_chain_cta<PolFrechetWin>(ctx, R, a, max_m, spill, nspill, tmp, ntmp);
+  }
   switch (kind) {
-    case DP_DTW_SQ: return launch_chain<PolDtwSq>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
-    case DP_DTW_EU: return launch_chain<PolDtwEu>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
-    case DP_LCSS: return launch_chain<PolLcss>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_SQ: return launch_chain<PolDtwSq>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp, rmax);
+    case DP_DTW_EU: return launch_chain<PolDtwEu>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp, rmax);
+    case DP_LCSS: return launch_chain<PolLcss>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp, rmax);
     case DP_FRECHET_SQ:
-      return launch_chain<PolFrechetSq>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
-    case DP_DTW_SQC: return launch_chain<PolDtwSqC>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
-    case DP_DTW_EUC: return launch_chain<PolDtwEuC>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
+      return launch_chain<PolFrechetSq>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp, rmax);
+    case DP_DTW_SQC: return launch_chain<PolDtwSqC>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp, rmax);
+    case DP_DTW_EUC: return launch_chain<PolDtwEuC>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp, rmax);
     case DP_FRECHET_SQC:
-      return launch_chain<PolFrechetSqC>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp);
+      return launch_chain<PolFrechetSqC>(ctx, R, W, a, max_m, spill, nspill, tmp, ntmp, rmax);
   }
   return fail(TSIM_ERR_UNSUPPORTED, "no anti-diagonal kernel for this DP kind");
 }

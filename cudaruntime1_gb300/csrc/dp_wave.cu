@@ -69,19 +69,23 @@ __host__ __device__ inline int wave_lmax(int n, int m, int w) {
   return (int)(l < mn ? l : mn);
 }
 
+// float2 slots of shared memory per warp: query points (qcap + pad),
+// candidate points (pad + ccap + pad), ilo | L << 16 of every anti-diagonal
+// (tcap ints)
+__host__ __device__ inline size_t wave_per_warp(int qcap, int ccap, int tcap) {
+  return (size_t)(qcap + kWavePad) + (ccap + 2 * kWavePad) + tcap / 2;
+}
+
 template <class P, int R>
 __global__ void __launch_bounds__(kWaveThreads)
     dp_wave_kernel(DpArgs a, int qcap, int ccap, int tcap, int* spill, int* nspill) {
   static_assert(P::kMin, "the band-relative kernel serves the minimum measures");
   using V = typename P::V;
   using C = typename P::C;
-  // per warp: query points (qcap + pad), candidate points (pad + ccap + pad),
-  // then ilo | L << 16 of every anti-diagonal (tcap)
   extern __shared__ __align__(16) float2 wave_smem[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  const size_t per_warp = (size_t)(qcap + kWavePad) + (ccap + 2 * kWavePad) + tcap / 2;
-  float2* qs = wave_smem + (size_t)warp * per_warp;
+  float2* qs = wave_smem + (size_t)warp * wave_per_warp(qcap, ccap, tcap);
   float2* cs = qs + qcap + kWavePad + kWavePad;  // cs[-kWavePad .. ccap + kWavePad)
   int* tab = reinterpret_cast<int*>(cs + ccap + kWavePad);
   const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -253,8 +257,7 @@ int launch_wave_one(tsim_ctx* ctx, const DpArgs& a, int qcap, int ccap, int tcap
                     int* nspill) {
   if (a.npairs <= 0) return TSIM_OK;
   auto kern = dp_wave_kernel<P, R>;
-  const size_t per_warp = (size_t)(qcap + kWavePad) + (ccap + 2 * kWavePad) + tcap / 2;
-  const size_t smem = (size_t)(kWaveThreads / 32) * per_warp * sizeof(float2);
+  const size_t smem = (size_t)(kWaveThreads / 32) * wave_per_warp(qcap, ccap, tcap) * sizeof(float2);
   if (smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;

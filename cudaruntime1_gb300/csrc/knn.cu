@@ -129,6 +129,8 @@ struct KArgs {
   int rdiag_cta;            // the same for a CTA per pair (0: no R fits the longest pair)
   int rdiag_w2;             // the same for two warps per pair
   float4* qtab;             // [nq*tstride] query sparse tables (global memory)
+  float4* qenv;             // LCSS with a window: [nq*env_stride] eps-inflated boxes of the
+  int env_stride;           //   query rows [i-delta, i+delta], i < max_qlen+delta (else null)
   int tstride;
   int* off2;                // [nq+1]
   int* npairs;              // [1]
@@ -497,6 +499,35 @@ __global__ void qtable_global_kernel(KArgs a, int sums) {
   }
 }
 
+// LCSS with an index window: column j of any candidate can only match query
+// rows [j-delta, j+delta], so its O(length) test needs the box of those rows
+// -- one box per j, the same for every candidate.  Built once per query
+// from its sparse table, inflated by eps with outward rounding (empty
+// windows get an empty box).
+__global__ void lcss_env_kernel(KArgs a) {
+  const int q = blockIdx.x;
+  const int n = a.qlen[q];
+  float4* E = a.qenv + (size_t)q * a.env_stride;
+  const int cnt = min(a.env_stride, n + a.delta + 1);
+  if (n <= 0 || n > a.max_qlen) {
+    for (int i = threadIdx.x; i < a.env_stride; i += blockDim.x)
+      E[i] = make_float4(-TSIM_INF, -TSIM_INF, TSIM_INF, TSIM_INF);  // no bound: everything in
+    return;
+  }
+  const QTable T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
+  const float e2 = __fmul_ru(a.eps, 1.0f + 1.0f / 1048576.0f);
+  for (int i = threadIdx.x; i < a.env_stride; i += blockDim.x) {
+    const int lo = max(0, i - a.delta), hi = min(n - 1, i + a.delta);
+    float4 b = make_float4(TSIM_INF, TSIM_INF, -TSIM_INF, -TSIM_INF);  // empty
+    if (i < cnt && lo <= hi) {
+      const float4 x = qtable_box(T, lo, hi);
+      b = make_float4(__fsub_rd(x.x, e2), __fsub_rd(x.y, e2), __fadd_ru(x.z, e2),
+                      __fadd_ru(x.w, e2));
+    }
+    E[i] = b;
+  }
+}
+
 // Segment bound of one pair: every column of candidate segment s lies in the
 // segment's box, and its band admits only the query rows between the band
 // rows of the segment's first and last column, so the column costs at least
@@ -797,12 +828,30 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
     }
     __syncthreads();
   }
-  for (int e = blockIdx.x * kLb2Warps + warp; e < cnt; e += gridDim.x * kLb2Warps) {
-    const int c = a.list1[(size_t)q * a.C + e];
-    const float2* B = a.cpts + a.coff[c];
-    const int m = a.clen[c];
+  // The warp's pairs e, e + S, ...: a pair's candidate index, then its
+  // offset, length and segment bound, are dependent loads; they are issued
+  // two and one pairs ahead of the pair being bounded, so their latency
+  // overlaps its column loop instead of preceding it.
+  const int S = gridDim.x * kLb2Warps;
+  const int* L1 = a.list1 + (size_t)q * a.C;
+  const float* LB1 = a.lb1 + (size_t)q * a.C;
+  int e = blockIdx.x * kLb2Warps + warp;
+  int c_nx = e < cnt ? L1[e] : 0;            // this pair's candidate
+  int c_nn = e + S < cnt ? L1[e + S] : 0;    // the next one's
+  int64_t o_nx = a.coff[c_nx];
+  int m_nx = a.clen[c_nx];
+  float s_nx = e < cnt ? LB1[c_nx] : 0.0f;
+  for (; e < cnt; e += S) {
+    const int c = c_nx;
+    const float2* B = a.cpts + o_nx;
+    const int m = m_nx;
+    const float sbnd = s_nx;  // the segment bound of stage A
+    c_nx = c_nn;
+    c_nn = e + 2 * S < cnt ? L1[e + 2 * S] : 0;
+    o_nx = a.coff[c_nx];
+    m_nx = a.clen[c_nx];
+    s_nx = e + S < cnt ? LB1[c_nx] : 0.0f;
     bool pass;
-    const float sbnd = a.lb1[(size_t)q * a.C + c];  // the segment bound of stage A
     float lbv = sbnd;  // the bound (no O(length) bound: stage A's)
     if (n <= 0 || m <= 0) {
       pass = false;
@@ -891,18 +940,18 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
     } else {
       // LCSS: candidate points that can match some query point of their
       // window (rows [j-delta, j+delta]) inside the eps-inflated box
+      // (the window's inflated box from the query's row boxes; the whole
+      // query's without a window)
       int count = 0;
-      for (int j = lane; j < m; j += 32) {
-        int lo = 0, hi = n - 1;
-        if (a.delta >= 0) {
-          lo = max(0, j - a.delta);
-          hi = min(n - 1, j + a.delta);
-        }
-        if (lo > hi) continue;
-        const float4 bx = qtable_box(T, lo, hi);
+      const float4* E = a.qenv ? a.qenv + (size_t)q * a.env_stride : nullptr;
+      const float4 qi = make_float4(__fsub_rd(qb.x, e2), __fsub_rd(qb.y, e2), __fadd_ru(qb.z, e2),
+                                    __fadd_ru(qb.w, e2));
+      const int jend = E ? min(m, a.env_stride) : m;  // columns past n-1+delta match nothing
+#pragma unroll 4
+      for (int j = lane; j < jend; j += 32) {
+        const float4 bx = E ? E[j] : qi;
         const float2 p = B[j];
-        if (p.x >= __fsub_rd(bx.x, e2) && p.x <= __fadd_ru(bx.z, e2) &&
-            p.y >= __fsub_rd(bx.y, e2) && p.y <= __fadd_ru(bx.w, e2)) {
+        if (p.x >= bx.x && p.x <= bx.z && p.y >= bx.y && p.y <= bx.w) {
           const float fx = (p.x - gx0) * ginv, fy = (p.y - gy0) * ginv;
           if (fx >= 0.0f && fy >= 0.0f && fx < (float)gnx && fy < (float)gny) {
             const int cell = (int)fy * gnx + (int)fx;
@@ -1410,10 +1459,10 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
     // lanes along the anti-diagonal, straight-line blocks of 16 steps: the
     // shortest FP32 step of the warp-per-pair forms (a lone 512 x 486 pair
     // 83 us against 104 on two warps per pair; compensated pairs are faster
-    // on two warps, 131 against 203 us), for the latency rounds; the
-    // survivor round stays on the row-group kernel, whose abandon test adds
-    // the remaining columns' bound (without it the batched workload's round
-    // computed 62 M cells instead of 38 M, 0.57 against 0.20 ms); pairs with
+    // on two warps, 131 against 203 us), for the latency rounds.  DTW's
+    // survivor round stays on the row-group kernel: with the same
+    // remaining-columns abandon bound (38 M cells either way) the batched
+    // workload's round took 0.24 ms here against 0.20 there; pairs with
     // more than 64 cells per anti-diagonal go on to the row-group kernels
     TSIM_TRY(launch_dp_wave(ctx, kind, d, d.max_n > 0 ? d.max_n : a.max_qlen, a.max_clen,
                             a.waves, a.nwaves, a.waves2, a.nwaves2));
@@ -1435,7 +1484,16 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
   const bool w2 = latency && a.rdiag_w2 > 0 && a.rdiag_w2 <= 2 &&
                   (twofloat || d.npairs <= 4 * ctx->num_sms);
   if (!w2 && latency && a.rdiag_cta > 0 && a.rdiag_shape >= (twofloat ? 4 : 8)) {
-    TSIM_TRY(launch_dp_diag(ctx, kind, a.rdiag_cta, d, a.max_clen, a.spill, a.nspill, a.spill2,
+    // the longest pair needs a CTA, but a round's lengths vary (lognormal
+    // Frechet queries): the pairs that fit a warp with up to 8 rows per lane
+    // run there, each at its fewest rows, the rest on a CTA per pair from
+    // one row per lane up -- instead of every pair at the longest pair's R
+    TSIM_TRY(launch_dp_diag(ctx, kind, 1, d, a.max_clen, a.lanes, a.nlanes, a.spill2, a.nspill2, 1,
+                            twofloat ? 4 : 8));
+    DpArgs rest = d;
+    rest.order = a.lanes;
+    rest.npairs_dev = a.nlanes;
+    TSIM_TRY(launch_dp_diag(ctx, kind, 1, rest, a.max_clen, a.spill, a.nspill, a.spill2,
                             a.nspill2, 8));
   } else if (w2 || (latency && twofloat && a.rdiag_shape >= 2 && a.rdiag_w2 > 0)) {
     // two warps per pair: a compensated row per lane and step, for a barrier
@@ -1507,8 +1565,16 @@ int finish_knn(tsim_ctx* ctx, KArgs& a, int dpc, int dp64) {
     r.pairs = a.r64pairs;
     r.out64 = a.r64;
     if (MEAS == M_FRECHET) {  // exact FP64 values from the FP32 ones: no FP64 DP
+      // a CTA of 8 warps per pair, each pair at the fewest rows per lane its
+      // length admits (the pairs are few and up to full rows of 2,041
+      // points: latency); longer ones on the striped kernel
       r.aux = a.rdc;
-      TSIM_TRY(launch_dp(ctx, DP_FRECHET_WIN, 32, 1, r, a.max_clen));
+      TSIM_TRY(launch_dp_diag(ctx, DP_FRECHET_WIN, 1, r, a.max_clen, a.spill, a.nspill, a.spill2,
+                              a.nspill2, 8));
+      DpArgs sp = r;
+      sp.order = a.spill;
+      sp.npairs_dev = a.nspill;
+      TSIM_TRY(launch_dp(ctx, DP_FRECHET_WIN, 32, 1, sp, a.max_clen));
     } else if (is_dp(MEAS)) {
       TSIM_TRY(launch_dp(ctx, dp64, 32, 1, r, a.max_clen));
     } else {
@@ -1643,6 +1709,10 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   stage_begin(ctx, TSIM_STAGE_FILTER);
   thresh_kernel<MEAS><<<(nq + 3) / 4, 128, 0, s>>>(a);
   qtable_global_kernel<<<nq, 256, 0, s>>>(a, MEAS == M_EUCLID);  // segment bounds
+  if (MEAS == M_LCSS && a.qenv) {
+    lcss_env_kernel<<<nq, 256, 0, s>>>(a);
+    launched(ctx);
+  }
   launched(ctx);
   compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
   segfilter_kernel<MEAS><<<dim3(std::max(1, std::min(1024, (8 * ctx->num_sms + nq - 1) / nq)), nq),
@@ -1797,6 +1867,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
   a.max_clen = db->max_len;
   a.max_qlen = max_qlen;
   a.tstride = qtable_stride(max_qlen);
+  a.env_stride = (p->measure == TSIM_LCSS && p->delta >= 0) ? max_qlen + p->delta + 1 : 0;
   a.k = k;
   a.S = std::min(C, std::min(64, std::max(2 * k, 16)));
   a.M = std::min(64, std::max(2 * k, 32));
@@ -1876,6 +1947,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
                 align256(sizeof(float) * nqC) + align256(sizeof(int2) * nq * a.M) +
                 align256(sizeof(float) * nq * a.M) + 2 * align256(sizeof(float) * (nq + 1)) +
                 align256(sizeof(float4) * (size_t)nq * a.tstride) +
+                align256(sizeof(float4) * (size_t)nq * a.env_stride) +
                 align256(sizeof(double2) * (size_t)nq * (max_qlen + 1)) +
                 align256(sizeof(float4) * (size_t)nq * kQBlocks) +
                 5 * align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 5 * 256;
@@ -1946,6 +2018,7 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.thr2 = arena_take<float>(ctx, nq + 1);
   a.fcnt = arena_take<int>(ctx, nq + 1);
   a.qtab = arena_take<float4>(ctx, (size_t)nq * a.tstride);
+  a.qenv = a.env_stride ? arena_take<float4>(ctx, (size_t)nq * a.env_stride) : nullptr;
   a.qpre = arena_take<double2>(ctx, (size_t)nq * (max_qlen + 1));
   a.qblk = arena_take<float4>(ctx, (size_t)nq * kQBlocks);
   a.spill = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));

@@ -321,8 +321,9 @@ int launch_dp(tsim_ctx* ctx, int kind, int G, int R, const DpArgs& a, int max_m)
 // bounds the candidate length (shared-memory staging).  warps: 1 = a warp
 // per pair (R up to 16), > 1 = a CTA of 8 warps per pair (R up to 4; for few,
 // long, full-row pairs, where the latency of one pair is the launch's).
+// rmax > 0 caps the chain's R (pairs needing more rows go to spill).
 int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, int* spill,
-                   int* nspill, int* tmp, int* ntmp, int warps = 1);
+                   int* nspill, int* tmp, int* ntmp, int warps = 1, int rmax = 0);
 // Band-relative anti-diagonal kernel (dp_wave.cu) for DTW and Frechet, FP32
 // and compensated (wave_kind): a warp per pair, lane p holding the p-th live
 // cells of the anti-diagonal, passes with R = 1 and 2 cells per lane; pairs
