@@ -624,6 +624,41 @@ SERVING = dict(workload="serving_mixed_measures", db_trajectories=1_000_000, db_
                seed=77)
 
 
+SHARED_REQUESTS = 300
+
+
+def shared_thresholds_leg(T, S, ctx, db, reqs, w):
+    """Repeated queries with and without TSIM_FLAG_SHARE_THRESHOLDS: each of
+    ``reqs`` is served once (which fills the server's threshold cache when
+    the flag is on), then the same requests again; the second pass's device
+    time per request and capacity, with the flag against without, and
+    whether the answers agree."""
+    from cudaruntime1_gb300 import api
+    out = {}
+    answers = {}
+    for name, flags in (("without", 0), ("with", api.FLAG_SHARE_THRESHOLDS)):
+        with T.Server(ctx, db, slots=w["slots"], hbm_budget_bytes=w["hbm_budget_bytes"]) as srv:
+            S.run_closed_loop(srv, reqs, w["k"], flags=flags)
+            tickets = [srv.submit(qp, qo, m, w["k"], flags=flags, **S.MEASURE_PARAMS[m])
+                       for m, qp, qo in reqs]
+            t0 = time.perf_counter()
+            res = [srv.wait(t) for t in tickets]
+            span = time.perf_counter() - t0
+            st = srv.stats()
+        answers[name] = res
+        dms = [info["device_ms"] for _, _, info in res]
+        out[name] = {"device_ms_mean": float(np.mean(dms)), "device_ms_p50": float(np.median(dms)),
+                     "capacity_rps": len(reqs) / span,
+                     "shared_threshold_hits": st["shared_threshold_hits"]}
+    out["device_ms_ratio"] = out["with"]["device_ms_mean"] / out["without"]["device_ms_mean"]
+    out["answers_identical"] = all(
+        np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        for a, b in zip(answers["without"], answers["with"]))
+    out["what"] = (f"the first {len(reqs)} open-loop requests served twice on one server (closed "
+                   "loop); figures are the second pass, whose queries all repeat")
+    return out
+
+
 def serving_workload(args):
     """Serving loop: a resident 1M-trajectory database, Poisson arrivals of
     single-query kNN requests of uniformly drawn measures and lengths,
@@ -662,6 +697,7 @@ def serving_workload(args):
             opened = S.run_open_loop(srv, reqs, w["offered_rps"], w["k"], seed=w["seed"] + 3,
                                      keep=set(keep.values()), kept=kept)
         st = srv.stats()
+    shared = shared_thresholds_leg(T, S, ctx, db, reqs[:SHARED_REQUESTS], w)
     dev_bytes = db.device_bytes()
     db.close()
     ctx.close()
@@ -672,6 +708,7 @@ def serving_workload(args):
             "latency_ms": {"p50": opened["p50_ms"], "p99": opened["p99_ms"],
                            "mean": opened["mean_ms"]},
             "open_loop": opened, "closed_loop_capacity": closed, "server": st,
+            "shared_thresholds": shared,
             "db_build_s": gen_s, "db_device_bytes": dev_bytes, "clocks": clk.summary()}
     if not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))

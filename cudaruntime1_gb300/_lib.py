@@ -23,7 +23,7 @@ TSIM_ERR_BUDGET, TSIM_PENDING, TSIM_ERR_BUSY = 6, 7, 8
 DTW, LCSS, FRECHET, HAUSDORFF, EUCLIDEAN = range(5)
 COST_SQEUCLID, COST_EUCLID = 0, 1
 FLAG_NO_PRUNE, FLAG_PLAIN, FLAG_NO_GRAPH, FLAG_FP64_RESCORE, FLAG_ALWAYS_PRUNE = 1, 2, 4, 8, 16
-FLAG_NO_LANE_DP, FLAG_NO_WAVE_DP = 32, 64
+FLAG_NO_LANE_DP, FLAG_NO_WAVE_DP, FLAG_SHARE_THRESHOLDS = 32, 64, 128
 STAGES = ["summary", "lb1", "seed", "filter", "dp", "select", "rescore", "ref", "dp_survivors"]
 
 _vp = C.c_void_p
@@ -65,7 +65,8 @@ class TsimServerStats(C.Structure):
                 ("rejected", C.c_int64), ("queued", C.c_int), ("in_flight", C.c_int),
                 ("peak_in_flight", C.c_int), ("slots", C.c_int), ("budget_bytes", C.c_int64),
                 ("scratch_in_use", C.c_int64), ("peak_scratch_bytes", C.c_int64),
-                ("launch_ms", C.c_double), ("busy_ms", C.c_double)]
+                ("launch_ms", C.c_double), ("busy_ms", C.c_double),
+                ("shared_threshold_hits", C.c_int64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

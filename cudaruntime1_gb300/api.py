@@ -19,7 +19,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (COST_EUCLID, COST_SQEUCLID, DTW, EUCLIDEAN, FLAG_ALWAYS_PRUNE,  # noqa: F401
-                   FLAG_FP64_RESCORE, FLAG_NO_LANE_DP, FLAG_NO_WAVE_DP,
+                   FLAG_FP64_RESCORE, FLAG_NO_LANE_DP, FLAG_NO_WAVE_DP, FLAG_SHARE_THRESHOLDS,
                    FLAG_NO_GRAPH, FLAG_NO_PRUNE, FLAG_PLAIN, FRECHET, HAUSDORFF, LCSS,
                    TSIM_PENDING, TsimParams, TsimRequestInfo, TsimServerOpts, TsimServerStats,
                    TsimStats, check)

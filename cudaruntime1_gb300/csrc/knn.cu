@@ -119,6 +119,9 @@ struct KArgs {
   int lane_gate;            // survivor rounds of at least this many pairs run a lane per
                             // pair (0: never)
   int lane_ring;            // its ring size (64 or 128)
+  const float* thr_in;      // optional [nq]: a pruning threshold known beforehand (an earlier
+                            //   identical query's), combined with the seeds' (else null)
+  float* thr_out;           // optional [nq]: the final pruning threshold, for later requests
   int* waves;               // what the band-relative kernel leaves to the row-group ones
   int* nwaves;
   int* waves2;              // the list between its two passes
@@ -407,7 +410,12 @@ __global__ void thresh_kernel(KArgs a) {
       const float v = ord2f((unsigned)(kth >> 32));
       t = MEAS == M_LCSS ? -v : widen(v, gamma_dp(MEAS, a.qlen[q], a.max_clen));
     }
-    if (a.noprune) t = MEAS == M_LCSS ? -TSIM_INF : TSIM_INF;
+    if (a.noprune) {
+      t = MEAS == M_LCSS ? -TSIM_INF : TSIM_INF;
+    } else if (a.thr_in) {  // a threshold shared from an earlier identical query
+      const float sv = a.thr_in[q];
+      t = MEAS == M_LCSS ? fmaxf(t, sv) : fminf(t, sv);
+    }
     a.thr[q] = t;
     a.cnt0[q] = 0;
     a.cnt1[q] = 0;
@@ -828,6 +836,15 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
     }
     __syncthreads();
   }
+  // LCSS: the query's window boxes (lcss_env_kernel) in shared memory, next
+  // to the grid: a point's test then reads only its own coordinates from
+  // global memory
+  float4* envs = reinterpret_cast<float4*>(smem_raw + sizeof(uint32_t) * kGridWords);
+  if (MEAS == M_LCSS && a.qenv) {
+    const float4* Eg = a.qenv + (size_t)q * a.env_stride;
+    for (int i = threadIdx.x; i < a.env_stride; i += blockDim.x) envs[i] = Eg[i];
+    __syncthreads();
+  }
   // The warp's pairs e, e + S, ...: a pair's candidate index, then its
   // offset, length and segment bound, are dependent loads; they are issued
   // two and one pairs ahead of the pair being bounded, so their latency
@@ -943,7 +960,7 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
       // (the window's inflated box from the query's row boxes; the whole
       // query's without a window)
       int count = 0;
-      const float4* E = a.qenv ? a.qenv + (size_t)q * a.env_stride : nullptr;
+      const float4* E = a.qenv ? envs : nullptr;
       const float4 qi = make_float4(__fsub_rd(qb.x, e2), __fsub_rd(qb.y, e2), __fadd_ru(qb.z, e2),
                                     __fadd_ru(qb.w, e2));
       const int jend = E ? min(m, a.env_stride) : m;  // columns past n-1+delta match nothing
@@ -1219,6 +1236,18 @@ __global__ void __launch_bounds__(kSelThreads) final_select_kernel(KArgs a) {
   const int q = blockIdx.x;
   const int ns = (a.S + a.M + a.fcnt[q] + kSeg - 1) / kSeg;
   block_select_k(a.segkeys + (size_t)q * a.nseg * 64, ns * a.k, a.k, sel, red);
+  if (a.thr_out && threadIdx.x == 0) {
+    // the query's final threshold: its k-th refined value (widened by the
+    // FP32 error bound; LCSS: the k-th count), valid for any later request
+    // with the same query, parameters and database (none: +inf / 0)
+    const unsigned long long kk = sel[a.k - 1];
+    float t = MEAS == M_LCSS ? 0.0f : TSIM_INF;
+    if (key_index(kk) >= 0) {
+      const float v = ord2f((unsigned)(kk >> 32));
+      t = MEAS == M_LCSS ? -v : widen(v, gamma_dp(MEAS, a.qlen[q], a.max_clen));
+    }
+    a.thr_out[q] = t;
+  }
   if (MEAS == M_LCSS) {
     for (int i = threadIdx.x; i < a.k; i += kSelThreads) {
       int c = key_index(sel[i]);
@@ -1723,11 +1752,16 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   // CTAs per query of the grid-stride filter kernels: about 8 per SM over the
   // whole request, so a single query against a large database fills the GPU
   const int ch = std::max(1, std::min(65535, (8 * ctx->num_sms + nq - 1) / nq));
-  const size_t lb2_smem = MEAS == M_LCSS ? sizeof(uint32_t) * kGridWords : 0;
+  // LCSS: the query's grid and window boxes per CTA, and 4x the CTAs per
+  // query (its queries' pair counts vary widely; a CTA's set-up is small)
+  const size_t lb2_smem =
+      MEAS == M_LCSS ? sizeof(uint32_t) * kGridWords + sizeof(float4) * (size_t)a.env_stride : 0;
+  const int ch2 = MEAS == M_LCSS ? std::max(1, std::min(65535, (32 * ctx->num_sms + nq - 1) / nq))
+                                 : ch;
   if (lb2_smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(lb2_kernel<MEAS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)lb2_smem));
-  lb2_kernel<MEAS><<<dim3(ch, nq), kLb2Warps * 32, lb2_smem, s>>>(a);
+  lb2_kernel<MEAS><<<dim3(ch2, nq), kLb2Warps * 32, lb2_smem, s>>>(a);
   seg_select_kernel<MEAS, 0><<<dim3(a.nseg, nq), kSelThreads, 0, s>>>(a, a.M);
   r1_select_kernel<MEAS><<<nq, kSelThreads, 0, s>>>(a);
   TSIM_CUDA(cudaGetLastError());
@@ -1962,10 +1996,13 @@ size_t knn_scratch_bytes(const tsim_params* p, int nq, int max_qlen, const tsim_
 }
 
 int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
-        int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st) {
+        int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st,
+        const float* thr_in, float* thr_out) {
   TSIM_CHECK_ARG(db->count >= 1, "database is empty");
   KArgs a{};
   const size_t need = knn_plan(p, nq, max_qlen, db, a);
+  a.thr_in = thr_in;
+  a.thr_out = thr_out;
   if (ctx->rdiag_override >= 0 && !a.plain && !a.noprune) a.rdiag = ctx->rdiag_override;
   TSIM_CHECK_ARG((size_t)a.nch * a.T * sizeof(unsigned long long) <= 200 * 1024,
                  "database too large for one request (seed selection)");

@@ -112,9 +112,21 @@ struct Slot {
   std::vector<Request*> batch;  // empty: the slot is free
   std::vector<int> first_q;     // each request's first query in the batch
   int nq = 0, max_qlen = 0, qb = 0;
-  size_t o_off = 0, o_ids = 0, o_dists = 0, staging = 0, scratch = 0;
+  size_t o_off = 0, o_thr_in = 0, o_ids = 0, o_dists = 0, o_thr_out = 0, staging = 0, scratch = 0;
   size_t off = 0, bytes = 0;
+  bool share = false;  // the batch shares pruning thresholds (TSIM_FLAG_SHARE_THRESHOLDS)
 };
+
+// Key of one query under one parameter set: the parameters that shape its
+// answer and its points' bytes.
+std::string share_key(const tsim_params& p, const tsim_point* pts, int64_t count) {
+  std::string k;
+  const int head[5] = {p.measure, p.k, p.cost, p.band_pct, p.delta};
+  k.append(reinterpret_cast<const char*>(head), sizeof(head));
+  k.append(reinterpret_cast<const char*>(&p.epsilon), sizeof(p.epsilon));
+  k.append(reinterpret_cast<const char*>(pts), sizeof(tsim_point) * (size_t)count);
+  return k;
+}
 
 bool same_params(const tsim_params& a, const tsim_params& b) {
   return a.measure == b.measure && a.k == b.k && a.cost == b.cost && a.band_pct == b.band_pct &&
@@ -142,6 +154,11 @@ struct tsim_server {
   int in_flight = 0, peak_in_flight = 0;
   size_t in_use = 0, peak_in_use = 0;
   double launch_ms = 0.0, busy_ms = 0.0;
+  // pruning thresholds of completed queries (TSIM_FLAG_SHARE_THRESHOLDS),
+  // keyed by parameters and query points, oldest evicted first (worker only)
+  std::unordered_map<std::string, float> shared;
+  std::deque<std::string> shared_order;
+  int64_t shared_hits = 0;
   std::thread worker;
 };
 
@@ -150,6 +167,13 @@ namespace {
 
 // Lay out a batch's staging (queries, offsets, ids, distances) and size its
 // pipeline scratch.
+constexpr size_t kSharedCap = 65536;  // queries whose thresholds the server keeps
+
+void sl_hits(tsim_server* s, int hits) {
+  std::lock_guard<std::mutex> g(s->mu);
+  s->shared_hits += hits;
+}
+
 void plan_batch(tsim_server* s, Slot& sl) {
   const tsim_params& p = sl.batch[0]->p;
   sl.first_q.clear();
@@ -165,10 +189,15 @@ void plan_batch(tsim_server* s, Slot& sl) {
   const int64_t kMaxPairs = int64_t(1) << 24;
   sl.qb = (int)std::max<int64_t>(1, std::min<int64_t>(sl.nq, kMaxPairs / std::max(s->db->count, 1)));
   sl.scratch = align256(knn_scratch_bytes(&p, sl.qb, sl.max_qlen, s->db));
+  // staging: queries, offsets, shared thresholds in (copied to the device);
+  // ids, distances, thresholds out (copied back)
+  sl.share = (p.flags & TSIM_FLAG_SHARE_THRESHOLDS) != 0;
   sl.o_off = align256(sizeof(tsim_point) * npts);
-  sl.o_ids = sl.o_off + align256(sizeof(int64_t) * (sl.nq + 1));
+  sl.o_thr_in = sl.o_off + align256(sizeof(int64_t) * (sl.nq + 1));
+  sl.o_ids = sl.o_thr_in + (sl.share ? align256(sizeof(float) * sl.nq) : 0);
   sl.o_dists = sl.o_ids + align256(sizeof(int) * (size_t)sl.nq * p.k);
-  sl.staging = sl.o_dists + align256(sizeof(float) * (size_t)sl.nq * p.k);
+  sl.o_thr_out = sl.o_dists + align256(sizeof(float) * (size_t)sl.nq * p.k);
+  sl.staging = sl.o_thr_out + (sl.share ? align256(sizeof(float) * sl.nq) : 0);
   sl.bytes = sl.staging + sl.scratch;
 }
 
@@ -189,12 +218,24 @@ int launch(tsim_server* s, Slot& sl) {
   size_t pt = 0;
   int qi = 0;
   hoff[0] = 0;
+  float* hthr = reinterpret_cast<float*>(sl.pinned + sl.o_thr_in);
+  int hits = 0;
   for (Request* r : sl.batch) {
     memcpy(sl.pinned + sizeof(tsim_point) * pt, r->pts.data(), sizeof(tsim_point) * r->pts.size());
-    for (int i = 0; i < r->nq; ++i) hoff[qi + i + 1] = (int64_t)pt + r->off[i + 1];
+    for (int i = 0; i < r->nq; ++i) {
+      hoff[qi + i + 1] = (int64_t)pt + r->off[i + 1];
+      if (sl.share) {  // an earlier identical query's threshold, else none
+        const auto it = s->shared.find(share_key(r->p, r->pts.data() + r->off[i],
+                                                 r->off[i + 1] - r->off[i]));
+        const bool hit = it != s->shared.end();
+        hits += hit;
+        hthr[qi + i] = hit ? it->second : (r->p.measure == TSIM_LCSS ? 0.0f : HUGE_VALF);
+      }
+    }
     pt += r->pts.size();
     qi += r->nq;
   }
+  sl_hits(s, hits);
   TSIM_CUDA(cudaMemcpyAsync(base, sl.pinned, sl.o_ids, cudaMemcpyHostToDevice, c->stream));
   c->arena = base + sl.staging;
   c->arena_cap = sl.scratch;
@@ -206,10 +247,13 @@ int launch(tsim_server* s, Slot& sl) {
   int* ids = reinterpret_cast<int*>(base + sl.o_ids);
   float* dists = reinterpret_cast<float*>(base + sl.o_dists);
   const int k = p.k;
+  const float* thr_in = sl.share ? reinterpret_cast<const float*>(base + sl.o_thr_in) : nullptr;
+  float* thr_out = sl.share ? reinterpret_cast<float*>(base + sl.o_thr_out) : nullptr;
   for (int q0 = 0; q0 < sl.nq; q0 += sl.qb) {
     const int nb = std::min(sl.qb, sl.nq - q0);
     TSIM_TRY(knn(c, &p, qpts, qoff + q0, nb, sl.max_qlen, s->db, ids + (size_t)q0 * k,
-                 dists + (size_t)q0 * k, nullptr, nullptr));
+                 dists + (size_t)q0 * k, nullptr, nullptr, thr_in ? thr_in + q0 : nullptr,
+                 thr_out ? thr_out + q0 : nullptr));
   }
   TSIM_CUDA(cudaEventRecord(sl.t1, c->stream));
   TSIM_CUDA(cudaMemcpyAsync(sl.pinned + sl.o_ids, base + sl.o_ids, sl.staging - sl.o_ids,
@@ -233,6 +277,24 @@ void finish(tsim_server* s, Slot& sl, int status, const std::string& err) {
       memcpy(r->dists.data(), sl.pinned + sl.o_dists + sizeof(float) * at, sizeof(float) * nk);
       r->device_ms = dms;
       ++s->completed;
+      if (sl.share) {  // the queries' final thresholds, for later identical queries
+        const float* t = reinterpret_cast<const float*>(sl.pinned + sl.o_thr_out) + sl.first_q[b];
+        for (int i = 0; i < r->nq; ++i) {
+          std::string key = share_key(r->p, r->pts.data() + r->off[i], r->off[i + 1] - r->off[i]);
+          auto it = s->shared.find(key);
+          if (it != s->shared.end()) {
+            it->second = r->p.measure == TSIM_LCSS ? std::max(it->second, t[i])
+                                                   : std::min(it->second, t[i]);
+            continue;
+          }
+          if (s->shared_order.size() >= kSharedCap) {  // evict the oldest
+            s->shared.erase(s->shared_order.front());
+            s->shared_order.pop_front();
+          }
+          s->shared_order.push_back(key);
+          s->shared.emplace(std::move(key), t[i]);
+        }
+      }
     } else {
       r->error = err;
       ++s->failed;
@@ -506,6 +568,7 @@ extern "C" int tsim_server_get_stats(tsim_server* s, tsim_server_stats* st) {
   st->peak_scratch_bytes = (int64_t)s->peak_in_use;
   st->launch_ms = s->launch_ms;
   st->busy_ms = s->busy_ms;
+  st->shared_threshold_hits = s->shared_hits;
   return TSIM_OK;
 }
 

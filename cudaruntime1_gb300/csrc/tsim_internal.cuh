@@ -284,8 +284,11 @@ int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
                 float* d_dists, double* d_dists64, tsim_stats* stats);
 // scratch bytes one knn() call carves from the arena
 size_t knn_scratch_bytes(const tsim_params* p, int nq, int max_qlen, const tsim_db* db);
+// thr_in / thr_out (optional, [nq]): pruning thresholds known beforehand
+// (an earlier identical query's), and the final ones for later requests
 int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* qoff, int nq,
-        int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st);
+        int max_qlen, tsim_db* db, int* ids, float* dists, double* dists64, tsim_stats* st,
+        const float* thr_in = nullptr, float* thr_out = nullptr);
 // reference-semantics batch: scratch size and the call on caller-given scratch
 size_t ref_scratch_bytes(int num_t, int m, bool* keys_in_smem);
 int ref_batch_core(tsim_ctx* ctx, int measure, const float2* d_t1, const float2* d_t2, int num_t,

@@ -114,11 +114,13 @@ def run_open_loop(server, requests, rate: float, k: int = 10, seed: int = 0, kee
     return summarize(infos, span, offered=rate)
 
 
-def run_closed_loop(server, requests, k: int = 10):
+def run_closed_loop(server, requests, k: int = 10, flags: int = 0):
     """Submit everything at once (the queue keeps every slot busy): the
-    server's capacity in requests/s."""
+    server's capacity in requests/s.  ``flags``: TSIM_FLAG_* added to every
+    request."""
     t0 = time.perf_counter()
-    tickets = [server.submit(qp, qo, m, k, **MEASURE_PARAMS[m]) for m, qp, qo in requests]
+    tickets = [server.submit(qp, qo, m, k, flags=flags, **MEASURE_PARAMS[m])
+               for m, qp, qo in requests]
     infos = []
     for i, t in enumerate(tickets):
         _, _, info = server.wait(t)

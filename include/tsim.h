@@ -82,6 +82,11 @@ typedef enum tsim_cost {
 #define TSIM_FLAG_NO_WAVE_DP 0x40u  /* DTW / Frechet rounds skip the band-relative DP
                                        kernel (lanes along the anti-diagonal) and start
                                        on the row-group ones; same values */
+#define TSIM_FLAG_SHARE_THRESHOLDS 0x80u /* server requests: a query's pruning threshold
+                                             starts from the final one of an earlier
+                                             identical query (same parameters, points and
+                                             database), so repeated queries prune at once;
+                                             same answers */
 
 typedef struct tsim_params {
   int measure;    /* tsim_measure */
@@ -276,6 +281,8 @@ typedef struct tsim_server_stats {
   int64_t budget_bytes, scratch_in_use, peak_scratch_bytes;
   double launch_ms;   /* host time the worker spent enqueueing requests */
   double busy_ms;     /* host time the worker spent on anything but waiting */
+  int64_t shared_threshold_hits; /* queries that started from an earlier identical query's
+                                    threshold (TSIM_FLAG_SHARE_THRESHOLDS) */
 } tsim_server_stats;
 
 TSIM_API int tsim_server_create(tsim_ctx* ctx, tsim_db* db, const tsim_server_opts* opts,

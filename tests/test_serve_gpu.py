@@ -114,3 +114,35 @@ def test_wait_timeout_and_destroy_with_pending(tsim, cuda_ctx, served_db):
     first = srv.wait(tickets[0])
     assert first[2]["status"] == 0
     srv.close()  # finishes the request in flight, fails the queued ones
+
+
+def test_shared_thresholds_same_answers(tsim, cuda_ctx, oracle, served_db):
+    """TSIM_FLAG_SHARE_THRESHOLDS: the server keeps each completed query's
+    final pruning threshold and starts a later identical query (same
+    parameters and points) from it.  Repeated requests then report shared
+    hits and return the same ids and distances as the requests run alone
+    (the shared threshold bounds the k-th distance from above, so no true
+    neighbour is pruned); distinct queries are untouched."""
+    cp, co, db = served_db
+    reqs = _requests(15, 17)
+    k = 10
+    share = tsim.api.FLAG_SHARE_THRESHOLDS
+    alone = [tsim.knn(cuda_ctx, db, qp, qo, m, k, stats=False, **PARAMS[m]) for m, qp, qo in reqs]
+    with tsim.Server(cuda_ctx, db, slots=4, hbm_budget_bytes=512 << 20) as srv:
+        first = [srv.wait(srv.submit(qp, qo, m, k, flags=share, **PARAMS[m])) for m, qp, qo in reqs]
+        st1 = srv.stats()
+        again = [srv.submit(qp, qo, m, k, flags=share, **PARAMS[m]) for m, qp, qo in reqs]
+        second = [srv.wait(t) for t in again]
+        st2 = srv.stats()
+        # a query never seen before gets no shared threshold
+        _, qn, on = _requests(1, 99)[0]
+        srv.wait(srv.submit(qn, on, "dtw", k, flags=share, **PARAMS["dtw"]))
+        st3 = srv.stats()
+    nq = sum(len(qo) - 1 for _, _, qo in reqs)
+    assert st1["shared_threshold_hits"] == 0
+    assert st2["shared_threshold_hits"] == nq
+    assert st3["shared_threshold_hits"] == nq
+    for (m, qp, qo), (ia, da, _), (i1, d1, f1), (i2, d2, f2) in zip(reqs, alone, first, second):
+        assert f1["status"] == 0 and f2["status"] == 0
+        assert np.array_equal(ia, i1) and np.array_equal(ia, i2), m
+        assert np.array_equal(da, d1) and np.array_equal(da, d2), m
