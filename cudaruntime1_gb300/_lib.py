@@ -96,13 +96,17 @@ def load(build_if_missing: bool = False):
     with _LOCK:
         if _LIB is not None:
             return _LIB
-        if not os.path.exists(_build.LIB):
+        path = os.environ.get("TSIM_LIB") or _build.LIB  # e.g. the bounds-checked build
+        if path != _build.LIB:
+            if not os.path.exists(path):
+                raise RuntimeError(f"TSIM_LIB={path} does not exist")
+        elif not os.path.exists(_build.LIB):
             if not build_if_missing:
                 raise RuntimeError(
                     f"{_build.LIB} is not built: run cudaruntime1_gb300.build() "
                     "(nvcc, sm_103a); there is no CPU fallback")
             _build.build()
-        L = C.CDLL(_build.LIB)
+        L = C.CDLL(path)
         sig = {
             "tsim_status_string": ([C.c_int], C.c_char_p),
             "tsim_last_error": ([], C.c_char_p),
@@ -137,6 +141,8 @@ def load(build_if_missing: bool = False):
             "tsim_probe_fp32_tflops": ([_vp, C.POINTER(C.c_double)], C.c_int),
             "tsim_debug_fail_allocations": ([C.c_int, C.c_int], C.c_int),
             "tsim_debug_set_canary": ([C.c_int], C.c_int),
+            "tsim_debug_bounds_violations": ([C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+                                             C.c_int),
             "tsim_ctx_set_concurrency": ([_vp, C.c_int], C.c_int),
             "tsim_ctx_survivor_cells": ([_vp, C.POINTER(C.c_int64)], C.c_int),
             "tsim_band_cells": ([_vp, C.POINTER(TsimParams), _vp, _vp, C.c_int, _vp,

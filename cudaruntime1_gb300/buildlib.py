@@ -18,6 +18,9 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libtsim.so")
+# the bounds-checked build (TSIM_DEBUG_BOUNDS): tests only, built on demand
+DEBUG_BUILD = os.path.join(PKG, "_build_debug")
+DEBUG_LIB = os.path.join(PKG, "libtsim_debug.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -44,15 +47,15 @@ def _deps():
         glob.glob(os.path.join(ROOT, "include", "compat", "*.cuh"))
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+def up_to_date(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
-def _compile(src: str, extra) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+def _compile(src: str, extra, build_dir: str = BUILD) -> str:
+    obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
     cmd = [nvcc()] + common_flags() + list(extra) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -60,23 +63,27 @@ def _compile(src: str, extra) -> str:
     return obj
 
 
-def build(force: bool = False, verbose: bool = False, extra=()) -> str:
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, extra=(), debug_bounds: bool = False) -> str:
+    """Build libtsim.so, or with ``debug_bounds`` libtsim_debug.so (every
+    shared-memory index of the DP and pairwise kernels checked)."""
+    lib, bdir = (DEBUG_LIB, DEBUG_BUILD) if debug_bounds else (LIB, BUILD)
+    extra = tuple(extra) + (("-DTSIM_DEBUG_BOUNDS",) if debug_bounds else ())
+    if not force and up_to_date(lib):
+        return lib
+    os.makedirs(bdir, exist_ok=True)
     srcs = _sources()
     workers = max(1, min(len(srcs), os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(workers) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
-    tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, extra, bdir), srcs))
+    tmp = lib + ".tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
 
 
 if __name__ == "__main__":

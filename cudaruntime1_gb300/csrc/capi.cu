@@ -6,7 +6,9 @@
 #include <cstring>
 #include <algorithm>
 #include <mutex>
+#include <vector>
 
+#include "debug_bounds.cuh"
 #include "tsim_internal.cuh"
 
 namespace tsim {
@@ -57,6 +59,17 @@ cudaError_t host_alloc(void** p, size_t bytes) {
 }
 
 bool debug_canary() { return g_canary.load() != 0; }
+
+// the bounds-check readers of the translation units (TSIM_DEBUG_BOUNDS
+// build), registered during static initialisation
+static std::vector<BoundsReader>& bounds_readers() {
+  static std::vector<BoundsReader> v;
+  return v;
+}
+int register_bounds_reader(BoundsReader r) {
+  bounds_readers().push_back(r);
+  return 0;
+}
 
 int arena_reserve(tsim_ctx* ctx, size_t bytes) {
   ctx->arena_used = 0;
@@ -345,6 +358,21 @@ extern "C" int tsim_debug_fail_allocations(int skip, int count) {
   tsim::g_fail_count.store(0);  // disarmed while the new values go in
   tsim::g_fail_skip.store(skip);
   tsim::g_fail_count.store(count);
+  return TSIM_OK;
+}
+
+extern "C" int tsim_debug_bounds_violations(int64_t* count, int64_t* first) {
+  TSIM_CHECK_ARG(count != nullptr, "count is NULL");
+#ifdef TSIM_DEBUG_BOUNDS
+  unsigned long long n = 0;
+  long long f = 0;
+  for (tsim::BoundsReader r : tsim::bounds_readers()) TSIM_CUDA(r(&n, &f));
+  *count = (int64_t)n;
+  if (first) *first = (int64_t)f;
+#else
+  *count = -1;  // built without the checks
+  if (first) *first = 0;
+#endif
   return TSIM_OK;
 }
 

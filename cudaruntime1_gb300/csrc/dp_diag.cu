@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "bounds.cuh"
+#include "debug_bounds.cuh"
 #include "dp_policies.cuh"
 #include "dp_ramps.cuh"
 
@@ -159,12 +160,12 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
     if (W == 1) {
       __syncwarp();
       if (staged)
-        for (int j = lane; j < m; j += 32) cs[j] = __ldg(B + j);
+        for (int j = lane; j < m; j += 32) cs[TSIM_SIDX(j, col_cap)] = __ldg(B + j);
       __syncwarp();
     } else {
       __syncthreads();  // the previous pair is done with the staging and the exchange
       if (staged)
-        for (int j = pl; j < m; j += kLanes) cs[j] = __ldg(B + j);
+        for (int j = pl; j < m; j += kLanes) cs[TSIM_SIDX(j, col_cap)] = __ldg(B + j);
       if (lane == 31) xbuf[0][warp] = xbuf[1][warp] = P::border();
       __syncthreads();
     }
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
           }
           if (lo <= hi) {
             const float4 bx = qtable_box(T, lo, hi);
-            const float2 c = cs[j];
+            const float2 c = cs[TSIM_SIDX(j, col_cap)];
             v = box_pt_d2_rd(bx.x, bx.y, bx.z, bx.w, c.x, c.y);
             if (std::is_same<P, PolDtwEu>::value) v = __fsqrt_rd(v);
           } else {
@@ -221,16 +222,16 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
           if (lane + o < 32) v = __fadd_rd(v, u);
         }
         v = __fadd_rd(v, carry);
-        if (j < m) sfx[j] = v;
+        if (j < m) sfx[TSIM_SIDX(j, sfx_cap)] = v;
         carry = __shfl_sync(0xffffffffu, v, 0);
       }
-      if (lane == 0) sfx[m] = 0.0f;
+      if (lane == 0) sfx[TSIM_SIDX(m, sfx_cap)] = 0.0f;
       __syncwarp();
       for (int c = lane; c <= (t_last >> 4); c += 32) {
         const int t = 16 * c + 15;  // the largest column of anti-diagonals t-1, t
         int jmax = min(t, m - 1);
         if (wband >= 0) jmax = min(jmax, floordiv_i((long long)t * (m - 1) + wband, n + m - 2));
-        chk[c] = sfx[jmax + 1];
+        chk[TSIM_SIDX(c, chk_cap)] = sfx[TSIM_SIDX(jmax + 1, sfx_cap)];
       }
       __syncwarp();
       const float shrink = __fsub_rd(1.0f, __fmul_ru((float)(n + m + 8), 6.03e-8f));
@@ -380,7 +381,7 @@ __global__ void __launch_bounds__(W == 1 ? kDiagThreads : 32 * W,
         if ((t & 15) == 15) {
           const float two = fminf(mstep, prev);
           float lb = __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(two)));
-          if (suffix) lb = __fadd_rd(lb, chk[t >> 4]);  // plus the remaining columns
+          if (suffix) lb = __fadd_rd(lb, chk[TSIM_SIDX(t >> 4, chk_cap)]);  // plus the remaining columns
           if (W > 1) {  // over the pair's warps (reads after this step's barrier)
             if (lane == 0) xred[warp] = lb;
             if (lane == 31) xbuf[t & 1][warp] = out;

@@ -19,6 +19,7 @@
 // lcss_refine_kernel_m_1 (lcss.cu:46-111), frechet_refine_kernel_m
 // (frechet.cu:44-117): one CTA per pair, one barrier per anti-diagonal, every
 // point re-read from global memory per cell.
+#include "debug_bounds.cuh"
 #include "dp_policies.cuh"
 
 namespace tsim {
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
           prev_up = P::origin();
         else {
           int x = rlo - 1;
-          prev_up = (x >= prev_lo && x <= prev_hi) ? buf[x] : P::border();
+          prev_up = (x >= prev_lo && x <= prev_hi) ? buf[TSIM_SIDX(x, a.buf_len)] : P::border();
         }
       }
       float bmin = TSIM_INF;
@@ -132,7 +133,7 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
       for (int s = 0; s < Smax; ++s) {
         const int j = rlo + s - sl;
         V up = shfl_up_seg(outv, G);
-        if (sl == 0) up = (r > 0 && j >= prev_lo && j <= prev_hi) ? buf[j] : P::border();
+        if (sl == 0) up = (r > 0 && j >= prev_lo && j <= prev_hi) ? buf[TSIM_SIDX(j, a.buf_len)] : P::border();
         const V diag = prev_up;
         prev_up = up;
         if (s < S && j >= rlo && j <= rhi) {
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(kDpThreads) dp_pairs_kernel(DpArgs a) {
             left[k] = v;
           }
           outv = u;
-          if (sl == G - 1) buf[j] = outv;
+          if (sl == G - 1) buf[TSIM_SIDX(j, a.buf_len)] = outv;
           if (P::kMin) bmin = fminf(bmin, vf(outv));
         }
       }

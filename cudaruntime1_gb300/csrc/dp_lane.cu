@@ -46,6 +46,7 @@
 // barriers per anti-diagonal.
 #include <type_traits>
 
+#include "debug_bounds.cuh"
 #include "dp_policies.cuh"
 #include "dp_ramps.cuh"
 
@@ -73,7 +74,9 @@ __global__ void __launch_bounds__(kLaneThreads, 3)
   constexpr bool kLcss = !P::kMin;
   constexpr int R = kLaneR;
   extern __shared__ __align__(16) unsigned char lane_smem[];
-  V* ring = reinterpret_cast<V*>(lane_smem) + threadIdx.x;  // slot s: ring[s * kLaneThreads]
+  // slot s of this lane's ring: ring[RSLOT(s)]
+  V* ring = reinterpret_cast<V*>(lane_smem);
+#define RSLOT(s) TSIM_SIDX(((s) & (RING - 1)) * kLaneThreads + (int)threadIdx.x, RING * kLaneThreads)
   const int npairs = a.npairs_dev ? min(*a.npairs_dev, a.npairs) : a.npairs;
   const int T = gridDim.x * kLaneThreads;
   const bool check = P::kMin && a.thr != nullptr;
@@ -193,9 +196,9 @@ __global__ void __launch_bounds__(kLaneThreads, 3)
     if (o0 == 0)
       U[0] = P::origin();
     else if (o0 > 0 && ulo - 1 >= pulo && ulo - 1 <= puhi)
-      U[0] = ring[((ulo - 1) & (RING - 1)) * kLaneThreads];
+      U[0] = ring[RSLOT(ulo - 1)];
     int j0 = ulo;  // row 0's column
-    V upv = j0 <= puhi ? ring[(j0 & (RING - 1)) * kLaneThreads] : P::border();
+    V upv = j0 <= puhi ? ring[RSLOT(j0)] : P::border();
     float bmin = TSIM_INF;
 
     // One step: R cells, then row R-1's value to the ring.  MASK: test every
@@ -206,7 +209,7 @@ __global__ void __launch_bounds__(kLaneThreads, 3)
       constexpr bool MASK = decltype(mask_tag)::value;
       const int jn = j0 + 1;  // the next step's inputs, ahead of this step's cells
       const float2 cpn = __ldg(I + min(jn, ni - 1));
-      const V upn = ring[(jn & (RING - 1)) * kLaneThreads];
+      const V upn = ring[RSLOT(jn)];
 #pragma unroll
       for (int k = R - 1; k >= 0; --k) {
         const V up = k > 0 ? L[k > 0 ? k - 1 : 0] : upv;
@@ -216,7 +219,7 @@ __global__ void __launch_bounds__(kLaneThreads, 3)
         U[k] = up;
         L[k] = v;
       }
-      if (!MASK || s >= R - 1) ring[((j0 - (R - 1)) & (RING - 1)) * kLaneThreads] = L[R - 1];
+      if (!MASK || s >= R - 1) ring[RSLOT(j0 - (R - 1))] = L[R - 1];
       if (P::kMin) bmin = fminf(bmin, vf(L[R - 1]));
 #pragma unroll
       for (int k = R - 1; k > 0; --k) cw[k] = cw[k - 1];
@@ -231,7 +234,7 @@ __global__ void __launch_bounds__(kLaneThreads, 3)
       pulo = ulo;
       puhi = uhi;
       if (o0 + R >= no) {  // the last row: its last band column holds the result
-        store_result(a, pid, ring[(uhi & (RING - 1)) * kLaneThreads]);
+        store_result(a, pid, ring[RSLOT(uhi)]);
         have = false;
       } else if (check && bmin > thr) {
         store_result(a, pid, P::border());
@@ -246,6 +249,8 @@ __global__ void __launch_bounds__(kLaneThreads, 3)
     if ((threadIdx.x & 31) == 0 && cells) atomicAdd(a.cells, (unsigned long long)cells);
   }
 }
+
+#undef RSLOT
 
 template <class P, int RING>
 int launch_lane_one(tsim_ctx* ctx, const DpArgs& a, int* spill, int* nspill, int gate) {

@@ -38,6 +38,7 @@
 // pair, a full anti-diagonal of threads and two barriers per step.
 #include <vector>
 
+#include "debug_bounds.cuh"
 #include "dp_policies.cuh"
 
 namespace tsim {
@@ -76,12 +77,176 @@ __host__ __device__ inline size_t wave_per_warp(int qcap, int ccap, int tcap) {
   return (size_t)(qcap + kWavePad) + (ccap + 2 * kWavePad) + tcap / 2;
 }
 
+// shared-memory views of the staged pair: query points [0, qcap + pad),
+// candidate points [-pad, ccap + pad), the anti-diagonal table [0, tcap)
+#define QS(i) qs[TSIM_SIDX(i, qcap + kWavePad)]
+#define CS(j) cs[TSIM_SIDX((j) + kWavePad, ccap + 2 * kWavePad) - kWavePad]
+#define TAB(t) tab[TSIM_SIDX(t, tcap)]
+
+// One pair on the warp, R cells per lane (its widest anti-diagonal fits 32 R).
 template <class P, int R>
+__device__ __forceinline__ void wave_pair(const DpArgs& a, const int pid, const int q, const int n,
+                                          const int m, const int w, const int64_t qo,
+                                          const int64_t co, float2* qs, float2* cs, int* tab,
+                                          const int qcap, const int ccap, const int tcap) {
+  using V = typename P::V;
+  using C = typename P::C;
+  const int lane = threadIdx.x & 31;
+  const bool check = a.thr != nullptr;
+  const int src_dn = (lane + 31) & 31, src_up = (lane + 1) & 31;
+  const int t_end = n + m - 2;
+  const float thr = check ? a.thr[q] : TSIM_INF;
+
+  // the pair's points, and the geometry of every anti-diagonal:
+  // ilo(t) = max(0, t-m+1, ceil((t(n-1) - W) / D)),
+  // ihi(t) = min(n-1, t, floor((t(n-1) + W) / D)),  D = n+m-2,
+  // stepped by 32 anti-diagonals per lane as quotient and remainder
+  __syncwarp();
+  {
+    const float2* A = a.qpts + qo;
+    const float2* B = a.cpts + co;
+    for (int i = lane; i < n; i += 32) QS(i) = __ldg(A + i);
+    for (int j = lane; j < m; j += 32) CS(j) = __ldg(B + j);
+    const int D = t_end;
+    const int W = w < 0 ? -1 : w * (min(n, m) - 1);
+    const int step = 32 * (n - 1), sq = step / D, sr = step % D;
+    // lo numerator shifted by K D (K D > W) to stay non-negative
+    const int K = W < 0 ? 0 : W / D + 1;
+    int lq = 0, lr = 0, hq = 0, hr = 0;
+    if (W >= 0 && lane <= t_end) {
+      const int xl = lane * (n - 1) - W + (D - 1) + K * D, xh = lane * (n - 1) + W;
+      lq = xl / D;
+      lr = xl % D;
+      hq = xh / D;
+      hr = xh % D;
+    }
+    for (int t = lane; t <= t_end; t += 32) {
+      int lo = max(0, t - (m - 1)), hi = min(n - 1, t);
+      if (W >= 0) {
+        lo = max(lo, lq - K);
+        hi = min(hi, hq);
+        lq += sq;
+        lr += sr;
+        if (lr >= D) lr -= D, ++lq;
+        hq += sq;
+        hr += sr;
+        if (hr >= D) hr -= D, ++hq;
+      }
+      TAB(t) = lo | (max(0, hi - lo + 1) << 16);
+    }
+    // two entries past the last anti-diagonal: the step after it reads
+    // them (its cells are never used)
+    if (lane < 2) TAB(t_end + 1 + lane) = (n - 1) | (1 << 16);
+  }
+  __syncwarp();
+
+  // step 0: cell (0, 0) at position 0; every other position outside
+  V v[R], mm[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) v[r] = mm[r] = P::border();
+  if (lane == 0) {
+    const float2 p = QS(0), c = CS(0);
+    v[0] = P::cell(p.x, p.y, c.x, c.y, P::border(), P::border(), P::origin(), a.eps);
+    mm[0] = v[0];  // its left (0, -1) is outside
+  }
+  // costs of the cells of step tt (positions lane R + r), geometry lo
+  auto costs = [&](C* out, int tt, int lo) {
+    const int i0 = lo + lane * R, j0 = tt - lo - lane * R;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const float2 qp = QS(i0 + r), cp = CS(j0 - r);
+      out[r] = P::cost(qp.x, qp.y, cp.x, cp.y);
+    }
+  };
+  C cst[R];
+  int e = TAB(1);   // geometry of the step computed next
+  int e1 = TAB(2);  // and of the one after (the table runs two entries past t_end)
+  costs(cst, 1, e & 0xffff);
+  V edge = P::border();  // lane 0: position 0's diagonal when the next shift is 0
+  int ilo = 0;
+  bool alive = true;
+  // one anti-diagonal: the shuffle, R cells, and the next step's costs
+  // (computed past the last step too: the padding keeps them in bounds)
+  auto step = [&](const int t) {
+    const int nlo = e & 0xffff, L = e >> 16;
+    const int s = nlo - ilo;  // 0 or 1, uniform
+    // across lanes: s = 0 takes M of the lane above's last position, s = 1
+    // V of the lane below's first position
+    const V xin = wshfl(s ? v[0] : mm[R - 1], s ? src_up : src_dn);
+    C cn[R];
+    costs(cn, t + 1, e1 & 0xffff);
+    const int e2 = TAB(t + 2);
+    const V edge_next = s ? v[0] : P::border();
+    V nv[R], nm[R];  // every position reads the last step's values
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const V mdu0 = r > 0 ? mm[r > 0 ? r - 1 : 0] : (lane == 0 ? edge : xin);
+      const V lft1 = r + 1 < R ? v[r + 1 < R ? r + 1 : 0] : (lane == 31 ? P::border() : xin);
+      const V mdu = s ? mm[r] : mdu0;
+      const V lft = s ? lft1 : v[r];
+      const V c = P::combine(cst[r], vmin(mdu, lft));
+      const bool in = lane * R + r < L;
+      nv[r] = in ? c : P::border();
+      nm[r] = in ? vmin(c, lft) : P::border();
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      v[r] = nv[r];
+      mm[r] = nm[r];
+      cst[r] = cn[r];
+    }
+    edge = edge_next;
+    ilo = nlo;
+    e = e1;
+    e1 = e2;
+  };
+  auto lane_min = [&]() {
+    float x = vf(v[0]);
+#pragma unroll
+    for (int r = 1; r < R; ++r) x = fminf(x, vf(v[r]));
+    return x;
+  };
+  // blocks of 16 straight-line steps; after each, the abandon test over
+  // its last two anti-diagonals
+  int t = 1;
+  for (; t + 15 <= t_end; t += 16) {
+    float m14 = TSIM_INF;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      step(t + u);
+      if (u == 14) m14 = lane_min();
+    }
+    if (check) {
+      const float two = fminf(lane_min(), m14);
+      const float lb = __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(two)));
+      if (lb > thr) {  // uniform across the warp
+        alive = false;
+        t += 15;
+        break;
+      }
+    }
+  }
+  if (alive)
+    for (; t <= t_end; ++t) step(t);
+  if (a.cells) {  // cells of the anti-diagonals computed, inside the band
+    const int t_done = alive ? t_end : min(t, t_end);
+    long long cells = 0;
+    for (int u = lane; u <= t_done; u += 32) cells += TAB(u) >> 16;
+    for (int o = 16; o; o >>= 1) cells += __shfl_xor_sync(0xffffffffu, cells, o);
+    if (lane == 0) atomicAdd(a.cells, (unsigned long long)cells);
+  }
+  // the result: cell (n-1, m-1), position 0 of the last anti-diagonal
+  if (lane == 0) store_result(a, pid, alive ? v[0] : P::border());
+}
+
+// RMAX = 1: pairs whose widest anti-diagonal fits 32 lanes; RMAX = 2: every
+// pair up to 64 cells per anti-diagonal, each with the R (1 or 2) it needs --
+// one launch instead of a pass per R (the passes would run one after the
+// other, each as long as its longest pair)
+template <class P, int RMAX>
 __global__ void __launch_bounds__(kWaveThreads)
     dp_wave_kernel(DpArgs a, int qcap, int ccap, int tcap, int* spill, int* nspill) {
   static_assert(P::kMin, "the band-relative kernel serves the minimum measures");
-  using V = typename P::V;
-  using C = typename P::C;
   extern __shared__ __align__(16) float2 wave_smem[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -91,8 +256,6 @@ __global__ void __launch_bounds__(kWaveThreads)
   const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nslots = (gridDim.x * blockDim.x) >> 5;
   const int npairs = a.npairs_dev ? min(*a.npairs_dev, a.npairs) : a.npairs;
-  const bool check = a.thr != nullptr;
-  const int src_dn = (lane + 31) & 31, src_up = (lane + 1) & 31;
 
   for (int wk = slot; wk < npairs; wk += nslots) {
     const int pid = a.order ? a.order[wk] : wk;
@@ -102,155 +265,21 @@ __global__ void __launch_bounds__(kWaveThreads)
     const int64_t qo = a.qoff[q], co = a.coff[pr.y];
     const int n = (int)(a.qoff[q + 1] - qo), m = (int)(a.coff[pr.y + 1] - co);
     const int w = band_w(n, m, a.band_pct);
-    const int t_end = n + m - 2;
-    if (n < 2 || m < 2 || n > qcap || m > ccap || t_end + 3 > tcap || wave_lmax(n, m, w) > 32 * R) {
+    const int lm = wave_lmax(n, m, w);
+    if (n < 2 || m < 2 || n > qcap || m > ccap || n + m + 1 > tcap || lm > 32 * RMAX) {
       if (lane == 0 && spill) spill[atomicAdd(nspill, 1)] = pid;
       continue;
     }
-    const float thr = check ? a.thr[q] : TSIM_INF;
-
-    // the pair's points, and the geometry of every anti-diagonal:
-    // ilo(t) = max(0, t-m+1, ceil((t(n-1) - W) / D)),
-    // ihi(t) = min(n-1, t, floor((t(n-1) + W) / D)),  D = n+m-2,
-    // stepped by 32 anti-diagonals per lane as quotient and remainder
-    __syncwarp();
-    {
-      const float2* A = a.qpts + qo;
-      const float2* B = a.cpts + co;
-      for (int i = lane; i < n; i += 32) qs[i] = __ldg(A + i);
-      for (int j = lane; j < m; j += 32) cs[j] = __ldg(B + j);
-      const int D = t_end;
-      const int W = w < 0 ? -1 : w * (min(n, m) - 1);
-      const int step = 32 * (n - 1), sq = step / D, sr = step % D;
-      // lo numerator shifted by K D (K D > W) to stay non-negative
-      const int K = W < 0 ? 0 : W / D + 1;
-      int lq = 0, lr = 0, hq = 0, hr = 0;
-      if (W >= 0 && lane <= t_end) {
-        const int xl = lane * (n - 1) - W + (D - 1) + K * D, xh = lane * (n - 1) + W;
-        lq = xl / D;
-        lr = xl % D;
-        hq = xh / D;
-        hr = xh % D;
-      }
-      for (int t = lane; t <= t_end; t += 32) {
-        int lo = max(0, t - (m - 1)), hi = min(n - 1, t);
-        if (W >= 0) {
-          lo = max(lo, lq - K);
-          hi = min(hi, hq);
-          lq += sq;
-          lr += sr;
-          if (lr >= D) lr -= D, ++lq;
-          hq += sq;
-          hr += sr;
-          if (hr >= D) hr -= D, ++hq;
-        }
-        tab[t] = lo | (max(0, hi - lo + 1) << 16);
-      }
-      // two entries past the last anti-diagonal: the step after it reads
-      // them (its cells are never used)
-      if (lane < 2) tab[t_end + 1 + lane] = (n - 1) | (1 << 16);
-    }
-    __syncwarp();
-
-    // step 0: cell (0, 0) at position 0; every other position outside
-    V v[R], mm[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = mm[r] = P::border();
-    if (lane == 0) {
-      const float2 p = qs[0], c = cs[0];
-      v[0] = P::cell(p.x, p.y, c.x, c.y, P::border(), P::border(), P::origin(), a.eps);
-      mm[0] = v[0];  // its left (0, -1) is outside
-    }
-    // costs of the cells of step tt (positions lane R + r), geometry lo
-    auto costs = [&](C* out, int tt, int lo) {
-      const int i0 = lo + lane * R, j0 = tt - lo - lane * R;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const float2 qp = qs[i0 + r], cp = cs[j0 - r];
-        out[r] = P::cost(qp.x, qp.y, cp.x, cp.y);
-      }
-    };
-    C cst[R];
-    int e = tab[1];   // geometry of the step computed next
-    int e1 = tab[2];  // and of the one after (the table runs two entries past t_end)
-    costs(cst, 1, e & 0xffff);
-    V edge = P::border();  // lane 0: position 0's diagonal when the next shift is 0
-    int ilo = 0;
-    bool alive = true;
-    // one anti-diagonal: the shuffle, R cells, and the next step's costs
-    // (computed past the last step too: the padding keeps them in bounds)
-    auto step = [&](const int t) {
-      const int nlo = e & 0xffff, L = e >> 16;
-      const int s = nlo - ilo;  // 0 or 1, uniform
-      // across lanes: s = 0 takes M of the lane above's last position, s = 1
-      // V of the lane below's first position
-      const V xin = wshfl(s ? v[0] : mm[R - 1], s ? src_up : src_dn);
-      C cn[R];
-      costs(cn, t + 1, e1 & 0xffff);
-      const int e2 = tab[t + 2];
-      const V edge_next = s ? v[0] : P::border();
-      V nv[R], nm[R];  // every position reads the last step's values
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const V mdu0 = r > 0 ? mm[r > 0 ? r - 1 : 0] : (lane == 0 ? edge : xin);
-        const V lft1 = r + 1 < R ? v[r + 1 < R ? r + 1 : 0] : (lane == 31 ? P::border() : xin);
-        const V mdu = s ? mm[r] : mdu0;
-        const V lft = s ? lft1 : v[r];
-        const V c = P::combine(cst[r], vmin(mdu, lft));
-        const bool in = lane * R + r < L;
-        nv[r] = in ? c : P::border();
-        nm[r] = in ? vmin(c, lft) : P::border();
-      }
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        v[r] = nv[r];
-        mm[r] = nm[r];
-        cst[r] = cn[r];
-      }
-      edge = edge_next;
-      ilo = nlo;
-      e = e1;
-      e1 = e2;
-    };
-    auto lane_min = [&]() {
-      float x = vf(v[0]);
-#pragma unroll
-      for (int r = 1; r < R; ++r) x = fminf(x, vf(v[r]));
-      return x;
-    };
-    // blocks of 16 straight-line steps; after each, the abandon test over
-    // its last two anti-diagonals
-    int t = 1;
-    for (; t + 15 <= t_end; t += 16) {
-      float m14 = TSIM_INF;
-#pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        step(t + u);
-        if (u == 14) m14 = lane_min();
-      }
-      if (check) {
-        const float two = fminf(lane_min(), m14);
-        const float lb = __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(two)));
-        if (lb > thr) {  // uniform across the warp
-          alive = false;
-          t += 15;
-          break;
-        }
-      }
-    }
-    if (alive)
-      for (; t <= t_end; ++t) step(t);
-    if (a.cells) {  // cells of the anti-diagonals computed, inside the band
-      const int t_done = alive ? t_end : min(t, t_end);
-      long long cells = 0;
-      for (int u = lane; u <= t_done; u += 32) cells += tab[u] >> 16;
-      for (int o = 16; o; o >>= 1) cells += __shfl_xor_sync(0xffffffffu, cells, o);
-      if (lane == 0) atomicAdd(a.cells, (unsigned long long)cells);
-    }
-    // the result: cell (n-1, m-1), position 0 of the last anti-diagonal
-    if (lane == 0) store_result(a, pid, alive ? v[0] : P::border());
+    if (RMAX == 1 || lm <= 32)  // uniform across the warp
+      wave_pair<P, 1>(a, pid, q, n, m, w, qo, co, qs, cs, tab, qcap, ccap, tcap);
+    else
+      wave_pair<P, RMAX>(a, pid, q, n, m, w, qo, co, qs, cs, tab, qcap, ccap, tcap);
   }
 }
+
+#undef QS
+#undef CS
+#undef TAB
 
 template <class P, int R>
 int launch_wave_one(tsim_ctx* ctx, const DpArgs& a, int qcap, int ccap, int tcap, int* spill,
@@ -274,36 +303,18 @@ int launch_wave_one(tsim_ctx* ctx, const DpArgs& a, int qcap, int ccap, int tcap
 }
 
 template <class P>
-int wave_chain(tsim_ctx* ctx, const DpArgs& a, int max_n, int max_m, int* spill, int* nspill,
-               int* tmp, int* ntmp) {
-  // passes R = 1, 2: each takes the pairs whose widest anti-diagonal fits
-  // 32 R lanes, the chain stopping at the first that takes every pair (the
-  // longest lengths give the widest band); pairs longer than the staging
-  // capacity or wider than 64 cells per anti-diagonal are left in spill
+int wave_chain(tsim_ctx* ctx, const DpArgs& a, int max_n, int max_m, int* spill, int* nspill) {
+  // one launch: R = 1 for the pairs whose widest anti-diagonal fits 32
+  // lanes, R = 2 for the others (the longest lengths give the widest band);
+  // pairs longer than the staging capacity or wider than 64 cells per
+  // anti-diagonal are left in spill
   const int qcap = (std::min(max_n, kWaveMaxLen) + 1) & ~1;
   const int ccap = (std::min(max_m, kWaveMaxLen) + 1) & ~1;
   const int tcap = ((qcap + ccap + 2) / 2) * 2;  // n+m-1 anti-diagonals and two past them
   const int lmax = wave_lmax(max_n, max_m, band_w(max_n, max_m, a.band_pct));
-  std::vector<int> rs;
-  for (int R = 1; R <= 2; R *= 2) {
-    rs.push_back(R);
-    if (lmax <= 32 * R) break;
-  }
-  const int np = (int)rs.size();
-  DpArgs in = a;
-  for (int p = 0; p < np; ++p) {
-    const bool to_spill = ((np - 1 - p) & 1) == 0;
-    int* out = to_spill ? spill : tmp;
-    int* nout = to_spill ? nspill : ntmp;
-    TSIM_CUDA(cudaMemsetAsync(nout, 0, sizeof(int), ctx->stream));
-    if (rs[p] == 1)
-      TSIM_TRY((launch_wave_one<P, 1>(ctx, in, qcap, ccap, tcap, out, nout)));
-    else
-      TSIM_TRY((launch_wave_one<P, 2>(ctx, in, qcap, ccap, tcap, out, nout)));
-    in.order = out;
-    in.npairs_dev = nout;
-  }
-  return TSIM_OK;
+  TSIM_CUDA(cudaMemsetAsync(nspill, 0, sizeof(int), ctx->stream));
+  if (lmax <= 32) return launch_wave_one<P, 1>(ctx, a, qcap, ccap, tcap, spill, nspill);
+  return launch_wave_one<P, 2>(ctx, a, qcap, ccap, tcap, spill, nspill);
 }
 
 }  // namespace
@@ -314,16 +325,16 @@ bool wave_kind(int kind) {
 }
 
 int launch_dp_wave(tsim_ctx* ctx, int kind, const DpArgs& a, int max_n, int max_m, int* spill,
-                   int* nspill, int* tmp, int* ntmp) {
+                   int* nspill) {
   switch (kind) {
-    case DP_DTW_SQ: return wave_chain<PolDtwSq>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
-    case DP_DTW_EU: return wave_chain<PolDtwEu>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
+    case DP_DTW_SQ: return wave_chain<PolDtwSq>(ctx, a, max_n, max_m, spill, nspill);
+    case DP_DTW_EU: return wave_chain<PolDtwEu>(ctx, a, max_n, max_m, spill, nspill);
     case DP_FRECHET_SQ:
-      return wave_chain<PolFrechetSq>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
-    case DP_DTW_SQC: return wave_chain<PolDtwSqC>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
-    case DP_DTW_EUC: return wave_chain<PolDtwEuC>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
+      return wave_chain<PolFrechetSq>(ctx, a, max_n, max_m, spill, nspill);
+    case DP_DTW_SQC: return wave_chain<PolDtwSqC>(ctx, a, max_n, max_m, spill, nspill);
+    case DP_DTW_EUC: return wave_chain<PolDtwEuC>(ctx, a, max_n, max_m, spill, nspill);
     case DP_FRECHET_SQC:
-      return wave_chain<PolFrechetSqC>(ctx, a, max_n, max_m, spill, nspill, tmp, ntmp);
+      return wave_chain<PolFrechetSqC>(ctx, a, max_n, max_m, spill, nspill);
   }
   return fail(TSIM_ERR_UNSUPPORTED, "no band-relative kernel for this DP kind");
 }

@@ -124,8 +124,6 @@ struct KArgs {
   float* thr_out;           // optional [nq]: the final pruning threshold, for later requests
   int* waves;               // what the band-relative kernel leaves to the row-group ones
   int* nwaves;
-  int* waves2;              // the list between its two passes
-  int* nwaves2;
   int wave;                 // DTW / Frechet rounds start on the band-relative kernel
   int rdiag;                // rows per lane-group of the anti-diagonal kernel (0: off)
   int rdiag_shape;          // the smallest R a warp per pair admits for the longest pair
@@ -1494,7 +1492,7 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
     // workload's round took 0.24 ms here against 0.20 there; pairs with
     // more than 64 cells per anti-diagonal go on to the row-group kernels
     TSIM_TRY(launch_dp_wave(ctx, kind, d, d.max_n > 0 ? d.max_n : a.max_qlen, a.max_clen,
-                            a.waves, a.nwaves, a.waves2, a.nwaves2));
+                            a.waves, a.nwaves));
     DpArgs rest = d;
     rest.order = a.waves;
     rest.npairs_dev = a.nwaves;
@@ -1984,7 +1982,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
                 align256(sizeof(float4) * (size_t)nq * a.env_stride) +
                 align256(sizeof(double2) * (size_t)nq * (max_qlen + 1)) +
                 align256(sizeof(float4) * (size_t)nq * kQBlocks) +
-                5 * align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 5 * 256;
+                4 * align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 4 * 256;
   return need;
 }
 
@@ -2066,8 +2064,6 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.nlanes = arena_take<int>(ctx, 4);
   a.waves = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
   a.nwaves = arena_take<int>(ctx, 4);
-  a.waves2 = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
-  a.nwaves2 = arena_take<int>(ctx, 4);
   a.csegbox = db->segbox;
   a.csegsum = db->segsum;
   a.order = arena_take<int>(ctx, nqC);
@@ -2441,7 +2437,7 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   int* sorted = arena_take<int>(ctx, npairs);
   int* buckets = arena_take<int>(ctx, lane_sort_buckets());
   if (kernel == 6 && wave_kind(kind)) {  // band-relative first; wider pairs on the others
-    TSIM_TRY(launch_dp_wave(ctx, kind, d, max_qlen, max_clen, rest, nrest, sorted, buckets));
+    TSIM_TRY(launch_dp_wave(ctx, kind, d, max_qlen, max_clen, rest, nrest));
     d.order = rest;
     d.npairs_dev = nrest;
   } else if (kernel == 5 && lane_kind(kind)) {  // a lane per pair first; wider pairs on a warp

@@ -1,6 +1,7 @@
 // pairwise.cu -- tiled pairwise-distance reductions: symmetric Hausdorff
 // (max-min), lock-step Euclidean (sum), and the bounding-box candidate
 // generator that stands in for the reference's Boost R-tree.
+#include "debug_bounds.cuh"
 #include "topk.cuh"
 #include "tsim_internal.cuh"
 
@@ -31,21 +32,25 @@ __device__ float directed_max_min(const float2* S, int ns, const float2* T, int 
   float run = 0.0f;
   for (int base = 0; base < ns; base += P) {
     const int i = base + il;
-    const float2 a = S[i < ns ? i : 0];
+    const float2 a = S[TSIM_SIDX(i < ns ? i : 0, ns)];
     float mn = TSIM_INF;
     int j = g;
     for (; j + 3 * G < nt; j += 4 * G) {  // four independent targets per iteration
-      const float2 b0 = T[j], b1 = T[j + G], b2 = T[j + 2 * G], b3 = T[j + 3 * G];
+      const float2 b0 = T[TSIM_SIDX(j, nt)], b1 = T[TSIM_SIDX(j + G, nt)],
+                   b2 = T[TSIM_SIDX(j + 2 * G, nt)], b3 = T[TSIM_SIDX(j + 3 * G, nt)];
       mn = fminf(mn, fminf(fminf(d2_exact(a.x, a.y, b0.x, b0.y), d2_exact(a.x, a.y, b1.x, b1.y)),
                            fminf(d2_exact(a.x, a.y, b2.x, b2.y), d2_exact(a.x, a.y, b3.x, b3.y))));
     }
-    for (; j < nt; j += G) mn = fminf(mn, d2_exact(a.x, a.y, T[j].x, T[j].y));
+    for (; j < nt; j += G) {
+      const float2 b = T[TSIM_SIDX(j, nt)];
+      mn = fminf(mn, d2_exact(a.x, a.y, b.x, b.y));
+    }
     red[threadIdx.x] = mn;
     __syncthreads();
     float loc = 0.0f;
     if (threadIdx.x < P && base + (int)threadIdx.x < ns) {
       float m2 = red[threadIdx.x];
-      for (int h = 1; h < G; ++h) m2 = fminf(m2, red[h * P + threadIdx.x]);
+      for (int h = 1; h < G; ++h) m2 = fminf(m2, red[TSIM_SIDX(h * P + threadIdx.x, kHdThreads)]);
       loc = m2;
     }
     for (int o = 16; o; o >>= 1) loc = fmaxf(loc, __shfl_xor_sync(0xffffffffu, loc, o));
@@ -73,14 +78,14 @@ __global__ void __launch_bounds__(kHdThreads)
   float2* B = A + n;
   const int q = blockIdx.x;
   const float2* ga = t1 + (size_t)q * n;
-  for (int i = threadIdx.x; i < n; i += kHdThreads) A[i] = ga[i];
+  for (int i = threadIdx.x; i < n; i += kHdThreads) A[TSIM_SIDX(i, n)] = ga[i];
   float best = TSIM_INF;
   for (int k = 0; k < top_k; ++k) {
     const int c = cand[(size_t)q * top_k + k];
     if (c < 0 || c >= num_t2) continue;  // out-of-range candidate slots are ignored
     const float2* gb = t2 + (size_t)c * m;
     __syncthreads();  // the previous candidate is done with B
-    for (int i = threadIdx.x; i < m; i += kHdThreads) B[i] = gb[i];
+    for (int i = threadIdx.x; i < m; i += kHdThreads) B[TSIM_SIDX(i, m)] = gb[i];
     __syncthreads();
     const float h1 = directed_max_min(A, n, B, m, red);
     if (!(h1 < best)) continue;  // uniform: every thread holds the same h1

@@ -329,12 +329,12 @@ int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, i
                    int* nspill, int* tmp, int* ntmp, int warps = 1, int rmax = 0);
 // Band-relative anti-diagonal kernel (dp_wave.cu) for DTW and Frechet, FP32
 // and compensated (wave_kind): a warp per pair, lane p holding the p-th live
-// cells of the anti-diagonal, passes with R = 1 and 2 cells per lane; pairs
+// cells of the anti-diagonal, R = 1 or 2 cells per lane as the pair needs; pairs
 // whose band holds more than 64 cells per anti-diagonal (or longer than
 // 2048 points, or than max_n x max_m) are left in spill[] (count in *nspill).
 bool wave_kind(int kind);
 int launch_dp_wave(tsim_ctx* ctx, int kind, const DpArgs& a, int max_n, int max_m, int* spill,
-                   int* nspill, int* tmp, int* ntmp);
+                   int* nspill);
 // Lane-per-pair kernel (dp_lane.cu) for the FP32 DTW, Frechet and LCSS
 // kinds (lane_kind): a lane runs a whole pair in passes of 8 rows, the row
 // above a pass in a shared-memory ring of `ring` (64 or 128) values per lane

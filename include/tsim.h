@@ -176,6 +176,13 @@ TSIM_API int tsim_debug_fail_allocations(int skip, int count);
  * floats, -1 integers) before its kernels run, so a kernel that reads scratch
  * before writing it changes results.  Process-wide; slows every call. */
 TSIM_API int tsim_debug_set_canary(int on);
+/* libtsim_debug.so (built with TSIM_DEBUG_BOUNDS): every shared-memory index
+ * of the DP and pairwise kernels is checked; one outside its array is
+ * replaced by 0 (the kernel carries on, touching nothing outside) and
+ * counted.  *count = violations since load, *first = (index << 32) | array
+ * size of the first (may be NULL); *count = -1 in the product library,
+ * which has no checks. */
+TSIM_API int tsim_debug_bounds_violations(int64_t* count, int64_t* first);
 
 /* ---- device-resident candidate database ---------------------------------- */
 /* Copies host points/offsets to the device and builds per-trajectory

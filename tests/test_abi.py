@@ -235,3 +235,12 @@ def test_cpp_caller_matches_reference_goldens_on_gpu(tsim, oracle, tmp_path):
         cand = oracle.mbr_knn(t1, n, t2, m, 10)
         want_h = oracle.ref_hausdorff_cands(t1, n, t2, m, cand)
         assert np.array_equal(got[3].view(np.uint32), want_h.view(np.uint32)), (ci, "hausdorff")
+
+
+def test_product_library_has_no_bounds_checks(tsim):
+    """The product library reports -1 from tsim_debug_bounds_violations: its
+    shared-memory indices are unchecked (libtsim_debug.so checks them)."""
+    L = tsim._lib.load()
+    n, f = C.c_int64(7), C.c_int64(7)
+    assert L.tsim_debug_bounds_violations(C.byref(n), C.byref(f)) == 0
+    assert n.value == -1 and f.value == 0
