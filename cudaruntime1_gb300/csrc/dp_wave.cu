@@ -36,8 +36,10 @@
 // Reference kernels replaced: dtw_refine_kernel (CudaRuntime1/dtw.cu:41-96)
 // and frechet_refine_kernel_m (CudaRuntime1/frechet.cu:44-117): a CTA per
 // pair, a full anti-diagonal of threads and two barriers per step.
+#include <type_traits>
 #include <vector>
 
+#include "bounds.cuh"
 #include "debug_bounds.cuh"
 #include "dp_policies.cuh"
 
@@ -47,7 +49,7 @@ using namespace dp;
 
 constexpr int kWaveThreads = 128;
 constexpr int kWavePad = 64;  // points staged past the ends (positions beyond L read them)
-constexpr int kWaveMaxLen = 2048;  // longest trajectory staged in shared memory
+constexpr int kWaveMaxLen = 2048;  // longest trajectory of either side
 
 template <class V>
 __device__ __forceinline__ V vmin(V a, V b) {
@@ -70,25 +72,82 @@ __host__ __device__ inline int wave_lmax(int n, int m, int w) {
   return (int)(l < mn ? l : mn);
 }
 
-// float2 slots of shared memory per warp: query points (qcap + pad),
-// candidate points (pad + ccap + pad), ilo | L << 16 of every anti-diagonal
-// (tcap ints)
-__host__ __device__ inline size_t wave_per_warp(int qcap, int ccap, int tcap) {
-  return (size_t)(qcap + kWavePad) + (ccap + 2 * kWavePad) + tcap / 2;
+// float2 slots of shared memory per warp: candidate points (pad + ccap +
+// pad), the remaining-columns bounds sfx[0 .. ccap] as floats, and with
+// qcap > 0 the query points (qcap + pad)
+__host__ __device__ inline size_t wave_per_warp(int ccap, int qcap) {
+  return (size_t)(ccap + 2 * kWavePad) + (ccap + 2) / 2 + (qcap > 0 ? qcap + kWavePad : 0);
 }
 
-// shared-memory views of the staged pair: query points [0, qcap + pad),
-// candidate points [-pad, ccap + pad), the anti-diagonal table [0, tcap)
-#define QS(i) qs[TSIM_SIDX(i, qcap + kWavePad)]
+// the remaining-columns bound (DTW, FP32, with the query's row-box table)
+template <class P>
+__host__ __device__ bool wave_suffix(const DpArgs& a) {
+  return (std::is_same<P, PolDtwSq>::value || std::is_same<P, PolDtwEu>::value) &&
+         a.qtab != nullptr && a.thr != nullptr && a.max_n > 0 && a.max_n <= 16384;
+}
+
+// Geometry of anti-diagonals base .. base+31, one per lane: ilo | L << 16,
+// from exact integer ramps of the band's edges,
+//   ilo(t) = max(0, t-m+1, ceil((t(n-1) - W) / D)),
+//   ihi(t) = min(n-1, t, floor((t(n-1) + W) / D)),  D = n+m-2,
+// as quotient and remainder (the lower numerator shifted by K D > W to stay
+// non-negative), advanced 16 anti-diagonals at a time.  Past the last
+// anti-diagonal L is 0 and ilo runs on past n-1 (those steps' cells are
+// never used; their point reads stay inside the buffers).
+struct WaveGeom {
+  int lq, lr, hq, hr;  // this lane's ramps
+  int t;               // this lane's anti-diagonal
+  int D, K, sq, sr;    // denominator, shift, 16 (n-1) = sq D + sr
+  bool band;
+  __device__ __forceinline__ void init(int n, int m, int W, int t0) {
+    D = n + m - 2;
+    band = W >= 0;
+    K = band ? W / D + 1 : 0;
+    t = t0;
+    sq = 16 * (n - 1) / D;
+    sr = 16 * (n - 1) - sq * D;
+    lq = lr = hq = hr = 0;
+    if (band) {
+      const int xl = t * (n - 1) - W + (D - 1) + K * D, xh = t * (n - 1) + W;
+      lq = xl / D;
+      lr = xl - lq * D;
+      hq = xh / D;
+      hr = xh - hq * D;
+    }
+  }
+  __device__ __forceinline__ int entry(int n, int m) const {
+    int lo = max(0, t - (m - 1)), hi = min(n - 1, t);
+    if (band) {
+      lo = max(lo, lq - K);
+      hi = min(hi, hq);
+    }
+    return lo | (max(0, hi - lo + 1) << 16);
+  }
+  __device__ __forceinline__ void advance16() {
+    t += 16;
+    if (band) {
+      lq += sq;
+      lr += sr;
+      if (lr >= D) lr -= D, ++lq;
+      hq += sq;
+      hr += sr;
+      if (hr >= D) hr -= D, ++hq;
+    }
+  }
+};
+
+// shared-memory views of the staged pair: candidate points [-pad, ccap +
+// pad), query points [0, qcap + pad) (QS: staged, else read through L1)
 #define CS(j) cs[TSIM_SIDX((j) + kWavePad, ccap + 2 * kWavePad) - kWavePad]
-#define TAB(t) tab[TSIM_SIDX(t, tcap)]
+#define SFX(j) sfx[TSIM_SIDX(j, ccap + 1)]
+#define QPT(i) (QS ? qs[TSIM_SIDX(i, qcap + kWavePad)] : __ldg(A + min(i, n - 1)))
 
 // One pair on the warp, R cells per lane (its widest anti-diagonal fits 32 R).
-template <class P, int R>
+template <class P, int R, bool QS>
 __device__ __forceinline__ void wave_pair(const DpArgs& a, const int pid, const int q, const int n,
                                           const int m, const int w, const int64_t qo,
-                                          const int64_t co, float2* qs, float2* cs, int* tab,
-                                          const int qcap, const int ccap, const int tcap) {
+                                          const int64_t co, float2* cs, float* sfx, float2* qs,
+                                          const int ccap, const int qcap) {
   using V = typename P::V;
   using C = typename P::C;
   const int lane = threadIdx.x & 31;
@@ -96,78 +155,103 @@ __device__ __forceinline__ void wave_pair(const DpArgs& a, const int pid, const 
   const int src_dn = (lane + 31) & 31, src_up = (lane + 1) & 31;
   const int t_end = n + m - 2;
   const float thr = check ? a.thr[q] : TSIM_INF;
+  const int W = w < 0 ? -1 : w * (min(n, m) - 1);
+  // the candidate's points are staged; the query's too in the latency
+  // rounds (a lone pair's step waits on them), else read through L1, which
+  // every pair of the query shares, for the smaller footprint
+  const float2* A = a.qpts + qo;
 
-  // the pair's points, and the geometry of every anti-diagonal:
-  // ilo(t) = max(0, t-m+1, ceil((t(n-1) - W) / D)),
-  // ihi(t) = min(n-1, t, floor((t(n-1) + W) / D)),  D = n+m-2,
-  // stepped by 32 anti-diagonals per lane as quotient and remainder
   __syncwarp();
   {
-    const float2* A = a.qpts + qo;
     const float2* B = a.cpts + co;
-    for (int i = lane; i < n; i += 32) QS(i) = __ldg(A + i);
     for (int j = lane; j < m; j += 32) CS(j) = __ldg(B + j);
-    const int D = t_end;
-    const int W = w < 0 ? -1 : w * (min(n, m) - 1);
-    const int step = 32 * (n - 1), sq = step / D, sr = step % D;
-    // lo numerator shifted by K D (K D > W) to stay non-negative
-    const int K = W < 0 ? 0 : W / D + 1;
-    int lq = 0, lr = 0, hq = 0, hr = 0;
-    if (W >= 0 && lane <= t_end) {
-      const int xl = lane * (n - 1) - W + (D - 1) + K * D, xh = lane * (n - 1) + W;
-      lq = xl / D;
-      lr = xl % D;
-      hq = xh / D;
-      hr = xh % D;
-    }
-    for (int t = lane; t <= t_end; t += 32) {
-      int lo = max(0, t - (m - 1)), hi = min(n - 1, t);
-      if (W >= 0) {
-        lo = max(lo, lq - K);
-        hi = min(hi, hq);
-        lq += sq;
-        lr += sr;
-        if (lr >= D) lr -= D, ++lq;
-        hq += sq;
-        hr += sr;
-        if (hr >= D) hr -= D, ++hq;
-      }
-      TAB(t) = lo | (max(0, hi - lo + 1) << 16);
-    }
-    // two entries past the last anti-diagonal: the step after it reads
-    // them (its cells are never used)
-    if (lane < 2) TAB(t_end + 1 + lane) = (n - 1) | (1 << 16);
+    if (QS)
+      for (int i = lane; i < n; i += 32) qs[TSIM_SIDX(i, qcap + kWavePad)] = __ldg(A + i);
   }
+  // Remaining-columns bound (the survivor round): every path crosses every
+  // column after the largest one of two consecutive anti-diagonals, and a
+  // cell of column j costs at least the distance from candidate point j to
+  // the box of the query rows j's band admits.  sfx[j] = those bounds summed
+  // over columns j .. m-1 (rounded down; sfx[m] = 0).  The FP32 path sum that
+  // adds those columns' costs can round below their exact sum by at most
+  // (n+m+8) 2^-24 relative, so the check compares with the threshold divided
+  // by 1 minus that.
+  const bool suffix = wave_suffix<P>(a) && n <= a.max_n;
+  float thr_chk = thr;
   __syncwarp();
+  if (suffix) {
+    const QTable T = qtable_view(a.qtab + (size_t)q * qtable_stride(a.max_n), n);
+    float carry = 0.0f;  // bound of the columns after the current block
+    for (int b0 = ((m - 1) >> 5) << 5; b0 >= 0; b0 -= 32) {  // blocks of 32 columns, last first
+      const int j = b0 + lane;
+      float v = 0.0f;
+      if (j < m) {
+        int lo = 0, hi = n - 1;
+        if (W >= 0) {
+          lo = max(0, floordiv_i((long long)j * (n - 1) - W + (m - 2), m - 1));  // ceil
+          hi = min(n - 1, floordiv_i((long long)j * (n - 1) + W, m - 1));
+        }
+        if (lo <= hi) {
+          const float4 bx = qtable_box(T, lo, hi);
+          const float2 c = CS(j);
+          v = box_pt_d2_rd(bx.x, bx.y, bx.z, bx.w, c.x, c.y);
+          if (std::is_same<P, PolDtwEu>::value) v = __fsqrt_rd(v);
+        } else {
+          v = TSIM_INF;  // a column with no admissible row: no path
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {  // suffix sums inside the block
+        const float u = __shfl_down_sync(0xffffffffu, v, o);
+        if (lane + o < 32) v = __fadd_rd(v, u);
+      }
+      v = __fadd_rd(v, carry);
+      if (j < m) SFX(j) = v;
+      carry = __shfl_sync(0xffffffffu, v, 0);
+    }
+    if (lane == 0) SFX(m) = 0.0f;
+    const float shrink = __fsub_rd(1.0f, __fmul_ru((float)(n + m + 8), 6.03e-8f));
+    thr_chk = __fdiv_ru(thr, shrink);
+    __syncwarp();
+  }
+
+  __syncwarp();
+  // anti-diagonals base .. base + 31 of this block and the next, a lane each
+  WaveGeom geo;
+  geo.init(n, m, W, 1 + lane);
+  int win = geo.entry(n, m);
+  int base = 1;
 
   // step 0: cell (0, 0) at position 0; every other position outside
   V v[R], mm[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) v[r] = mm[r] = P::border();
   if (lane == 0) {
-    const float2 p = QS(0), c = CS(0);
+    const float2 p = QPT(0), c = CS(0);
     v[0] = P::cell(p.x, p.y, c.x, c.y, P::border(), P::border(), P::origin(), a.eps);
     mm[0] = v[0];  // its left (0, -1) is outside
   }
-  // costs of the cells of step tt (positions lane R + r), geometry lo
+  // costs of the cells of step tt (positions lane R + r), geometry lo; rows
+  // past the query's end (masked positions) read its last point
   auto costs = [&](C* out, int tt, int lo) {
     const int i0 = lo + lane * R, j0 = tt - lo - lane * R;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const float2 qp = QS(i0 + r), cp = CS(j0 - r);
+      const float2 qp = QPT(i0 + r), cp = CS(j0 - r);
       out[r] = P::cost(qp.x, qp.y, cp.x, cp.y);
     }
   };
   C cst[R];
-  int e = TAB(1);   // geometry of the step computed next
-  int e1 = TAB(2);  // and of the one after (the table runs two entries past t_end)
+  int e = __shfl_sync(0xffffffffu, win, 0);   // geometry of the step computed next
+  int e1 = __shfl_sync(0xffffffffu, win, 1);  // and of the one after
   costs(cst, 1, e & 0xffff);
   V edge = P::border();  // lane 0: position 0's diagonal when the next shift is 0
   int ilo = 0;
   bool alive = true;
   // one anti-diagonal: the shuffle, R cells, and the next step's costs
-  // (computed past the last step too: the padding keeps them in bounds)
-  auto step = [&](const int t) {
+  // (computed past the last step too: the padding keeps them in bounds);
+  // e2 is the geometry of step t + 2
+  auto step = [&](const int t, const int e2) {
     const int nlo = e & 0xffff, L = e >> 16;
     const int s = nlo - ilo;  // 0 or 1, uniform
     // across lanes: s = 0 takes M of the lane above's last position, s = 1
@@ -175,7 +259,6 @@ __device__ __forceinline__ void wave_pair(const DpArgs& a, const int pid, const 
     const V xin = wshfl(s ? v[0] : mm[R - 1], s ? src_up : src_dn);
     C cn[R];
     costs(cn, t + 1, e1 & 0xffff);
-    const int e2 = TAB(t + 2);
     const V edge_next = s ? v[0] : P::border();
     V nv[R], nm[R];  // every position reads the last step's values
 #pragma unroll
@@ -207,31 +290,43 @@ __device__ __forceinline__ void wave_pair(const DpArgs& a, const int pid, const 
     return x;
   };
   // blocks of 16 straight-line steps; after each, the abandon test over
-  // its last two anti-diagonals
+  // its last two anti-diagonals (plus the columns after them)
   int t = 1;
   for (; t + 15 <= t_end; t += 16) {
     float m14 = TSIM_INF;
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
-      step(t + u);
+      step(t + u, __shfl_sync(0xffffffffu, win, u + 2));
       if (u == 14) m14 = lane_min();
     }
+    geo.advance16();
+    const int win_next = geo.entry(n, m);
     if (check) {
       const float two = fminf(lane_min(), m14);
-      const float lb = __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(two)));
-      if (lb > thr) {  // uniform across the warp
+      float lb = __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(two)));
+      // the largest column of anti-diagonals t+14, t+15 is t+15 - ilo(t+15)
+      if (suffix) lb = __fadd_rd(lb, SFX(min(t + 15 - ilo + 1, m)));
+      if (lb > thr_chk) {  // uniform across the warp
         alive = false;
         t += 15;
         break;
       }
     }
+    win = win_next;
+    base += 16;
   }
   if (alive)
-    for (; t <= t_end; ++t) step(t);
+    for (; t <= t_end; ++t) step(t, __shfl_sync(0xffffffffu, win, t + 2 - base));
   if (a.cells) {  // cells of the anti-diagonals computed, inside the band
     const int t_done = alive ? t_end : min(t, t_end);
     long long cells = 0;
-    for (int u = lane; u <= t_done; u += 32) cells += TAB(u) >> 16;
+    WaveGeom g2;
+    g2.init(n, m, W, lane);
+    for (int u = lane; u <= t_done; u += 32) {
+      cells += g2.entry(n, m) >> 16;
+      g2.advance16();
+      g2.advance16();
+    }
     for (int o = 16; o; o >>= 1) cells += __shfl_xor_sync(0xffffffffu, cells, o);
     if (lane == 0) atomicAdd(a.cells, (unsigned long long)cells);
   }
@@ -243,16 +338,17 @@ __device__ __forceinline__ void wave_pair(const DpArgs& a, const int pid, const 
 // pair up to 64 cells per anti-diagonal, each with the R (1 or 2) it needs --
 // one launch instead of a pass per R (the passes would run one after the
 // other, each as long as its longest pair)
-template <class P, int RMAX>
+template <class P, int RMAX, bool QS>
 __global__ void __launch_bounds__(kWaveThreads)
-    dp_wave_kernel(DpArgs a, int qcap, int ccap, int tcap, int* spill, int* nspill) {
+    dp_wave_kernel(DpArgs a, int ccap, int qcap, int* spill, int* nspill) {
   static_assert(P::kMin, "the band-relative kernel serves the minimum measures");
   extern __shared__ __align__(16) float2 wave_smem[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  float2* qs = wave_smem + (size_t)warp * wave_per_warp(qcap, ccap, tcap);
-  float2* cs = qs + qcap + kWavePad + kWavePad;  // cs[-kWavePad .. ccap + kWavePad)
-  int* tab = reinterpret_cast<int*>(cs + ccap + kWavePad);
+  float2* cs = wave_smem + (size_t)warp * wave_per_warp(ccap, QS ? qcap : 0) +
+               kWavePad;  // cs[-pad .. ccap + pad)
+  float* sfx = reinterpret_cast<float*>(cs + ccap + kWavePad);
+  float2* qs = cs + ccap + kWavePad + (ccap + 2) / 2;  // QS: qs[0 .. qcap + pad)
   const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nslots = (gridDim.x * blockDim.x) >> 5;
   const int npairs = a.npairs_dev ? min(*a.npairs_dev, a.npairs) : a.npairs;
@@ -266,27 +362,27 @@ __global__ void __launch_bounds__(kWaveThreads)
     const int n = (int)(a.qoff[q + 1] - qo), m = (int)(a.coff[pr.y + 1] - co);
     const int w = band_w(n, m, a.band_pct);
     const int lm = wave_lmax(n, m, w);
-    if (n < 2 || m < 2 || n > qcap || m > ccap || n + m + 1 > tcap || lm > 32 * RMAX) {
+    if (n < 2 || m < 2 || n > (QS ? qcap : kWaveMaxLen) || m > ccap || lm > 32 * RMAX) {
       if (lane == 0 && spill) spill[atomicAdd(nspill, 1)] = pid;
       continue;
     }
     if (RMAX == 1 || lm <= 32)  // uniform across the warp
-      wave_pair<P, 1>(a, pid, q, n, m, w, qo, co, qs, cs, tab, qcap, ccap, tcap);
+      wave_pair<P, 1, QS>(a, pid, q, n, m, w, qo, co, cs, sfx, qs, ccap, qcap);
     else
-      wave_pair<P, RMAX>(a, pid, q, n, m, w, qo, co, qs, cs, tab, qcap, ccap, tcap);
+      wave_pair<P, RMAX, QS>(a, pid, q, n, m, w, qo, co, cs, sfx, qs, ccap, qcap);
   }
 }
 
-#undef QS
 #undef CS
-#undef TAB
+#undef SFX
+#undef QPT
 
-template <class P, int R>
-int launch_wave_one(tsim_ctx* ctx, const DpArgs& a, int qcap, int ccap, int tcap, int* spill,
-                    int* nspill) {
+template <class P, int R, bool QS>
+int launch_wave_one(tsim_ctx* ctx, const DpArgs& a, int ccap, int qcap, int* spill, int* nspill) {
   if (a.npairs <= 0) return TSIM_OK;
-  auto kern = dp_wave_kernel<P, R>;
-  const size_t smem = (size_t)(kWaveThreads / 32) * wave_per_warp(qcap, ccap, tcap) * sizeof(float2);
+  auto kern = dp_wave_kernel<P, R, QS>;
+  const size_t smem =
+      (size_t)(kWaveThreads / 32) * wave_per_warp(ccap, QS ? qcap : 0) * sizeof(float2);
   if (smem > 48 * 1024)
     TSIM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
@@ -295,26 +391,29 @@ int launch_wave_one(tsim_ctx* ctx, const DpArgs& a, int qcap, int ccap, int tcap
   const long long warps = kWaveThreads / 32;
   const long long blocks = std::min<long long>((a.npairs + warps - 1) / warps,
                                                (long long)per_sm * ctx->num_sms);
-  kern<<<(unsigned)std::max(blocks, 1ll), kWaveThreads, smem, ctx->stream>>>(a, qcap, ccap, tcap,
-                                                                             spill, nspill);
+  kern<<<(unsigned)std::max(blocks, 1ll), kWaveThreads, smem, ctx->stream>>>(a, ccap, qcap, spill,
+                                                                             nspill);
   TSIM_CUDA(cudaGetLastError());
   launched(ctx);
   return TSIM_OK;
 }
 
 template <class P>
-int wave_chain(tsim_ctx* ctx, const DpArgs& a, int max_n, int max_m, int* spill, int* nspill) {
+int wave_chain(tsim_ctx* ctx, const DpArgs& a, int max_n, int max_m, bool latency, int* spill,
+               int* nspill) {
   // one launch: R = 1 for the pairs whose widest anti-diagonal fits 32
   // lanes, R = 2 for the others (the longest lengths give the widest band);
   // pairs longer than the staging capacity or wider than 64 cells per
-  // anti-diagonal are left in spill
-  const int qcap = (std::min(max_n, kWaveMaxLen) + 1) & ~1;
+  // anti-diagonal are left in spill.  Latency rounds stage the query too.
   const int ccap = (std::min(max_m, kWaveMaxLen) + 1) & ~1;
-  const int tcap = ((qcap + ccap + 2) / 2) * 2;  // n+m-1 anti-diagonals and two past them
+  const int qcap = (std::min(max_n, kWaveMaxLen) + 1) & ~1;
   const int lmax = wave_lmax(max_n, max_m, band_w(max_n, max_m, a.band_pct));
   TSIM_CUDA(cudaMemsetAsync(nspill, 0, sizeof(int), ctx->stream));
-  if (lmax <= 32) return launch_wave_one<P, 1>(ctx, a, qcap, ccap, tcap, spill, nspill);
-  return launch_wave_one<P, 2>(ctx, a, qcap, ccap, tcap, spill, nspill);
+  if (latency)
+    return lmax <= 32 ? launch_wave_one<P, 1, true>(ctx, a, ccap, qcap, spill, nspill)
+                      : launch_wave_one<P, 2, true>(ctx, a, ccap, qcap, spill, nspill);
+  return lmax <= 32 ? launch_wave_one<P, 1, false>(ctx, a, ccap, qcap, spill, nspill)
+                    : launch_wave_one<P, 2, false>(ctx, a, ccap, qcap, spill, nspill);
 }
 
 }  // namespace
@@ -324,17 +423,17 @@ bool wave_kind(int kind) {
          kind == DP_DTW_EUC || kind == DP_FRECHET_SQC;
 }
 
-int launch_dp_wave(tsim_ctx* ctx, int kind, const DpArgs& a, int max_n, int max_m, int* spill,
-                   int* nspill) {
+int launch_dp_wave(tsim_ctx* ctx, int kind, const DpArgs& a, int max_n, int max_m, bool latency,
+                   int* spill, int* nspill) {
   switch (kind) {
-    case DP_DTW_SQ: return wave_chain<PolDtwSq>(ctx, a, max_n, max_m, spill, nspill);
-    case DP_DTW_EU: return wave_chain<PolDtwEu>(ctx, a, max_n, max_m, spill, nspill);
+    case DP_DTW_SQ: return wave_chain<PolDtwSq>(ctx, a, max_n, max_m, latency, spill, nspill);
+    case DP_DTW_EU: return wave_chain<PolDtwEu>(ctx, a, max_n, max_m, latency, spill, nspill);
     case DP_FRECHET_SQ:
-      return wave_chain<PolFrechetSq>(ctx, a, max_n, max_m, spill, nspill);
-    case DP_DTW_SQC: return wave_chain<PolDtwSqC>(ctx, a, max_n, max_m, spill, nspill);
-    case DP_DTW_EUC: return wave_chain<PolDtwEuC>(ctx, a, max_n, max_m, spill, nspill);
+      return wave_chain<PolFrechetSq>(ctx, a, max_n, max_m, latency, spill, nspill);
+    case DP_DTW_SQC: return wave_chain<PolDtwSqC>(ctx, a, max_n, max_m, latency, spill, nspill);
+    case DP_DTW_EUC: return wave_chain<PolDtwEuC>(ctx, a, max_n, max_m, latency, spill, nspill);
     case DP_FRECHET_SQC:
-      return wave_chain<PolFrechetSqC>(ctx, a, max_n, max_m, spill, nspill);
+      return wave_chain<PolFrechetSqC>(ctx, a, max_n, max_m, latency, spill, nspill);
   }
   return fail(TSIM_ERR_UNSUPPORTED, "no band-relative kernel for this DP kind");
 }

@@ -564,10 +564,48 @@ __device__ __forceinline__ float row_seg_min(const QTable& T, const float4* sb, 
   return mn;
 }
 
-// t: the pair's pruning threshold; once a partial bound exceeds it the pair
-// is pruned and the rest is not evaluated
+// A pair's segment bound is evaluated by a group of kSegs lanes (aligned
+// within the warp, all active): lane g takes candidate segment g and query
+// row segments 4g .. 4g+3, and the parts meet by shuffles inside the group.
+// A lane alone ran the 8 + 32 box lookups of a pair one after the other,
+// each waiting on the last (latency-bound: 64 us for 8 queries' 6,251 pairs).
+// Sums are rounded downward in a tree, a different order from a sequential
+// sum but every partial sum still at most the exact one; the group's lanes
+// end with the same value (each level adds the same two operands).
+constexpr int kSegGroup = kSegs;
+constexpr int kRowPerLane = kRowSegs / kSegGroup;
+static_assert(kSegGroup == 8 && kRowSegs % kSegGroup == 0, "one candidate segment per lane");
+
+__device__ __forceinline__ unsigned seg_group_mask() {
+  return 0xffu << (threadIdx.x & 31 & ~(kSegGroup - 1));
+}
+__device__ __forceinline__ float group_sum_rd(float v) {
+  const unsigned mk = seg_group_mask();
+#pragma unroll
+  for (int o = kSegGroup / 2; o; o >>= 1) v = __fadd_rd(v, __shfl_xor_sync(mk, v, o, kSegGroup));
+  return v;
+}
+__device__ __forceinline__ float group_max(float v) {
+  const unsigned mk = seg_group_mask();
+#pragma unroll
+  for (int o = kSegGroup / 2; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(mk, v, o, kSegGroup));
+  return v;
+}
+__device__ __forceinline__ int group_isum(int v) {
+  const unsigned mk = seg_group_mask();
+#pragma unroll
+  for (int o = kSegGroup / 2; o; o >>= 1) v += __shfl_xor_sync(mk, v, o, kSegGroup);
+  return v;
+}
+__device__ __forceinline__ bool group_any(bool v) {
+  return (__ballot_sync(seg_group_mask(), v) & seg_group_mask()) != 0u;
+}
+
+// t: the pair's pruning threshold; once the candidate segments' part exceeds
+// it the row segments are not evaluated.  Called by every lane of a group
+// with the same pair; g is the lane within the group.
 template <int MEAS>
-__device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1, float t) {
+__device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1, float t, int g) {
   if (n > a.max_qlen || n < 1 || m < 1) return lb1;
   const float4* sb = a.csegbox + (size_t)c * kSegs;
   const float4 qb = a.qbox[q];
@@ -580,10 +618,10 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
     if (n < m) return TSIM_INF;
     const float2* ss = a.csegsum + (size_t)c * kSegs;
     const double2* P = a.qpre + (size_t)q * (a.max_qlen + 1);
-    float acc = 0.0f;
-    for (int s = 0; s < kSegs && acc <= t; ++s) {
-      const int b0 = seg_first(s, m), b1 = seg_first(s + 1, m) - 1;
-      if (b1 < b0) continue;
+    float part = 0.0f;
+    const int s = g;
+    const int b0 = seg_first(s, m), b1 = seg_first(s + 1, m) - 1;
+    if (b1 >= b0) {
       const float L = (float)(b1 - b0 + 1);
       const float d = box_box_d2_rd(qtable_box(T, b0, b1), sb[s]);
       const float2 sc = ss[s];
@@ -600,99 +638,113 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
                                  __fmul_ru(fabsf((float)p1.y) + fabsf((float)p0.y), pe));
       const float ax = fmaxf(0.0f, __fsub_rd(dx, ex)), ay = fmaxf(0.0f, __fsub_rd(dy, ey));
       const float cs = __fdiv_rd(__fadd_rd(__fmul_rd(ax, ax), __fmul_rd(ay, ay)), L);
-      acc = __fadd_rd(acc, fmaxf(__fmul_rd(L, d), cs));
+      part = fmaxf(__fmul_rd(L, d), cs);
     }
-    return fmaxf(acc, lb1);
+    return fmaxf(group_sum_rd(part), lb1);
   }
   if (MEAS == M_FRECHET || MEAS == M_HAUSDORFF) {
     // every point of either set is matched to some point of the other
     float mx = lb1;
-    for (int s = 0; s < kSegs; ++s) {
-      const float4 b = sb[s];
-      if (b.x > b.z) continue;  // empty segment
-      mx = fmaxf(mx, box_box_d2_rd(qb, b));
-    }
+    const float4 b = sb[g];
+    if (!(b.x > b.z)) mx = fmaxf(mx, box_box_d2_rd(qb, b));  // else an empty segment
+    mx = group_max(mx);
+    if (mx > t) return mx;
     const int L = (n + kRowSegs - 1) / kRowSegs;
-    int sf = 0;
-    for (int r0 = 0; r0 < n && mx <= t; r0 += L) {
-      sf = 0;
-      mx = fmaxf(mx, row_seg_min(T, sb, m, r0, min(n - 1, r0 + L - 1), 0, m - 1, sf));
+#pragma unroll
+    for (int k = 0; k < kRowPerLane; ++k) {
+      const int r0 = (g * kRowPerLane + k) * L;
+      int sf = 0;
+      if (r0 < n) mx = fmaxf(mx, row_seg_min(T, sb, m, r0, min(n - 1, r0 + L - 1), 0, m - 1, sf));
     }
-    return mx;
+    return group_max(mx);
   }
   if (MEAS == M_LCSS) {
     const float e2 = __fmul_ru(a.eps, 1.0f + 1.0f / 1048576.0f);
     int count = 0;
-    for (int s = 0; s < kSegs; ++s) {
-      const int b0 = (int)((long long)s * m / kSegs), b1 = (int)((long long)(s + 1) * m / kSegs) - 1;
-      if (b1 < b0) continue;
-      int lo = 0, hi = n - 1;
-      if (a.delta >= 0) {
-        lo = max(0, b0 - a.delta);
-        hi = min(n - 1, b1 + a.delta);
-      }
-      if (lo > hi) continue;
+    const int s = g;
+    const int b0 = (int)((long long)s * m / kSegs), b1 = (int)((long long)(s + 1) * m / kSegs) - 1;
+    int lo = 0, hi = n - 1;
+    if (a.delta >= 0) {
+      lo = max(0, b0 - a.delta);
+      hi = min(n - 1, b1 + a.delta);
+    }
+    if (b1 >= b0 && lo <= hi) {
       const float4 qx = qtable_box(T, lo, hi), b = sb[s];
       if (b.z >= __fsub_rd(qx.x, e2) && b.x <= __fadd_ru(qx.z, e2) && b.w >= __fsub_rd(qx.y, e2) &&
           b.y <= __fadd_ru(qx.w, e2))
-        count += b1 - b0 + 1;
+        count = b1 - b0 + 1;
     }
+    count = group_isum(count);
     return fminf(lb1, (float)min(count, min(n, m)));
   }
   // DTW
   const float4 qe = a.qends[q], ce = a.cends[c];
-  float acc;
   if (m == 1) {
     float d = pd2_rd(qe.x, qe.y, ce.x, ce.y);
-    acc = a.cost ? __fsqrt_rd(d) : d;
+    float acc = a.cost ? __fsqrt_rd(d) : d;
     if (n > 1) {
       float d2 = pd2_rd(qe.z, qe.w, ce.x, ce.y);
       acc = __fadd_rd(acc, a.cost ? __fsqrt_rd(d2) : d2);
     }
     return fmaxf(acc, lb1);
   }
+  float corners;
   {
     float d0 = pd2_rd(qe.x, qe.y, ce.x, ce.y), d1 = pd2_rd(qe.z, qe.w, ce.z, ce.w);
-    acc = a.cost ? __fadd_rd(__fsqrt_rd(d0), __fsqrt_rd(d1)) : __fadd_rd(d0, d1);
+    corners = a.cost ? __fadd_rd(__fsqrt_rd(d0), __fsqrt_rd(d1)) : __fadd_rd(d0, d1);
   }
   const int w = band_w(n, m, a.band_pct);
   const bool banded = w >= 0 && n > 1;
   const long long W = banded ? (long long)w * (min(n, m) - 1) : 0;
-  for (int s = 0; s < kSegs; ++s) {
+  // columns 1 .. m-2 in the candidate's segments, each at least its box's
+  // distance to the box of the query rows its band admits
+  float part = 0.0f;
+  bool infeasible = false;
+  {
+    const int s = g;
     const int b0 = max(1, (int)((long long)s * m / kSegs));
     const int b1 = min(m - 2, (int)((long long)(s + 1) * m / kSegs) - 1);
-    if (b1 < b0) continue;
-    int lo = 0, hi = n - 1;
-    if (banded) {
-      lo = max(0, floordiv_i((long long)b0 * (n - 1) - W + (m - 2), m - 1));  // ceil
-      hi = min(n - 1, floordiv_i((long long)b1 * (n - 1) + W, m - 1));
+    if (b1 >= b0) {
+      int lo = 0, hi = n - 1;
+      if (banded) {
+        lo = max(0, floordiv_i((long long)b0 * (n - 1) - W + (m - 2), m - 1));  // ceil
+        hi = min(n - 1, floordiv_i((long long)b1 * (n - 1) + W, m - 1));
+      }
+      if (lo > hi) {
+        infeasible = true;  // a column with no admissible row
+      } else {
+        const float d = box_box_d2_rd(qtable_box(T, lo, hi), sb[s]);
+        part = __fmul_rd((float)(b1 - b0 + 1), a.cost ? __fsqrt_rd(d) : d);
+      }
     }
-    if (lo > hi) return TSIM_INF;  // a column with no admissible row: infeasible
-    const float4 qx = qtable_box(T, lo, hi);
-    const float d = box_box_d2_rd(qx, sb[s]);
-    acc = __fadd_rd(acc, __fmul_rd((float)(b1 - b0 + 1), a.cost ? __fsqrt_rd(d) : d));
   }
+  if (group_any(infeasible)) return TSIM_INF;
+  const float acc = __fadd_rd(corners, group_sum_rd(part));
+  if (fmaxf(acc, lb1) > t) return fmaxf(acc, lb1);
   // rows 1 .. n-2, each with at least one path cell inside its band columns
   // (the corner cells of rows 0 and n-1 are already counted); a segment of
   // rows r0..r1 admits columns [lo(r0), hi(r0 + L - 1)], from integer ramps
-  if (fmaxf(acc, lb1) > t) return fmaxf(acc, lb1);
-  float accr;
-  {
-    const float d0 = pd2_rd(qe.x, qe.y, ce.x, ce.y), d1 = pd2_rd(qe.z, qe.w, ce.z, ce.w);
-    accr = a.cost ? __fadd_rd(__fsqrt_rd(d0), __fsqrt_rd(d1)) : __fadd_rd(d0, d1);
-  }
+  // started at this lane's first segment
+  float accr = corners;
   if (n > 2) {
     const int L = (n - 2 + kRowSegs - 1) / kRowSegs;
     const long long d = n - 1, sl = (long long)L * (m - 1);
     const long long K = floordiv_i(W, (int)d) + 1;
-    long long xl = (long long)(m - 1) - W + (d - 1) + K * d;  // lo numerator at row 1
-    long long xh = (long long)L * (m - 1) + W;                // hi numerator at row L
+    const int k0 = g * kRowPerLane;
+    // lo numerator at row 1 + k0 L, hi numerator at row (k0 + 1) L
+    long long xl = (long long)(m - 1) - W + (d - 1) + K * d + (long long)k0 * sl;
+    long long xh = (long long)L * (m - 1) + W + (long long)k0 * sl;
     int ql, rl, qh, rh, sq, sr;
     divmod_floor(xl, (int)d, ql, rl);
     divmod_floor(xh, (int)d, qh, rh);
     divmod_floor(sl, (int)d, sq, sr);
+    float pr = 0.0f;
     int sf = 0;
-    for (int r0 = 1; r0 <= n - 2; r0 += L) {
+    bool none = false;
+#pragma unroll
+    for (int k = 0; k < kRowPerLane; ++k) {
+      const int r0 = 1 + (k0 + k) * L;
+      if (r0 > n - 2) break;
       const int r1 = min(n - 2, r0 + L - 1);
       int clo = 0, chi = m - 1;
       if (banded) {
@@ -705,11 +757,15 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
         rh += sr;
         if (rh >= d) rh -= (int)d, ++qh;
       }
-      if (chi < clo) return TSIM_INF;  // rows with no admissible column: infeasible
+      if (chi < clo) {  // rows with no admissible column
+        none = true;
+        break;
+      }
       const float mn = row_seg_min(T, sb, m, r0, r1, clo, chi, sf);
-      accr = __fadd_rd(accr, __fmul_rd((float)(r1 - r0 + 1), a.cost ? __fsqrt_rd(mn) : mn));
-      if (accr > t) break;
+      pr = __fadd_rd(pr, __fmul_rd((float)(r1 - r0 + 1), a.cost ? __fsqrt_rd(mn) : mn));
     }
+    if (group_any(none)) return TSIM_INF;
+    accr = __fadd_rd(corners, group_sum_rd(pr));
   }
   return fmaxf(fmaxf(acc, accr), lb1);
 }
@@ -766,17 +822,19 @@ __global__ void __launch_bounds__(256) segfilter_kernel(KArgs a) {
   const int cnt = a.cnt0[q];
   const float t = a.thr[q];
   const int n = a.qlen[q];
-  const int start = blockIdx.x * blockDim.x;
-  const int stride = gridDim.x * blockDim.x;
+  const int g = threadIdx.x & (kSegGroup - 1);
+  const int per_block = blockDim.x / kSegGroup;  // pairs per block and pass
+  const int start = blockIdx.x * per_block;
+  const int stride = gridDim.x * per_block;
   for (int e0 = start; e0 < cnt; e0 += stride) {  // uniform per block: whole blocks iterate
-    const int e = e0 + threadIdx.x;
+    const int e = e0 + (int)threadIdx.x / kSegGroup;
     bool pass = false;
     int c = 0;
-    if (e < cnt) {
+    if (e < cnt) {  // uniform per group
       c = a.list2[(size_t)q * a.C + e];
       const float b = a.lb1[(size_t)q * a.C + c];
-      const float sbnd = seg_bound<MEAS>(a, q, c, n, a.clen[c], b, t);
-      pass = MEAS == M_LCSS ? (sbnd >= t) : (sbnd <= t);
+      const float sbnd = seg_bound<MEAS>(a, q, c, n, a.clen[c], b, t, g);
+      pass = g == 0 && (MEAS == M_LCSS ? (sbnd >= t) : (sbnd <= t));
       if (pass) a.lb1[(size_t)q * a.C + c] = sbnd;
     }
     block_append(pass, a.cnt1 + q, a.list1 + (size_t)q * a.C, c);
@@ -1482,16 +1540,15 @@ int run_dp(tsim_ctx* ctx, const KArgs& a, int kind, int G, int R, const DpArgs& 
   }
   if (!diag_kind || a.rdiag == 0) return launch_dp(ctx, kind, G, R, d, a.max_clen);
   const bool twofloat_kind = kind == DP_DTW_SQC || kind == DP_DTW_EUC || kind == DP_FRECHET_SQC;
-  if (a.wave && latency && wave_kind(kind) && !twofloat_kind) {
+  if (a.wave && wave_kind(kind) && !twofloat_kind) {
     // lanes along the anti-diagonal, straight-line blocks of 16 steps: the
     // shortest FP32 step of the warp-per-pair forms (a lone 512 x 486 pair
     // 83 us against 104 on two warps per pair; compensated pairs are faster
-    // on two warps, 131 against 203 us), for the latency rounds.  DTW's
-    // survivor round stays on the row-group kernel: with the same
-    // remaining-columns abandon bound (38 M cells either way) the batched
-    // workload's round took 0.24 ms here against 0.20 there; pairs with
-    // more than 64 cells per anti-diagonal go on to the row-group kernels
-    TSIM_TRY(launch_dp_wave(ctx, kind, d, d.max_n > 0 ? d.max_n : a.max_qlen, a.max_clen,
+    // on two warps, 131 against 203 us), and no masked row slots: the
+    // latency rounds and the survivor round (after the lane kernel's gate);
+    // pairs with more than 64 cells per anti-diagonal go on to the row-group
+    // kernels
+    TSIM_TRY(launch_dp_wave(ctx, kind, d, d.max_n > 0 ? d.max_n : a.max_qlen, a.max_clen, latency,
                             a.waves, a.nwaves));
     DpArgs rest = d;
     rest.order = a.waves;
@@ -1742,7 +1799,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   }
   launched(ctx);
   compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
-  segfilter_kernel<MEAS><<<dim3(std::max(1, std::min(1024, (8 * ctx->num_sms + nq - 1) / nq)), nq),
+  segfilter_kernel<MEAS><<<dim3(std::max(1, std::min(1024, (32 * ctx->num_sms + nq - 1) / nq)), nq),
                            256, 0, s>>>(a);
   launched(ctx);
   launched(ctx, 2);
@@ -2437,7 +2494,7 @@ extern "C" int tsim_dp_pairs(tsim_ctx* ctx, const tsim_params* p, int precision,
   int* sorted = arena_take<int>(ctx, npairs);
   int* buckets = arena_take<int>(ctx, lane_sort_buckets());
   if (kernel == 6 && wave_kind(kind)) {  // band-relative first; wider pairs on the others
-    TSIM_TRY(launch_dp_wave(ctx, kind, d, max_qlen, max_clen, rest, nrest));
+    TSIM_TRY(launch_dp_wave(ctx, kind, d, max_qlen, max_clen, npairs <= 4 * ctx->num_sms, rest, nrest));
     d.order = rest;
     d.npairs_dev = nrest;
   } else if (kernel == 5 && lane_kind(kind)) {  // a lane per pair first; wider pairs on a warp

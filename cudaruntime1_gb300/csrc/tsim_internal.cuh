@@ -333,8 +333,8 @@ int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, i
 // whose band holds more than 64 cells per anti-diagonal (or longer than
 // 2048 points, or than max_n x max_m) are left in spill[] (count in *nspill).
 bool wave_kind(int kind);
-int launch_dp_wave(tsim_ctx* ctx, int kind, const DpArgs& a, int max_n, int max_m, int* spill,
-                   int* nspill);
+int launch_dp_wave(tsim_ctx* ctx, int kind, const DpArgs& a, int max_n, int max_m, bool latency,
+                   int* spill, int* nspill);
 // Lane-per-pair kernel (dp_lane.cu) for the FP32 DTW, Frechet and LCSS
 // kinds (lane_kind): a lane runs a whole pair in passes of 8 rows, the row
 // above a pass in a shared-memory ring of `ring` (64 or 128) values per lane
