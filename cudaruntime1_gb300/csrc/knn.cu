@@ -637,7 +637,10 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
       const float ey = __fadd_ru(__fmul_ru(fabsf(sc.y) + dy, 1.0f / 4194304.0f),
                                  __fmul_ru(fabsf((float)p1.y) + fabsf((float)p0.y), pe));
       const float ax = fmaxf(0.0f, __fsub_rd(dx, ex)), ay = fmaxf(0.0f, __fsub_rd(dy, ey));
-      const float cs = __fdiv_rd(__fadd_rd(__fmul_rd(ax, ax), __fmul_rd(ay, ay)), L);
+      // / L as * (1/L rounded, times 1 - 2^-23 rounded down: below 1/L), no
+      // division sequence
+      const float rl = __fmul_rd(__frcp_rn(L), 0.99999988f);
+      const float cs = __fmul_rd(__fadd_rd(__fmul_rd(ax, ax), __fmul_rd(ay, ay)), rl);
       part = fmaxf(__fmul_rd(L, d), cs);
     }
     return fmaxf(group_sum_rd(part), lb1);
@@ -848,6 +851,23 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int cnt = a.cnt1[q];
   if (cnt == 0) return;  // uniform across the CTA
+  if (MEAS == M_EUCLID) {
+    // no O(length) bound (the exact sum costs the same): the list passes
+    // whole, in order, with the segment bounds -- no append per pair (an
+    // atomic per pair on the query's counter cost 26 ms per 1,024 x 262,144
+    // request)
+    // (an empty trajectory on either side leaves a consumed entry, -1)
+    const int* L1 = a.list1 + (size_t)q * a.C;
+    const bool qok = a.qlen[q] > 0;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += gridDim.x * blockDim.x) {
+      const int c = L1[e];
+      const bool ok = qok && a.clen[c] > 0;
+      a.list2[(size_t)q * a.C + e] = ok ? c : -1;
+      a.lb2v[(size_t)q * a.C + e] = ok ? a.lb1[(size_t)q * a.C + c] : TSIM_INF;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt2[q] = cnt;
+    return;
+  }
   const float2* A = a.qpts + a.qoff[q];
   const int n = a.qlen[q];
   const float4 qb = a.qbox[q];
