@@ -108,7 +108,8 @@ struct KArgs {
   int* fcnt;                // [nq]  round-2 pairs per query (in list1)
   const float4* csegbox;    // [C*kSegs] candidate segment boxes
   const float2* csegsum;    // [C*kSegs] sums of the candidate segments' points
-  double2* qpre;            // [nq*(max_qlen+1)] query prefix sums (FP64)
+  float2* qpf;              // [nq*(max_qlen+1)] query prefix sums of p_j - p_0, FP32-rounded
+  float* qpe;               // [nq] twice a bound on their FP64 accumulation error
   float4* qblk;             // [nq*kQBlocks] boxes of the query's row blocks
   int* spill;               // pairs the anti-diagonal kernel leaves to the striped one
   int* nspill;
@@ -475,33 +476,47 @@ __global__ void qtable_global_kernel(KArgs a, int sums) {
   QTable T;
   qtable_build(T, A, n, a.qtab + (size_t)q * a.tstride);
   if (!sums) return;  // prefix sums: lock-step Euclidean only
-  // prefix sums P[j] = sum of points 0 .. j-1, j = 0 .. n: a chunk per thread
-  double2* P = a.qpre + (size_t)q * (a.max_qlen + 1);
+  // P[j] = sum of (p_i - p_0) over i = 0 .. j-1, j = 0 .. n, in FP64 (each
+  // difference of two floats exact), rounded once to float; a chunk per
+  // thread.  The FP64 sums are within n 2^-53 sum |p_i - p_0| of exact;
+  // qpe[q] keeps twice that, rounded up.
+  __shared__ double2 mag[256];
+  float2* P = a.qpf + (size_t)q * (a.max_qlen + 1);
+  const double x0 = A[0].x, y0 = A[0].y;
   const int per = (n + blockDim.x - 1) / blockDim.x;
   const int j0 = min(n, (int)threadIdx.x * per), j1 = min(n, j0 + per);
-  double sx = 0.0, sy = 0.0;
+  double sx = 0.0, sy = 0.0, ax = 0.0, ay = 0.0;
   for (int j = j0; j < j1; ++j) {
-    sx += A[j].x;
-    sy += A[j].y;
+    const double dx = (double)A[j].x - x0, dy = (double)A[j].y - y0;
+    sx += dx;
+    sy += dy;
+    ax += fabs(dx);
+    ay += fabs(dy);
   }
   part[threadIdx.x] = make_double2(sx, sy);
+  mag[threadIdx.x] = make_double2(ax, ay);
   __syncthreads();
   if (threadIdx.x == 0) {
-    double rx = 0.0, ry = 0.0;
+    double rx = 0.0, ry = 0.0, mx = 0.0, my = 0.0;
     for (int i = 0; i < (int)blockDim.x; ++i) {
       const double2 v = part[i];
       part[i] = make_double2(rx, ry);
       rx += v.x;
       ry += v.y;
+      mx += mag[i].x;
+      my += mag[i].y;
     }
-    P[n] = make_double2(rx, ry);
+    P[n] = make_float2((float)rx, (float)ry);
+    // n 2^-53 (1 + 2^-40) max(sum |dx|, sum |dy|), doubled, rounded up
+    a.qpe[q] = __double2float_ru(2.0 * (double)n * 1.1102230246251565e-16 * (1.0 + 1e-12) *
+                                 fmax(mx, my));
   }
   __syncthreads();
   double rx = part[threadIdx.x].x, ry = part[threadIdx.x].y;
   for (int j = j0; j < j1; ++j) {
-    P[j] = make_double2(rx, ry);
-    rx += A[j].x;
-    ry += A[j].y;
+    P[j] = make_float2((float)rx, (float)ry);
+    rx += (double)A[j].x - x0;
+    ry += (double)A[j].y - y0;
   }
 }
 
@@ -617,26 +632,34 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
     // / L per coordinate (Cauchy-Schwarz); the larger of the two per segment
     if (n < m) return TSIM_INF;
     const float2* ss = a.csegsum + (size_t)c * kSegs;
-    const double2* P = a.qpre + (size_t)q * (a.max_qlen + 1);
+    const float2* P = a.qpf + (size_t)q * (a.max_qlen + 1);
+    const float4 qe = a.qends[q];  // the query's first point: P's origin
     float part = 0.0f;
     const int s = g;
     const int b0 = seg_first(s, m), b1 = seg_first(s + 1, m) - 1;
     if (b1 >= b0) {
       const float L = (float)(b1 - b0 + 1);
-      const float d = box_box_d2_rd(qtable_box(T, b0, b1), sb[s]);
+      const float4 cb = sb[s];
+      const float d = box_box_d2_rd(qtable_box(T, b0, b1), cb);
       const float2 sc = ss[s];
-      const double2 p1 = P[b1 + 1], p0 = P[b0];
-      // error margins: the candidate sum's float rounding and the rounding of
-      // the difference to float (each <= 2^-24 relative; 4x slack), and the
-      // FP64 prefix sums' accumulated rounding (<= (n+1) 2^-53 of their size)
-      const float dx = fabsf((float)(p1.x - p0.x - (double)sc.x));
-      const float dy = fabsf((float)(p1.y - p0.y - (double)sc.y));
-      const float pe = (float)(n + 1) * (1.0f / 2251799813685248.0f);  // (n+1) 2^-51
-      const float ex = __fadd_ru(__fmul_ru(fabsf(sc.x) + dx, 1.0f / 4194304.0f),
-                                 __fmul_ru(fabsf((float)p1.x) + fabsf((float)p0.x), pe));
-      const float ey = __fadd_ru(__fmul_ru(fabsf(sc.y) + dy, 1.0f / 4194304.0f),
-                                 __fmul_ru(fabsf((float)p1.y) + fabsf((float)p0.y), pe));
-      const float ax = fmaxf(0.0f, __fsub_rd(dx, ex)), ay = fmaxf(0.0f, __fsub_rd(dy, ey));
+      const float2 f1 = P[b1 + 1], f0 = P[b0];
+      const float e64 = a.qpe[q];
+      // |sum q - sum c| per coordinate, in FP32 from origin-shifted sums:
+      // A = f1 - f0 (the query's, less L p_0), B = sc - L p_0 (the
+      // candidate's), D = |A - B|.  Each rounding -- f1, f0, A, t = L p_0, B,
+      // D, and the candidate sum's (one float rounding of an FP64 sum) -- is
+      // at most 2^-24 of its value, so 2^-22 of the magnitudes below covers
+      // them twice over; e64 covers the query's FP64 prefix sums and 2^-30 L
+      // max|c| the candidate's (at most L^2 2^-53 max|c|, L <= 2^11).
+      auto gap = [&](float a1, float a0, float scv, float p0, float c0, float c1) {
+        const float A = a1 - a0, t = L * p0, B = scv - t, D = fabsf(A - B);
+        float mgn = __fadd_ru(__fadd_ru(fabsf(a1), fabsf(a0)), __fadd_ru(fabsf(t), fabsf(scv)));
+        mgn = __fadd_ru(__fmul_ru(__fadd_ru(mgn, D), 1.0f / 4194304.0f), e64);
+        mgn = __fadd_ru(mgn, __fmul_ru(__fmul_ru(L, fmaxf(fabsf(c0), fabsf(c1))), 1.0f / 1073741824.0f));
+        return fmaxf(0.0f, __fsub_rd(D, mgn));
+      };
+      const float ax = gap(f1.x, f0.x, sc.x, qe.x, cb.x, cb.z);
+      const float ay = gap(f1.y, f0.y, sc.y, qe.y, cb.y, cb.w);
       // / L as * (1/L rounded, times 1 - 2^-23 rounded down: below 1/L), no
       // division sequence
       const float rl = __fmul_rd(__frcp_rn(L), 0.99999988f);
@@ -2057,7 +2080,7 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
                 align256(sizeof(float) * nq * a.M) + 2 * align256(sizeof(float) * (nq + 1)) +
                 align256(sizeof(float4) * (size_t)nq * a.tstride) +
                 align256(sizeof(float4) * (size_t)nq * a.env_stride) +
-                align256(sizeof(double2) * (size_t)nq * (max_qlen + 1)) +
+                align256(sizeof(float2) * (size_t)nq * (max_qlen + 1)) + align256(sizeof(float) * nq) +
                 align256(sizeof(float4) * (size_t)nq * kQBlocks) +
                 4 * align256(sizeof(int) * (size_t)nq * std::max(C, a.RC)) + 4 * 256;
   return need;
@@ -2131,7 +2154,8 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.fcnt = arena_take<int>(ctx, nq + 1);
   a.qtab = arena_take<float4>(ctx, (size_t)nq * a.tstride);
   a.qenv = a.env_stride ? arena_take<float4>(ctx, (size_t)nq * a.env_stride) : nullptr;
-  a.qpre = arena_take<double2>(ctx, (size_t)nq * (max_qlen + 1));
+  a.qpf = arena_take<float2>(ctx, (size_t)nq * (max_qlen + 1));
+  a.qpe = arena_take<float>(ctx, nq);
   a.qblk = arena_take<float4>(ctx, (size_t)nq * kQBlocks);
   a.spill = arena_take<int>(ctx, (size_t)nq * std::max(C, a.RC));
   a.nspill = arena_take<int>(ctx, 4);

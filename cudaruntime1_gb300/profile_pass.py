@@ -19,6 +19,9 @@ graph replay, one chunk on a single stream.
     python -m cudaruntime1_gb300.profile_pass --lcss-frechet
         one LCSS and one Frechet exact-kNN request of the 256 x 65,536
         workload (lognormal lengths) on one stream
+    python -m cudaruntime1_gb300.profile_pass --hausdorff-euclid MEASURE [NQ]
+        one exact-kNN request (MEASURE hausdorff or euclidean) of the
+        1,024 x 262,144 workload on one stream, or of its first NQ queries
 """
 from __future__ import annotations
 
@@ -95,6 +98,33 @@ def lcss_frechet_case():
     ctx.close()
 
 
+def hausdorff_euclid_case(measure, nq_use):
+    import torch
+
+    import cudaruntime1_gb300 as T
+    from bench import KNN_WORKLOADS, knn_workload_data
+    from cudaruntime1_gb300 import api
+    T.build()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = T.Context(0, stream.cuda_stream)
+    ctx.set_concurrency(1)
+    w = KNN_WORKLOADS["hausdorff_euclid"]
+    qp, qo, cp, co = knn_workload_data("hausdorff_euclid", w, measure)
+    db = T.Database(ctx, cp, co)
+    qpt, qot = torch.from_numpy(qp).cuda(), torch.from_numpy(qo).cuda()
+    nq = nq_use if nq_use > 0 else len(qo) - 1
+    maxq, k = int(np.max(np.diff(qo))), w["k"]
+    ids = torch.empty(nq * k, dtype=torch.int32, device="cuda")
+    dd = torch.empty(nq * k, dtype=torch.float32, device="cuda")
+    api.knn_device(ctx, db, qpt.data_ptr(), qot.data_ptr(), nq, maxq, ids.data_ptr(),
+                   dd.data_ptr(), 0, measure, k, flags=api.FLAG_NO_GRAPH)
+    torch.cuda.synchronize()
+    print("ok", ids[:k].tolist())
+    db.close()
+    ctx.close()
+
+
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -104,6 +134,10 @@ def main(argv=None):
             return dp_pairs_case(int(argv[argv.index(flag) + 1]), flag == "--dp-saturated")
     if "--lcss-frechet" in argv:
         return lcss_frechet_case()
+    if "--hausdorff-euclid" in argv:
+        i = argv.index("--hausdorff-euclid")
+        rest = argv[i + 1:]
+        return hausdorff_euclid_case(rest[0], int(rest[1]) if len(rest) > 1 else 0)
     serving = "--serving" in argv
     argv = [x for x in argv if x != "--serving"]
     passes = int(argv[0]) if argv else 1
