@@ -47,9 +47,9 @@ WORKLOAD = dict(workload="dtw_knn_batched_uneven", queries=64, candidates=16384,
                 len_hi=512, band_pct=10, cost="squared_euclidean", k=10, seed=2024)
 DP_FLOPS_PER_CELL = 8  # 2 sub, mul, fma (2), 2 min, add
 # dram__bytes_read.sum + dram__bytes_write.sum of the survivor-round DP launch
-# of this workload (single stream, planner's R), one ncu capture of
+# of this workload (dp_wave_kernel, single stream), one ncu capture of
 # `python -m cudaruntime1_gb300.profile_pass 1` on a GB300
-SURVIVOR_DP_DRAM_BYTES = 11567872
+SURVIVOR_DP_DRAM_BYTES = 11592448
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -1132,7 +1132,8 @@ def main():
             "parity": {"ids_bit_exact_vs_fp64_oracle": ids_match, "max_rel_err": max_rel},
             "dp_saturated": sat,
             "roofline": {
-                "kernel": "dp_diag_kernel<PolDtwSq,R>, survivor round (FP32 anti-diagonal DTW)",
+                "kernel": "dp_wave_kernel<PolDtwSq,R>, survivor round (FP32 band-relative "
+                          "anti-diagonal DTW, a warp per pair)",
                 "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak if fp32_peak else None,
                 "traffic": SURVIVOR_DP_DRAM_BYTES, "traffic_unit": "bytes per launch (ncu)",

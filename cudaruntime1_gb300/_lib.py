@@ -141,6 +141,7 @@ def load(build_if_missing: bool = False):
             "tsim_probe_fp32_tflops": ([_vp, C.POINTER(C.c_double)], C.c_int),
             "tsim_debug_fail_allocations": ([C.c_int, C.c_int], C.c_int),
             "tsim_debug_set_canary": ([C.c_int], C.c_int),
+            "tsim_debug_set_wait_limit": ([C.c_int64], C.c_int),
             "tsim_debug_bounds_violations": ([C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
                                              C.c_int),
             "tsim_ctx_set_concurrency": ([_vp, C.c_int], C.c_int),

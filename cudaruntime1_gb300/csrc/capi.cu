@@ -381,6 +381,10 @@ extern "C" int tsim_debug_set_canary(int on) {
   return TSIM_OK;
 }
 
+extern "C" int tsim_debug_set_wait_limit(int64_t attempts) {
+  return tsim::set_wait_limit((long long)attempts);
+}
+
 extern "C" int tsim_probe_fp32_tflops(tsim_ctx* ctx, double* tflops) {
   TSIM_CHECK_ARG(ctx && tflops, "NULL argument");
   TSIM_CUDA(cudaSetDevice(ctx->device));

@@ -31,8 +31,10 @@
 // candidate by a heuristic bound, refines a fixed 10 and returns one value:
 // not an exact kNN.  This path returns the exact top-k ids and distances.
 #include <cstring>
+#include <type_traits>
 
 #include "bounds.cuh"
+#include "bulk_copy.cuh"
 #include "topk.cuh"
 #include "tsim_internal.cuh"
 
@@ -110,6 +112,9 @@ struct KArgs {
   const float2* csegsum;    // [C*kSegs] sums of the candidate segments' points
   float2* qpf;              // [nq*(max_qlen+1)] query prefix sums of p_j - p_0, FP32-rounded
   float* qpe;               // [nq] twice a bound on their FP64 accumulation error
+  int lb2_cap;              // DTW O(length) stage: points per bulk-copy buffer (0: no bulk copies)
+  int64_t ctotal;           // points in the database's array (bulk copies stay inside it)
+  unsigned* status;         // device status word: bit 0 = a bounded wait ran out
   float4* qblk;             // [nq*kQBlocks] boxes of the query's row blocks
   int* spill;               // pairs the anti-diagonal kernel leaves to the striped one
   int* nspill;
@@ -867,6 +872,11 @@ __global__ void __launch_bounds__(256) segfilter_kernel(KArgs a) {
   }
 }
 
+// Attempts of a bounded wait on a bulk copy (each may suspend briefly): the
+// default, or a smaller count set for tests (0: every wait runs out at once).
+constexpr uint32_t kWaitLimitDefault = 1u << 22;
+__device__ uint32_t g_wait_limit = kWaitLimitDefault;
+
 template <int MEAS>
 __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -944,29 +954,99 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
     for (int i = threadIdx.x; i < a.env_stride; i += blockDim.x) envs[i] = Eg[i];
     __syncthreads();
   }
+  // DTW: a pair's candidate points come by bulk copy into one of the warp's
+  // two shared-memory buffers, the next pair's copy in flight while the
+  // current one is bounded (the column loop otherwise waits on each point
+  // load).  The copy covers the points rounded out to an even start and
+  // count (16-byte alignment); a pair whose range would leave the array, or
+  // longer than a buffer, reads global memory as before.  A wait that runs
+  // out sets the status word and the pair reads global memory: the bound is
+  // the same either way.
+  constexpr bool kBulk = MEAS == M_DTW;
+  const int cap = kBulk ? a.lb2_cap : 0;
+  __shared__ __align__(8) uint64_t bars[kLb2Warps][2];
+  float2* bufs = reinterpret_cast<float2*>(smem_raw) + (size_t)warp * 2 * (cap + 2);
+  if (kBulk && cap > 0) {
+    if (threadIdx.x < 2 * kLb2Warps) mbar_init(&bars[threadIdx.x >> 1][threadIdx.x & 1], 1);
+    mbar_init_fence();
+    __syncthreads();
+  }
+  uint32_t phase[2] = {0u, 0u};
+  bool pend[2] = {false, false};
+  const uint32_t limit = g_wait_limit;
+  auto bulk_ok = [&](int64_t o, int m) {
+    return cap > 0 && m >= 2 && m <= cap && (o & ~1ll) + (((o & 1) + m + 1) & ~1ll) <= a.ctotal;
+  };
+  auto drain = [&](int sl) {  // an issued copy not yet waited for
+    if (pend[sl]) {
+      mbar_wait(&bars[warp][sl], phase[sl], kWaitLimitDefault);
+      phase[sl] ^= 1u;
+      pend[sl] = false;
+    }
+  };
+  auto issue = [&](int sl, int64_t o, int m) {
+    drain(sl);
+    const int64_t beg = o & ~1ll;
+    const int npts = (int)(((o & 1) + m + 1) & ~1ll);
+    if (lane == 0) bulk_load(bufs + sl * (cap + 2), a.cpts + beg, (uint32_t)npts * 8u, &bars[warp][sl]);
+    pend[sl] = true;
+  };
+
   // The warp's pairs e, e + S, ...: a pair's candidate index, then its
   // offset, length and segment bound, are dependent loads; they are issued
-  // two and one pairs ahead of the pair being bounded, so their latency
-  // overlaps its column loop instead of preceding it.
+  // three and two pairs ahead of the pair being bounded, so that the next
+  // pair's offset is known when its bulk copy starts and no load latency
+  // precedes a column loop.
   const int S = gridDim.x * kLb2Warps;
   const int* L1 = a.list1 + (size_t)q * a.C;
   const float* LB1 = a.lb1 + (size_t)q * a.C;
   int e = blockIdx.x * kLb2Warps + warp;
-  int c_nx = e < cnt ? L1[e] : 0;            // this pair's candidate
-  int c_nn = e + S < cnt ? L1[e + S] : 0;    // the next one's
+  int c_cur = e < cnt ? L1[e] : 0;
+  int c_nx = e + S < cnt ? L1[e + S] : 0;
+  int c_nn = e + 2 * S < cnt ? L1[e + 2 * S] : 0;
+  int64_t o_cur = a.coff[c_cur];
+  int m_cur = a.clen[c_cur];
+  float s_cur = e < cnt ? LB1[c_cur] : 0.0f;
   int64_t o_nx = a.coff[c_nx];
   int m_nx = a.clen[c_nx];
-  float s_nx = e < cnt ? LB1[c_nx] : 0.0f;
+  float s_nx = e + S < cnt ? LB1[c_nx] : 0.0f;
+  int slot = 0;
+  bool bulk_cur = e < cnt && bulk_ok(o_cur, m_cur);
+  if (bulk_cur) issue(0, o_cur, m_cur);
   for (; e < cnt; e += S) {
-    const int c = c_nx;
-    const float2* B = a.cpts + o_nx;
-    const int m = m_nx;
-    const float sbnd = s_nx;  // the segment bound of stage A
+    const int c = c_cur;
+    const int m = m_cur;
+    const float sbnd = s_cur;  // the segment bound of stage A
+    const int64_t co = o_cur;
+    const bool bulk = bulk_cur;
+    // the next pair's copy, then the loads two pairs ahead
+    const bool bulk_nx = e + S < cnt && bulk_ok(o_nx, m_nx);
+    if (bulk_nx) issue(slot ^ 1, o_nx, m_nx);
+    const int c_nnn = e + 3 * S < cnt ? L1[e + 3 * S] : 0;
+    const int64_t o_nn = a.coff[c_nn];
+    const int m_nn = a.clen[c_nn];
+    const float s_nn = e + 2 * S < cnt ? LB1[c_nn] : 0.0f;
+    const float2* B = a.cpts + co;
+    if (bulk) {
+      const bool got = __all_sync(0xffffffffu, mbar_wait(&bars[warp][slot], phase[slot], limit));
+      if (got) {
+        phase[slot] ^= 1u;
+        pend[slot] = false;
+        B = bufs + slot * (cap + 2) + (co & 1);
+      } else if (lane == 0) {
+        atomicOr(a.status, 1u);
+      }
+    }
+    c_cur = c_nx;
+    o_cur = o_nx;
+    m_cur = m_nx;
+    s_cur = s_nx;
+    bulk_cur = bulk_nx;
     c_nx = c_nn;
-    c_nn = e + 2 * S < cnt ? L1[e + 2 * S] : 0;
-    o_nx = a.coff[c_nx];
-    m_nx = a.clen[c_nx];
-    s_nx = e + S < cnt ? LB1[c_nx] : 0.0f;
+    o_nx = o_nn;
+    m_nx = m_nn;
+    s_nx = s_nn;
+    c_nn = c_nnn;
     bool pass;
     float lbv = sbnd;  // the bound (no O(length) bound: stage A's)
     if (n <= 0 || m <= 0) {
@@ -1012,24 +1092,38 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
         int dq = 0, dr = 0;
         if (banded) divmod_floor(inc, D, dq, dr);
         // no early exit: an infeasible pair's bound is +inf whatever the sum,
-        // and a loop without one keeps several point loads in flight
+        // and a loop without one keeps several point loads in flight.  The
+        // band and the cost are compile-time in the loop (a runtime cost test
+        // left the rounded square root in every column's code path)
+        auto columns = [&](auto band_c, auto eu_c) {
+          constexpr bool BAND = decltype(band_c)::value, EU = decltype(eu_c)::value;
 #pragma unroll 4
-        for (int j = j0; j < m - 1; j += 32) {
-          int lo = 0, hi = n - 1;
-          if (banded) {
-            lo = max(lo_d.q, 0);
-            hi = min(hi_d.q, n - 1);
-            lo_d.step(dq, dr);
-            hi_d.step(dq, dr);
+          for (int j = j0; j < m - 1; j += 32) {
+            int lo = 0, hi = n - 1;
+            if (BAND) {
+              lo = max(lo_d.q, 0);
+              hi = min(hi_d.q, n - 1);
+              lo_d.step(dq, dr);
+              hi_d.step(dq, dr);
+            }
+            if (lo > hi) {  // a column with no admissible row
+              feasible = false;
+              lo = hi = min(lo, n - 1);
+            }
+            const float4 bx = qtable_box(T, lo, hi);
+            const float2 p = B[j];
+            const float d = box_pt_d2_rd(bx.x, bx.y, bx.z, bx.w, p.x, p.y);
+            acc = __fadd_rd(acc, EU ? __fsqrt_rd(d) : d);
           }
-          if (lo > hi) {  // a column with no admissible row
-            feasible = false;
-            lo = hi = min(lo, n - 1);
-          }
-          const float4 bx = qtable_box(T, lo, hi);
-          const float2 p = B[j];
-          float d = box_pt_d2_rd(bx.x, bx.y, bx.z, bx.w, p.x, p.y);
-          acc = __fadd_rd(acc, a.cost ? __fsqrt_rd(d) : d);
+        };
+        using T1 = std::true_type;
+        using F0 = std::false_type;
+        if (banded) {
+          if (a.cost) columns(T1{}, T1{});
+          else columns(T1{}, F0{});
+        } else {
+          if (a.cost) columns(F0{}, T1{});
+          else columns(F0{}, F0{});
         }
       }
       for (int o = 16; o; o >>= 1) acc = __fadd_rd(acc, __shfl_xor_sync(0xffffffffu, acc, o));
@@ -1084,7 +1178,12 @@ __global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
       a.list2[(size_t)q * a.C + pos] = c;
       a.lb2v[(size_t)q * a.C + pos] = lbv;
     }
+    __syncwarp();  // every lane is done with this buffer before it is refilled
+    slot ^= 1;
   }
+  // no copy may be left running into shared memory the next CTA gets
+  drain(0);
+  drain(1);
 }
 
 // Round 1: the M best survivors of each query by their O(length) bound
@@ -1853,7 +1952,9 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   // LCSS: the query's grid and window boxes per CTA, and 4x the CTAs per
   // query (its queries' pair counts vary widely; a CTA's set-up is small)
   const size_t lb2_smem =
-      MEAS == M_LCSS ? sizeof(uint32_t) * kGridWords + sizeof(float4) * (size_t)a.env_stride : 0;
+      MEAS == M_LCSS   ? sizeof(uint32_t) * kGridWords + sizeof(float4) * (size_t)a.env_stride
+      : MEAS == M_DTW ? sizeof(float2) * (size_t)kLb2Warps * 2 * (a.lb2_cap + 2)
+                       : 0;
   const int ch2 = MEAS == M_LCSS ? std::max(1, std::min(65535, (32 * ctx->num_sms + nq - 1) / nq))
                                  : ch;
   if (lb2_smem > 48 * 1024)
@@ -2167,6 +2268,19 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
   a.nwaves = arena_take<int>(ctx, 4);
   a.csegbox = db->segbox;
   a.csegsum = db->segsum;
+  // bulk copies of candidate points (DTW's O(length) stage): buffers of up to
+  // 512 points, a 16-byte aligned array (the copies' sources are even
+  // points), and a database larger than L2, whose points come from HBM: the
+  // 1M-trajectory serving database's stage went from 1.84 to 1.35 ms, while
+  // the 38 MB batched one's, L2-resident, went from 102 to 113 us (the
+  // buffers cut the CTAs per SM from 5 to 3)
+  a.ctotal = db->total;
+  const bool db_beyond_l2 = (double)db->total * sizeof(float2) > 96.0 * (1 << 20);
+  a.lb2_cap = (p->measure == TSIM_DTW && db_beyond_l2 &&
+               (reinterpret_cast<uintptr_t>(db->pts) & 15) == 0)
+                  ? (std::min(db->max_len, 512) + 1) & ~1
+                  : 0;
+  a.status = reinterpret_cast<unsigned*>(ctx->dcounters + kStatusSlot);
   a.order = arena_take<int>(ctx, nqC);
   a.shape_cnt = arena_take<int>(ctx, kNumShapes);
   if (!a.shape_cnt) return fail(TSIM_ERR_OUT_OF_MEMORY, "knn scratch carve failed");
@@ -2239,6 +2353,31 @@ std::vector<uint64_t> arena_gens(tsim_ctx* ctx) {
 // the graph.  Graphs are dropped when an arena is reallocated or a database
 // is destroyed.  Stats, profiling, the plain form and TSIM_FLAG_NO_GRAPH
 // run eagerly.
+namespace tsim {
+int set_wait_limit(long long attempts) {
+  const uint32_t v = attempts < 0 ? kWaitLimitDefault
+                                  : (uint32_t)std::min<long long>(attempts, 0xffffffffll);
+  TSIM_CUDA(cudaMemcpyToSymbol(g_wait_limit, &v, sizeof(v)));
+  return TSIM_OK;
+}
+
+int take_device_status(tsim_ctx* ctx) {
+  unsigned any = 0;
+  std::vector<tsim_ctx*> all{ctx};
+  all.insert(all.end(), ctx->subs.begin(), ctx->subs.end());
+  for (tsim_ctx* c : all) {
+    if (!c->dcounters) continue;
+    unsigned v = 0;
+    unsigned* w = reinterpret_cast<unsigned*>(c->dcounters + kStatusSlot);
+    TSIM_CUDA(cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost));
+    if (v) TSIM_CUDA(cudaMemset(w, 0, sizeof(v)));
+    any |= v;
+  }
+  if (any & 1u) return fail(TSIM_ERR_TIMEOUT, "a bounded wait on a bulk copy ran out");
+  return TSIM_OK;
+}
+}  // namespace tsim
+
 extern "C" int tsim_knn(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
                         const int64_t* d_qoff, int nq, int max_qlen, tsim_db* db, int* d_ids,
                         float* d_dists, double* d_dists64, tsim_stats* stats) {
@@ -2386,6 +2525,7 @@ int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
     }
   if (stats) {
     TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+    TSIM_TRY(tsim::take_device_status(ctx));
     for (tsim_ctx* c : lanes) {
       unsigned long long v[5];
       TSIM_CUDA(cudaMemcpy(v, c->dcounters + 2, sizeof(v), cudaMemcpyDeviceToHost));
@@ -2450,6 +2590,7 @@ extern "C" int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
   TSIM_CUDA(cudaMemcpyAsync(hp + in_bytes, dp + in_bytes, out_bytes, cudaMemcpyDeviceToHost,
                             ctx->stream));
   TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
+  TSIM_TRY(tsim::take_device_status(ctx));
   memcpy(h_ids, hp + in_bytes, sizeof(int) * nq * p->k);
   memcpy(h_dists, hp + in_bytes + tsim::align256(sizeof(int) * nq * p->k), sizeof(float) * nq * p->k);
   return TSIM_OK;

@@ -46,6 +46,9 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 // consecutive column segments: segment s covers columns [s*m/kSegs,
 // (s+1)*m/kSegs).  At most 32 (one lane per segment builds them).
 constexpr int kSegs = 8;
+// slot of the context's device counters that holds its status word: bit 0
+// is set by a kernel whose bounded wait on a bulk copy ran out
+constexpr int kStatusSlot = 40;
 
 // ---------------------------------------------------------------------------
 // context: device, stream and a grow-only scratch arena
@@ -77,7 +80,7 @@ struct tsim_ctx {
   int nstage_ev = 0;
   double stage_ms[TSIM_STAGE_COUNT] = {};
   int64_t stage_calls[TSIM_STAGE_COUNT] = {};
-  unsigned long long* dcounters = nullptr;  // device: [0] DP cells computed
+  unsigned long long* dcounters = nullptr;  // device: [0] DP cells computed, [kStatusSlot] status
   // concurrency: a request's queries are split into chunks that run on these
   // child contexts (own stream and arena), forked from and joined back to
   // `stream` with events, so that latency-bound stages of different chunks
@@ -333,6 +336,11 @@ int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, i
 // whose band holds more than 64 cells per anti-diagonal (or longer than
 // 2048 points, or than max_n x max_m) are left in spill[] (count in *nspill).
 bool wave_kind(int kind);
+// After a synchronisation: TSIM_ERR_TIMEOUT (and the status words cleared)
+// if a kernel of ctx or of its chunk contexts set the timeout bit, else OK.
+int take_device_status(tsim_ctx* ctx);
+// Attempts of the bounded waits on bulk copies (< 0: the default); for tests.
+int set_wait_limit(long long attempts);
 int launch_dp_wave(tsim_ctx* ctx, int kind, const DpArgs& a, int max_n, int max_m, bool latency,
                    int* spill, int* nspill);
 // Lane-per-pair kernel (dp_lane.cu) for the FP32 DTW, Frechet and LCSS

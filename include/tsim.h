@@ -176,6 +176,15 @@ TSIM_API int tsim_debug_fail_allocations(int skip, int count);
  * floats, -1 integers) before its kernels run, so a kernel that reads scratch
  * before writing it changes results.  Process-wide; slows every call. */
 TSIM_API int tsim_debug_set_canary(int on);
+/* Attempts of the device-side bounded waits (a kernel waiting for its bulk
+ * copies of candidate points): attempts < 0 restores the default (about 4 M,
+ * seconds at most); 0 makes every such wait run out at once.  A wait that
+ * runs out sets the context's status word, the kernel reads the points from
+ * global memory instead (results unchanged) and waits for its copies before
+ * it exits; the next synchronising call (stats requested, or the
+ * host-pointer entry point) returns TSIM_ERR_TIMEOUT and clears the word.
+ * Process-wide; for tests of the timeout path. */
+TSIM_API int tsim_debug_set_wait_limit(int64_t attempts);
 /* libtsim_debug.so (built with TSIM_DEBUG_BOUNDS): every shared-memory index
  * of the DP and pairwise kernels is checked; one outside its array is
  * replaced by 0 (the kernel carries on, touching nothing outside) and

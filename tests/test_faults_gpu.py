@@ -12,6 +12,12 @@ unless TSIM_COMPAT_NO_EXIT is set.)
 tsim_debug_set_canary fills every scratch reservation with 0xff bytes (NaN
 floats, -1 integers) before a call's kernels run: no result may change, so
 no kernel reads scratch before writing it.
+
+tsim_debug_set_wait_limit(0) makes every bounded device-side wait on a bulk
+copy run out at once (nothing is faulted or hung: the copies complete, the
+kernel just stops waiting for them, reads global memory instead and waits
+for them before it exits).  The synchronising call reports TSIM_ERR_TIMEOUT;
+its context stays usable.
 """
 import numpy as np
 import pytest
@@ -20,6 +26,7 @@ from cudaruntime1_gb300 import datagen as G
 
 pytestmark = pytest.mark.gpu
 OOM = 3
+TIMEOUT = 4
 
 
 def _data(seed, nc=800, nq=3, lo=20, hi=120):
@@ -34,6 +41,7 @@ def lib(tsim):
     yield L
     L.tsim_debug_fail_allocations(0, 0)
     L.tsim_debug_set_canary(0)
+    L.tsim_debug_set_wait_limit(-1)
 
 
 def test_arena_allocation_failure_leaves_context_usable(tsim, lib):
@@ -124,4 +132,28 @@ def test_scratch_canary_changes_nothing(tsim, lib, measure, kw):
             a, b = runs[(0, flags)], runs[(1, flags)]
             assert np.array_equal(a[0], b[0]), (measure, flags)
             assert np.array_equal(a[1].view(np.uint32), b[1].view(np.uint32)), (measure, flags)
+        db.close()
+
+
+def test_bounded_wait_timeout_is_reported(tsim, lib):
+    """The DTW O(length) stage waits (boundedly) for its bulk copies of
+    candidate points -- made for a database larger than L2, here 50,000
+    trajectories of 240-300 points (108 MB).  With the limit at 0 every wait
+    runs out: the call returns TSIM_ERR_TIMEOUT, and the next one (limit
+    restored) returns the same answer as before."""
+    cp, co, qp, qo = _data(41, nc=50000, nq=6, lo=240, hi=300)
+    assert cp.nbytes > 100 * (1 << 20)
+    fl = tsim.api.FLAG_ALWAYS_PRUNE | tsim.api.FLAG_NO_GRAPH
+    with tsim.Context(0) as ctx:
+        db = tsim.Database(ctx, cp, co)
+        want = tsim.knn(ctx, db, qp, qo, "dtw", 10, stats=True, band_pct=10, flags=fl)
+        assert want[2]["pairs_lb2"] > 0  # the stage ran
+        assert lib.tsim_debug_set_wait_limit(0) == 0
+        with pytest.raises(tsim._lib.TsimError) as err:
+            tsim.knn(ctx, db, qp, qo, "dtw", 10, stats=True, band_pct=10, flags=fl)
+        assert err.value.status == TIMEOUT, str(err.value)
+        lib.tsim_debug_set_wait_limit(-1)
+        got = tsim.knn(ctx, db, qp, qo, "dtw", 10, stats=True, band_pct=10, flags=fl)
+        assert np.array_equal(got[0], want[0])
+        assert np.array_equal(got[1].view(np.uint32), want[1].view(np.uint32))
         db.close()
