@@ -390,11 +390,11 @@ __device__ unsigned long long warp_kth(unsigned long long (&key)[SLOTS], int k) 
 
 // k-th best seed value -> threshold (DTW/Frechet: widened; LCSS: count).
 // One warp per query.
+// The seeds' k-th value widened by the FP32 error bound: query q's first
+// pruning threshold (a warp, lane = its lane); the query's list counters are
+// reset with it.
 template <int MEAS>
-__global__ void thresh_kernel(KArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (q >= a.nq) return;
+__device__ void seed_threshold(const KArgs& a, int q, int lane) {
   unsigned long long key[2];
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
@@ -470,11 +470,14 @@ __device__ __forceinline__ void qtable_build(QTable& T, const float2* A, int n, 
 // Bytes of the table buffer of a query of up to max_n rows.
 size_t qtable_bytes(int max_n) { return (size_t)qtable_stride(max_n) * sizeof(float4); }
 
-// one CTA per query: its sparse table and its FP64 prefix sums in global
-// memory (read by the segment bounds of every pair of the query)
+// One CTA per query: its first pruning threshold (warp 0, from the seeds),
+// then its sparse table and, for lock-step Euclidean, its prefix sums in
+// global memory (read by the segment bounds of every pair of the query).
+template <int MEAS>
 __global__ void qtable_global_kernel(KArgs a, int sums) {
   __shared__ double2 part[256];
   const int q = blockIdx.x;
+  if (threadIdx.x < 32) seed_threshold<MEAS>(a, q, threadIdx.x);
   const int n = a.qlen[q];
   if (n <= 0 || n > a.max_qlen) return;
   const float2* A = a.qpts + a.qoff[q];
@@ -1195,6 +1198,7 @@ __global__ void __launch_bounds__(kSelThreads) r1_select_kernel(KArgs a) {
   __shared__ unsigned long long sel[64];
   const int q = blockIdx.x;
   const int ns = (a.cnt2[q] + kSeg - 1) / kSeg;
+  if (threadIdx.x == 0) a.fcnt[q] = 0;  // round 2's list count (refilter_kernel)
   // the segments' M best (seg_select_kernel) hold the query's M best
   block_select_k(a.segkeys + (size_t)q * a.nseg * 64, ns * a.M, a.M, sel, red);
   for (int i = threadIdx.x; i < a.M; i += kSelThreads) {
@@ -1210,11 +1214,10 @@ __global__ void __launch_bounds__(kSelThreads) r1_select_kernel(KArgs a) {
 
 // k-th best of seeds and round 1 -> tightened threshold (never looser).
 // One warp per query.
+// k-th best of seeds and round 1 -> tightened threshold (never looser), for
+// query q (a warp, lane = its lane)
 template <int MEAS>
-__global__ void thresh2_kernel(KArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (q >= a.nq) return;
+__device__ float round1_threshold(const KArgs& a, int q, int lane) {
   unsigned long long key[4];
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
@@ -1233,18 +1236,15 @@ __global__ void thresh2_kernel(KArgs a) {
     }
   }
   const unsigned long long kth = warp_kth(key, a.k);
-  if (lane == 0) {
-    float t = a.thr[q];
-    if (kth != ~0ull && !a.noprune) {
-      const float v = ord2f((unsigned)(kth >> 32));
-      if (MEAS == M_LCSS)
-        t = fmaxf(t, -v);
-      else
-        t = fminf(t, widen(v, gamma_dp(MEAS, a.qlen[q], a.max_clen)));
-    }
-    a.thr2[q] = t;
-    a.fcnt[q] = 0;
+  float t = a.thr[q];
+  if (kth != ~0ull && !a.noprune) {
+    const float v = ord2f((unsigned)(kth >> 32));
+    if (MEAS == M_LCSS)
+      t = fmaxf(t, -v);
+    else
+      t = fminf(t, widen(v, gamma_dp(MEAS, a.qlen[q], a.max_clen)));
   }
+  return t;
 }
 
 // Round 2: the remaining survivors whose bound passes the tightened
@@ -1253,7 +1253,19 @@ template <int MEAS>
 __global__ void refilter_kernel(KArgs a) {
   const int q = blockIdx.y;
   const int N = a.cnt2[q];
-  const float t = a.thr2[q];
+  // every CTA of the query derives the tightened threshold (a warp's
+  // selection over at most 128 values); the first stores it for the later
+  // stages
+  __shared__ float t_sh;
+  if (threadIdx.x < 32) {
+    const float tq = round1_threshold<MEAS>(a, q, threadIdx.x);
+    if (threadIdx.x == 0) {
+      t_sh = tq;
+      if (blockIdx.x == 0) a.thr2[q] = tq;
+    }
+  }
+  __syncthreads();
+  const float t = t_sh;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
     const int c = a.list2[(size_t)q * a.C + e];
     if (c < 0) continue;
@@ -1813,9 +1825,11 @@ int finish_knn(tsim_ctx* ctx, KArgs& a, int dpc, int dp64) {
     launched(ctx, 2);
     stage_end(ctx);
   }
-  stats_kernel<<<1, 256, 0, s>>>(a, ctx->dcounters, MEAS != M_LCSS ? 1 : 0);
-  TSIM_CUDA(cudaGetLastError());
-  launched(ctx);
+  if (ctx->count_funnel) {  // a synchronising request that reports its funnel
+    stats_kernel<<<1, 256, 0, s>>>(a, ctx->dcounters, MEAS != M_LCSS ? 1 : 0);
+    TSIM_CUDA(cudaGetLastError());
+    launched(ctx);
+  }
   return TSIM_OK;
 }
 
@@ -1933,13 +1947,11 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   stage_end(ctx);
 
   stage_begin(ctx, TSIM_STAGE_FILTER);
-  thresh_kernel<MEAS><<<(nq + 3) / 4, 128, 0, s>>>(a);
-  qtable_global_kernel<<<nq, 256, 0, s>>>(a, MEAS == M_EUCLID);  // segment bounds
+  qtable_global_kernel<MEAS><<<nq, 256, 0, s>>>(a, MEAS == M_EUCLID);  // threshold, segment bounds
   if (MEAS == M_LCSS && a.qenv) {
     lcss_env_kernel<<<nq, 256, 0, s>>>(a);
     launched(ctx);
   }
-  launched(ctx);
   compact_kernel<MEAS><<<g1, kChunk, 0, s>>>(a);
   segfilter_kernel<MEAS><<<dim3(std::max(1, std::min(1024, (32 * ctx->num_sms + nq - 1) / nq)), nq),
                            256, 0, s>>>(a);
@@ -1991,7 +2003,6 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   stage_end(ctx);
 
   stage_begin(ctx, TSIM_STAGE_FILTER);
-  thresh2_kernel<MEAS><<<(nq + 3) / 4, 128, 0, s>>>(a);
   refilter_kernel<MEAS><<<dim3(ch, nq), 256, 0, s>>>(a);
   scan_kernel<<<1, 1024, 0, s>>>(a);
   flatten_kernel<<<dim3(ch, nq), 256, 0, s>>>(a);
@@ -2001,7 +2012,7 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
   shape_scan_kernel<<<1, 1024, 0, s>>>(a);
   shape_scatter_kernel<<<sb, 256, 0, s>>>(a);
   TSIM_CUDA(cudaGetLastError());
-  launched(ctx, 7);
+  launched(ctx, 6);
   stage_end(ctx);
 
   stage_begin(ctx, TSIM_STAGE_DP_SURVIVORS);
@@ -2505,6 +2516,7 @@ int knn_request(tsim_ctx* ctx, const tsim_params* p, const tsim_point* d_qpts,
       TSIM_CUDA(cudaStreamWaitEvent(s->stream, ctx->fork_ev, 0));
     }
   }
+  for (tsim_ctx* c : lanes) c->count_funnel = stats != nullptr;
   if (stats)
     for (tsim_ctx* c : lanes)
       TSIM_CUDA(cudaMemsetAsync(c->dcounters + 2, 0, 5 * sizeof(unsigned long long), c->stream));

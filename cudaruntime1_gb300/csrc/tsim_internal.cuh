@@ -81,6 +81,7 @@ struct tsim_ctx {
   double stage_ms[TSIM_STAGE_COUNT] = {};
   int64_t stage_calls[TSIM_STAGE_COUNT] = {};
   unsigned long long* dcounters = nullptr;  // device: [0] DP cells computed, [kStatusSlot] status
+  bool count_funnel = false;  // requests add their pruning funnel to dcounters[2..6]
   // concurrency: a request's queries are split into chunks that run on these
   // child contexts (own stream and arena), forked from and joined back to
   // `stream` with events, so that latency-bound stages of different chunks
