@@ -279,6 +279,7 @@ int ensure_subs(tsim_ctx* ctx, int n) {
     TSIM_TRY(tsim_ctx_create(ctx->device, nullptr, &s));
     s->concurrency = 1;
     s->profiling = ctx->profiling;
+    s->status = ctx->status;  // a chunk's timeouts are its request's
     ctx->subs.push_back(s);
     cudaEvent_t ev;
     TSIM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
@@ -454,6 +455,7 @@ int tsim_ctx_create(int device, void* stream, tsim_ctx** out) {
   cudaEventCreate(&c->ev1);
   e = dev_malloc(reinterpret_cast<void**>(&c->dcounters), 64 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(c->dcounters, 0, 64 * sizeof(unsigned long long));
+  if (e == cudaSuccess) c->status = reinterpret_cast<unsigned*>(c->dcounters + kStatusSlot);
   if (e != cudaSuccess) {
     if (c->owns_stream) cudaStreamDestroy(c->stream);
     delete c;

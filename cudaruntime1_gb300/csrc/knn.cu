@@ -2291,7 +2291,7 @@ int knn(tsim_ctx* ctx, const tsim_params* p, const float2* qpts, const int64_t* 
                (reinterpret_cast<uintptr_t>(db->pts) & 15) == 0)
                   ? (std::min(db->max_len, 512) + 1) & ~1
                   : 0;
-  a.status = reinterpret_cast<unsigned*>(ctx->dcounters + kStatusSlot);
+  a.status = ctx->status;
   a.order = arena_take<int>(ctx, nqC);
   a.shape_cnt = arena_take<int>(ctx, kNumShapes);
   if (!a.shape_cnt) return fail(TSIM_ERR_OUT_OF_MEMORY, "knn scratch carve failed");
@@ -2373,18 +2373,16 @@ int set_wait_limit(long long attempts) {
 }
 
 int take_device_status(tsim_ctx* ctx) {
-  unsigned any = 0;
-  std::vector<tsim_ctx*> all{ctx};
-  all.insert(all.end(), ctx->subs.begin(), ctx->subs.end());
-  for (tsim_ctx* c : all) {
-    if (!c->dcounters) continue;
-    unsigned v = 0;
-    unsigned* w = reinterpret_cast<unsigned*>(c->dcounters + kStatusSlot);
-    TSIM_CUDA(cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost));
-    if (v) TSIM_CUDA(cudaMemset(w, 0, sizeof(v)));
-    any |= v;
-  }
-  if (any & 1u) return fail(TSIM_ERR_TIMEOUT, "a bounded wait on a bulk copy ran out");
+  unsigned v = 0;
+  if (!ctx->status) return TSIM_OK;
+  TSIM_CUDA(cudaMemcpy(&v, ctx->status, sizeof(v), cudaMemcpyDeviceToHost));
+  return status_result(ctx, v);
+}
+
+int status_result(tsim_ctx* ctx, unsigned v) {
+  if (!v) return TSIM_OK;
+  TSIM_CUDA(cudaMemset(ctx->status, 0, sizeof(v)));
+  if (v & 1u) return fail(TSIM_ERR_TIMEOUT, "a bounded wait on a bulk copy ran out");
   return TSIM_OK;
 }
 }  // namespace tsim
@@ -2576,7 +2574,7 @@ extern "C" int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
   const size_t npts = (size_t)h_qoff[nq];
   const size_t in_bytes = tsim::align256(sizeof(tsim_point) * npts) + tsim::align256(8 * (nq + 1));
   const size_t out_bytes = tsim::align256(sizeof(int) * nq * p->k) + tsim::align256(sizeof(float) * nq * p->k);
-  TSIM_TRY(tsim::pinned_reserve(ctx, in_bytes + out_bytes));
+  TSIM_TRY(tsim::pinned_reserve(ctx, in_bytes + out_bytes + 256));
   // device staging lives in a separate allocation (the arena is reset by the knn call)
   if (ctx->hstage_cap < in_bytes + out_bytes) {
     if (ctx->hstage) {
@@ -2601,8 +2599,12 @@ extern "C" int tsim_knn_host(tsim_ctx* ctx, const tsim_params* p, const tsim_poi
                     db, d_ids, d_d, nullptr, stats));
   TSIM_CUDA(cudaMemcpyAsync(hp + in_bytes, dp + in_bytes, out_bytes, cudaMemcpyDeviceToHost,
                             ctx->stream));
+  // the status word rides with the results (no extra round trip)
+  unsigned* h_status = reinterpret_cast<unsigned*>(hp + in_bytes + out_bytes);
+  TSIM_CUDA(cudaMemcpyAsync(h_status, ctx->status, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            ctx->stream));
   TSIM_CUDA(cudaStreamSynchronize(ctx->stream));
-  TSIM_TRY(tsim::take_device_status(ctx));
+  TSIM_TRY(tsim::status_result(ctx, *h_status));
   memcpy(h_ids, hp + in_bytes, sizeof(int) * nq * p->k);
   memcpy(h_dists, hp + in_bytes + tsim::align256(sizeof(int) * nq * p->k), sizeof(float) * nq * p->k);
   return TSIM_OK;

@@ -82,6 +82,7 @@ struct tsim_ctx {
   int64_t stage_calls[TSIM_STAGE_COUNT] = {};
   unsigned long long* dcounters = nullptr;  // device: [0] DP cells computed, [kStatusSlot] status
   bool count_funnel = false;  // requests add their pruning funnel to dcounters[2..6]
+  unsigned* status = nullptr;  // device status word (its own dcounters slot; a chunk context: its parent's)
   // concurrency: a request's queries are split into chunks that run on these
   // child contexts (own stream and arena), forked from and joined back to
   // `stream` with events, so that latency-bound stages of different chunks
@@ -337,9 +338,12 @@ int launch_dp_diag(tsim_ctx* ctx, int kind, int R, const DpArgs& a, int max_m, i
 // whose band holds more than 64 cells per anti-diagonal (or longer than
 // 2048 points, or than max_n x max_m) are left in spill[] (count in *nspill).
 bool wave_kind(int kind);
-// After a synchronisation: TSIM_ERR_TIMEOUT (and the status words cleared)
-// if a kernel of ctx or of its chunk contexts set the timeout bit, else OK.
+// After a synchronisation: TSIM_ERR_TIMEOUT (and the status word cleared) if
+// a kernel of ctx or of its chunk contexts (which share its word) set the
+// timeout bit, else OK.
 int take_device_status(tsim_ctx* ctx);
+// The same for a status word value already read on the host.
+int status_result(tsim_ctx* ctx, unsigned v);
 // Attempts of the bounded waits on bulk copies (< 0: the default); for tests.
 int set_wait_limit(long long attempts);
 int launch_dp_wave(tsim_ctx* ctx, int kind, const DpArgs& a, int max_n, int max_m, bool latency,
