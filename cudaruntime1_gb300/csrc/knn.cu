@@ -2165,7 +2165,8 @@ size_t knn_plan(const tsim_params* p, int nq, int max_qlen, const tsim_db* db, K
                        : p->measure == TSIM_FRECHET ? DP_FRECHET_SQ
                        : p->cost ? DP_DTW_EU : DP_DTW_SQ;
     a.lane_ring = lane_ring_for(kind32, n, m, p->measure == TSIM_DTW ? p->band_pct : -1, p->delta);
-    a.lane_gate = (a.plain || (p->flags & TSIM_FLAG_NO_LANE_DP)) ? 0 : lane_gate_for(kind32, n, m, p->band_pct, p->delta);
+    a.lane_gate = (a.plain || (p->flags & TSIM_FLAG_NO_LANE_DP)) ? 0 : lane_gate_for(kind32, n, m, p->band_pct, p->delta,
+                                         db->ctx ? db->ctx->num_sms : 0);
     a.wave = (a.plain || (p->flags & TSIM_FLAG_NO_WAVE_DP)) ? 0 : 1;
   }
   a.cost = p->cost;

@@ -363,7 +363,7 @@ int lane_sort(tsim_ctx* ctx, const DpArgs& a, int* order, int* counts);
 int lane_sort_buckets();
 // pair count from which a survivor round of pairs up to max_n x max_m runs
 // on a lane per pair (band_pct / delta < 0: none)
-int lane_gate_for(int kind, int max_n, int max_m, int band_pct, int delta);
+int lane_gate_for(int kind, int max_n, int max_m, int band_pct, int delta, int num_sms);
 int lane_ring_for(int kind, int max_n, int max_m, int band_pct, int delta);
 int launch_dp_lane(tsim_ctx* ctx, int kind, const DpArgs& a, int ring, int* spill, int* nspill,
                    int gate = 0);
