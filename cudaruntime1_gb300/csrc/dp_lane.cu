@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(kLaneThreads, 3)
     if (!__any_sync(0xffffffffu, have)) break;
 
     // the pass's rows: points, bands, and the union of the bands
-    float ox[R], oy[R];
+    float2 o[R];  // the rows' points
     int base[R], span[R];  // row k is in its band at step s iff 0 <= s - base[k] <= span[k]
     int ulo = 0, uhi = -1;
     const int k0 = -o0;    // row 0's place in a first pass that starts above it
@@ -169,8 +169,7 @@ __global__ void __launch_bounds__(kLaneThreads, 3)
           h = -1;
         }
       }
-      ox[k] = p.x;
-      oy[k] = p.y;
+      o[k] = p;
       base[k] = l == kEmptyLo ? kEmptyLo : l + k;
       span[k] = l == kEmptyLo ? 0 : h - l;
     }
@@ -214,7 +213,7 @@ __global__ void __launch_bounds__(kLaneThreads, 3)
       for (int k = R - 1; k >= 0; --k) {
         const V up = k > 0 ? L[k > 0 ? k - 1 : 0] : upv;
         const V lf = L[k];
-        V v = P::cell(ox[k], oy[k], cw[k].x, cw[k].y, up, lf, U[k], a.eps);
+        V v = P::cellp(o[k], cw[k], up, lf, U[k], a.eps);
         if (MASK) v = (unsigned)(s - base[k]) <= (unsigned)span[k] ? v : P::masked(lf);
         U[k] = up;
         L[k] = v;

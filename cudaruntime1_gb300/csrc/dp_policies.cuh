@@ -15,6 +15,19 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
   return r;
 }
 
+// q - c per coordinate in one packed instruction (sub.rn.f32x2, sm_100 and
+// later): two round-to-nearest subtractions, the bits of two scalar ones
+__device__ __forceinline__ float2 sub2(float2 q, float2 c) {
+  union {
+    float2 f;
+    unsigned long long u;
+  } a, b, r;
+  a.f = q;
+  b.f = c;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.u) : "l"(a.u), "l"(b.u));
+  return r.f;
+}
+
 // Minimum of three normalised pairs.  A normalised pair's hi is its value
 // rounded to nearest, so pairs with different hi order as their hi parts;
 // among the operands whose hi is the smallest, the smallest lo decides.
@@ -77,6 +90,12 @@ struct PolDtwSq {  // squared cost; FMA allowed, error bounded by the caller
     float c = fmaf(dy, dy, dx * dx);
     return c + min3f(up, lf, dg);
   }
+  // cell() with the points as pairs: the same operations, the two
+  // differences in one packed subtraction
+  __device__ static V cellp(float2 q, float2 p, V up, V lf, V dg, float) {
+    const float2 d = sub2(q, p);
+    return fmaf(d.y, d.y, d.x * d.x) + min3f(up, lf, dg);
+  }
 };
 
 struct PolDtwEu {
@@ -96,6 +115,10 @@ struct PolDtwEu {
     float c = sqrtf(fmaf(dy, dy, dx * dx));
     return c + min3f(up, lf, dg);
   }
+  __device__ static V cellp(float2 q, float2 p, V up, V lf, V dg, float) {
+    const float2 d = sub2(q, p);
+    return sqrtf(fmaf(d.y, d.y, d.x * d.x)) + min3f(up, lf, dg);
+  }
 };
 
 struct PolFrechetSq {  // squared domain; sqrt is applied once at the end
@@ -114,6 +137,10 @@ struct PolFrechetSq {  // squared domain; sqrt is applied once at the end
     float dx = qx - cx, dy = qy - cy;
     float d2 = fmaf(dy, dy, dx * dx);
     return fmaxf(d2, min3f(up, lf, dg));
+  }
+  __device__ static V cellp(float2 q, float2 p, V up, V lf, V dg, float) {
+    const float2 d = sub2(q, p);
+    return fmaxf(fmaf(d.y, d.y, d.x * d.x), min3f(up, lf, dg));
   }
 };
 
@@ -269,6 +296,11 @@ struct PolLcss {
   __device__ static V masked(V lf) { return lf; }
   __device__ static V cell(float qx, float qy, float cx, float cy, V up, V lf, V dg, float eps) {
     bool match = (fabsf(qx - cx) < eps) && (fabsf(qy - cy) < eps);
+    return match ? dg + 1 : max(max(up, lf), dg);
+  }
+  __device__ static V cellp(float2 q, float2 p, V up, V lf, V dg, float eps) {
+    const float2 d = sub2(q, p);
+    const bool match = (fabsf(d.x) < eps) && (fabsf(d.y) < eps);
     return match ? dg + 1 : max(max(up, lf), dg);
   }
 };
