@@ -1310,15 +1310,19 @@ __global__ void flatten_kernel(KArgs a) {
     a.flat[base + e] = make_int2(q, a.list1[(size_t)q * a.C + e]);
 }
 
-// Shape-sorted schedule of the survivor pairs: counting sort by (query
-// length / 16, candidate length / 16), longest first, so that the pairs
-// sharing a warp have similar shapes (a warp runs as long as its longest
-// pair) and the long pairs do not form the tail of the launch.
-constexpr int kShapeBits = 7;  // 128 length buckets of 16 points per side
+// Shape-sorted schedule of the survivor pairs: counting sort by ((query +
+// candidate length) / 32, longer length / 16), longest first, so that the
+// pairs sharing a warp have similar shapes (a warp runs as long as its
+// longest pair) and the pairs with the most anti-diagonals -- a warp-per-pair
+// kernel's steps -- start first instead of forming the launch's tail (the
+// batched workload's survivor round 0.185 -> 0.178 ms against query length
+// first).
+constexpr int kShapeBits = 7;  // 128 buckets per key part: total length / 32, longer length / 16
 constexpr int kNumShapes = 1 << (2 * kShapeBits);
 
 __device__ __forceinline__ int shape_key(int n, int m) {
-  return (min(n >> 4, (1 << kShapeBits) - 1) << kShapeBits) | min(m >> 4, (1 << kShapeBits) - 1);
+  return (min((n + m) >> 5, (1 << kShapeBits) - 1) << kShapeBits) |
+         min(max(n, m) >> 4, (1 << kShapeBits) - 1);
 }
 
 __global__ void shape_hist_kernel(KArgs a) {
