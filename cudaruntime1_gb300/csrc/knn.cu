@@ -628,11 +628,10 @@ __device__ __forceinline__ bool group_any(bool v) {
 // it the row segments are not evaluated.  Called by every lane of a group
 // with the same pair; g is the lane within the group.
 template <int MEAS>
-__device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1, float t, int g) {
+__device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1, float t, int g,
+                           const QTable& T, float4 qb) {
   if (n > a.max_qlen || n < 1 || m < 1) return lb1;
   const float4* sb = a.csegbox + (size_t)c * kSegs;
-  const float4 qb = a.qbox[q];
-  const QTable T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
   if (MEAS == M_EUCLID) {
     // lock-step: column j meets row j only, so segment s (L points) costs at
     // least L times its box's squared distance to the box of the same query
@@ -668,9 +667,9 @@ __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1
       };
       const float ax = gap(f1.x, f0.x, sc.x, qe.x, cb.x, cb.z);
       const float ay = gap(f1.y, f0.y, sc.y, qe.y, cb.y, cb.w);
-      // / L as * (1/L rounded, times 1 - 2^-23 rounded down: below 1/L), no
-      // division sequence
-      const float rl = __fmul_rd(__frcp_rn(L), 0.99999988f);
+      // / L as * (1/L within 2 ulp, times 1 - 2^-21 rounded down: below
+      // 1/L), no division sequence
+      const float rl = __fmul_rd(__fdividef(1.0f, L), 0.99999952f);
       const float cs = __fmul_rd(__fadd_rd(__fmul_rd(ax, ax), __fmul_rd(ay, ay)), rl);
       part = fmaxf(__fmul_rd(L, d), cs);
     }
@@ -858,6 +857,10 @@ __global__ void __launch_bounds__(256) segfilter_kernel(KArgs a) {
   const int n = a.qlen[q];
   const int g = threadIdx.x & (kSegGroup - 1);
   const int per_block = blockDim.x / kSegGroup;  // pairs per block and pass
+  // the query's table view and box, once per thread (not per pair)
+  QTable T{};
+  if (n >= 1 && n <= a.max_qlen) T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
+  const float4 qb = a.qbox[q];
   const int start = blockIdx.x * per_block;
   const int stride = gridDim.x * per_block;
   for (int e0 = start; e0 < cnt; e0 += stride) {  // uniform per block: whole blocks iterate
@@ -867,7 +870,7 @@ __global__ void __launch_bounds__(256) segfilter_kernel(KArgs a) {
     if (e < cnt) {  // uniform per group
       c = a.list2[(size_t)q * a.C + e];
       const float b = a.lb1[(size_t)q * a.C + c];
-      const float sbnd = seg_bound<MEAS>(a, q, c, n, a.clen[c], b, t, g);
+      const float sbnd = seg_bound<MEAS>(a, q, c, n, a.clen[c], b, t, g, T, qb);
       pass = g == 0 && (MEAS == M_LCSS ? (sbnd >= t) : (sbnd <= t));
       if (pass) a.lb1[(size_t)q * a.C + c] = sbnd;
     }
