@@ -629,9 +629,19 @@ __device__ __forceinline__ bool group_any(bool v) {
 // with the same pair; g is the lane within the group.
 template <int MEAS>
 __device__ float seg_bound(const KArgs& a, int q, int c, int n, int m, float lb1, float t, int g,
-                           const QTable& T, float4 qb) {
+                           const QTable& Tq, float4 qbq) {
   if (n > a.max_qlen || n < 1 || m < 1) return lb1;
   const float4* sb = a.csegbox + (size_t)c * kSegs;
+  // lock-step Euclidean takes the query's table view and box from the
+  // caller (read once per thread: 765 -> 712 M instructions per 64-query
+  // chunk); the other measures read them per pair, which keeps their kernels
+  // at 48 registers (62 with them held across the loop)
+  QTable T = Tq;
+  float4 qb = qbq;
+  if (MEAS != M_EUCLID) {
+    qb = a.qbox[q];
+    T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
+  }
   if (MEAS == M_EUCLID) {
     // lock-step: column j meets row j only, so segment s (L points) costs at
     // least L times its box's squared distance to the box of the same query
@@ -857,10 +867,13 @@ __global__ void __launch_bounds__(256) segfilter_kernel(KArgs a) {
   const int n = a.qlen[q];
   const int g = threadIdx.x & (kSegGroup - 1);
   const int per_block = blockDim.x / kSegGroup;  // pairs per block and pass
-  // the query's table view and box, once per thread (not per pair)
+  // lock-step Euclidean: the query's table view and box once per thread
   QTable T{};
-  if (n >= 1 && n <= a.max_qlen) T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
-  const float4 qb = a.qbox[q];
+  float4 qb{};
+  if (MEAS == M_EUCLID) {
+    if (n >= 1 && n <= a.max_qlen) T = qtable_view(a.qtab + (size_t)q * a.tstride, n);
+    qb = a.qbox[q];
+  }
   const int start = blockIdx.x * per_block;
   const int stride = gridDim.x * per_block;
   for (int e0 = start; e0 < cnt; e0 += stride) {  // uniform per block: whole blocks iterate
@@ -883,8 +896,12 @@ __global__ void __launch_bounds__(256) segfilter_kernel(KArgs a) {
 constexpr uint32_t kWaitLimitDefault = 1u << 22;
 __device__ uint32_t g_wait_limit = kWaitLimitDefault;
 
+// At most 48 registers (5 CTAs of 8 warps per SM where shared memory allows):
+// the bulk-copy pipeline's state took it to 64 (4 CTAs), and the batched
+// workload's step ran 1.4 % slower for it; the few spilled values are
+// per-pair state, outside the column loop.
 template <int MEAS>
-__global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
+__global__ void __launch_bounds__(kLb2Warps * 32, 5) lb2_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int q = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
