@@ -896,12 +896,8 @@ __global__ void __launch_bounds__(256) segfilter_kernel(KArgs a) {
 constexpr uint32_t kWaitLimitDefault = 1u << 22;
 __device__ uint32_t g_wait_limit = kWaitLimitDefault;
 
-// At most 48 registers (5 CTAs of 8 warps per SM where shared memory allows):
-// the bulk-copy pipeline's state took it to 64 (4 CTAs), and the batched
-// workload's step ran 1.4 % slower for it; the few spilled values are
-// per-pair state, outside the column loop.
 template <int MEAS>
-__global__ void __launch_bounds__(kLb2Warps * 32, 5) lb2_kernel(KArgs a) {
+__device__ __forceinline__ void lb2_body(const KArgs& a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int q = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1207,6 +1203,20 @@ __global__ void __launch_bounds__(kLb2Warps * 32, 5) lb2_kernel(KArgs a) {
   // no copy may be left running into shared memory the next CTA gets
   drain(0);
   drain(1);
+}
+
+template <int MEAS>
+__global__ void __launch_bounds__(kLb2Warps * 32) lb2_kernel(KArgs a) {
+  lb2_body<MEAS>(a);
+}
+
+// DTW's at most 48 registers (5 CTAs of 8 warps per SM where shared memory
+// allows): the bulk-copy pipeline's state took it to 64 (4 CTAs), and the
+// batched workload's step ran 1.4 % slower for it; the few spilled values are
+// per-pair state, outside the column loop.  The other measures keep the
+// compiler's choice (LCSS spilled in its point loop under the same bound).
+__global__ void __launch_bounds__(kLb2Warps * 32, 5) lb2_dtw_kernel(KArgs a) {
+  lb2_body<M_DTW>(a);
 }
 
 // Round 1: the M best survivors of each query by their O(length) bound
@@ -1993,10 +2003,11 @@ int run_knn(tsim_ctx* ctx, KArgs& a, int max_qlen, int dp32, int dpc, int dp64, 
                        : 0;
   const int ch2 = MEAS == M_LCSS ? std::max(1, std::min(65535, (32 * ctx->num_sms + nq - 1) / nq))
                                  : ch;
+  auto lb2 = MEAS == M_DTW ? lb2_dtw_kernel : lb2_kernel<MEAS>;
   if (lb2_smem > 48 * 1024)
-    TSIM_CUDA(cudaFuncSetAttribute(lb2_kernel<MEAS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    TSIM_CUDA(cudaFuncSetAttribute(lb2, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)lb2_smem));
-  lb2_kernel<MEAS><<<dim3(ch2, nq), kLb2Warps * 32, lb2_smem, s>>>(a);
+  lb2<<<dim3(ch2, nq), kLb2Warps * 32, lb2_smem, s>>>(a);
   seg_select_kernel<MEAS, 0><<<dim3(a.nseg, nq), kSelThreads, 0, s>>>(a, a.M);
   r1_select_kernel<MEAS><<<nq, kSelThreads, 0, s>>>(a);
   TSIM_CUDA(cudaGetLastError());
