@@ -201,7 +201,11 @@ TSIM_API int tsim_debug_bounds_violations(int64_t* count, int64_t* first);
 TSIM_API int tsim_db_create(tsim_ctx* ctx, const tsim_point* host_pts, const int64_t* host_off,
                             int count, tsim_db** out);
 /* Wraps device-resident points/offsets (not copied, caller keeps them alive).
- * max_len is advisory: the longest trajectory is taken from the offsets. */
+ * max_len is advisory: the longest trajectory is taken from the offsets.
+ * On a database larger than L2, DTW's LB_Keogh stage fetches candidate
+ * points by bulk copy when dev_pts is 16-byte aligned (cudaMalloc's 256-byte
+ * alignment is; an offset into a larger allocation may not be), else with
+ * ordinary loads: the results are the same either way. */
 TSIM_API int tsim_db_wrap_device(tsim_ctx* ctx, const tsim_point* dev_pts,
                                  const int64_t* dev_off, int count, int max_len, tsim_db** out);
 TSIM_API int tsim_db_destroy(tsim_db* db);
