@@ -64,6 +64,7 @@ def test_loads_and_reports_errors_without_gpu(tsim):
     assert L.tsim_version() >= 10000
     assert L.tsim_status_string(0) == b"ok"
     assert L.tsim_status_string(5) == b"unsupported"
+    assert L.tsim_status_string(4) == b"bounded wait timed out"
     if torch.cuda.is_available():
         pytest.skip("a GPU is present: covered by the gpu tests")
     h = C.c_void_p()
@@ -73,6 +74,9 @@ def test_loads_and_reports_errors_without_gpu(tsim):
     # null arguments are rejected before any CUDA call
     assert L.tsim_knn(None, None, None, None, 0, 0, None, None, None, None, None) == 1
     assert b"NULL" in L.tsim_last_error()
+    # the device-side wait limit lives in device memory: without a GPU the
+    # setter reports the CUDA error instead of crashing
+    assert L.tsim_debug_set_wait_limit(0) != 0
 
 
 def test_python_api_raises_on_bad_input(tsim):
