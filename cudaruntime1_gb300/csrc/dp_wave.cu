@@ -2,7 +2,9 @@
 // a warp per (query, candidate) pair, lane p holding the p-th live cell of
 // the current anti-diagonal (R cells per lane for anti-diagonals of up to
 // 32 R live cells).  The latency form of the DP: a round of few pairs lasts
-// as long as its longest pair, whose n+m-1 anti-diagonals are its steps.
+// as long as its longest pair, whose n+m-1 anti-diagonals are its steps --
+// and, with the query read through L1 and the remaining columns' LB_Keogh
+// bound in its abandon test, DTW's survivor round.
 //
 // Anti-diagonal t = i + j holds the band's cells i in [ilo(t), ihi(t)]
 // (|i(m-1) - j(n-1)| <= W inside the matrix), L(t) of them.  From one
@@ -24,14 +26,17 @@
 // two steps back, which lane 0 keeps.  Below the last position lies +inf.
 //
 // Per step a lane does: one shuffle, R cells, and the costs of the next
-// step's R cells from the pair's points staged in shared memory (padded so
-// that positions past L read inside the buffers and are masked).  The
-// geometry (ilo, L) of every anti-diagonal is a table built per pair from
-// exact integer ramps.  Steps run in straight-line blocks of 16.  Early
-// abandon: every warping path crosses one of any two consecutive
-// anti-diagonals and values never decrease along a path, so after every
-// block the minimum over its last two anti-diagonals is compared with the
-// query's threshold.
+// step's R cells from the pair's points (the candidate staged in shared
+// memory, padded so that positions past L read inside the buffer and are
+// masked; the query staged too in the latency rounds, else read through L1
+// with its index clamped).  The geometry (ilo, L) of the anti-diagonals
+// comes from exact integer ramps, 32 steps at a time, one per lane, read by
+// a shuffle.  Steps run in straight-line blocks of 16; R (1 or 2) is chosen
+// per pair inside one launch.  Early abandon: every warping path crosses one
+// of any two consecutive anti-diagonals and values never decrease along a
+// path, so after every block the minimum over its last two anti-diagonals
+// (plus, in the survivor round, the bound of the columns after them) is
+// compared with the query's threshold.
 //
 // Reference kernels replaced: dtw_refine_kernel (CudaRuntime1/dtw.cu:41-96)
 // and frechet_refine_kernel_m (CudaRuntime1/frechet.cu:44-117): a CTA per
