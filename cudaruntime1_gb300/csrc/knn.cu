@@ -1,5 +1,6 @@
 // knn.cu -- exact k-nearest-neighbour search over a device-resident
-// trajectory database for DTW, LCSS and discrete Frechet.
+// trajectory database for DTW, LCSS, discrete Frechet, symmetric Hausdorff
+// and lock-step Euclidean.
 //
 // Stages (all on one stream, fixed launch shapes, data-dependent counts kept
 // on the device so the whole sequence can be captured in a CUDA graph):
@@ -8,16 +9,21 @@
 //                      CTA also keeps its chunk's best few candidates; once
 //                      B has set the threshold, compact_kernel lists the
 //                      pairs the O(1) bound keeps and segfilter_kernel
-//                      bounds them by 8 column segments per candidate;
+//                      bounds them by 8 column segments per candidate and
+//                      32 query row segments (a group of 8 lanes a pair);
 //   B  seeds           the S best chunk candidates per query are refined
 //                      exactly; the k-th best refined value, widened by the
 //                      FP32 error bound, is the query's pruning threshold;
 //   C  lb2_kernel      the listed pairs get the O(length) bound (banded
 //                      LB_Keogh from the query's sparse table in global
-//                      memory for DTW, box distances for Frechet, the
-//                      windowed eps-box count for LCSS);
-//   D  DP              the survivors run the wavefront DP with early
-//                      abandon against the threshold;
+//                      memory for DTW, its candidates fetched by bulk copy
+//                      on databases larger than L2; box distances for
+//                      Frechet and Hausdorff, the windowed eps-box count for
+//                      LCSS; lock-step Euclidean passes the list on);
+//   D  DP              round 1 (the best survivors by bound) tightens the
+//                      threshold, then the remaining survivors run the
+//                      wavefront DP (or the pairwise distance) with early
+//                      abandon against it;
 //   E  final           the k-th best FP32 value fixes the re-score set (all
 //                      pairs within the FP32 error bound of it); the set is
 //                      re-computed with compensated (hi, lo) FP32 arithmetic,
